@@ -1,0 +1,328 @@
+"""cybermeshgenerator_gb300 — GB300-native voxelization for CyberMeshGenerator.
+
+The module mirrors the reference binding's surface
+(bindings/python/src/cybermesh/__init__.py): ``PLC``, ``voxelize(plc,
+resolution, mode, pad) -> VoxelGrid`` with the same argument meaning, array
+layout ((nx, ny, nz), C-order per axis after the reference's transpose) and
+error behaviour (``RuntimeError`` carrying the C error text, ``ValueError`` /
+``TypeError`` for bad Python arguments). Underneath, libcmg_c.so runs the
+occupancy and signed-distance kernels on the GPU.
+
+Additions beyond the reference: ``voxelize_ex`` (explicit grid, FP64 and mixed
+precision distance fields, exact predicates, nearest-feature checkpoints, run
+statistics), ``Batch`` (many meshes in one pipeline, optionally replayed as a
+CUDA graph) and, in ``cybermeshgenerator_gb300.torch_sdf``, a differentiable
+signed distance field.
+
+    import numpy as np, cybermeshgenerator_gb300 as cm
+    plc = cm.PLC().add_points(points)
+    for tri in triangles:
+        plc.add_facet(tri)
+    vg = cm.voxelize(plc, resolution=64, mode="sdf")
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as _L
+
+_clib = _L.Lazy()
+
+OUT_OCCUPANCY, OUT_SDF_F32, OUT_SDF_F64, OUT_NEAREST, OUT_ERROR_BOUND = 1, 2, 4, 8, 16
+PREC_FP64, PREC_MIXED = 0, 1
+PRED_COMPAT, PRED_EXACT = 0, 1
+
+
+def _check(status: int, err) -> None:
+    if status != 0:
+        raise RuntimeError(err.value.decode() or f"cmg error {status}")
+
+
+class PLC:
+    """A piecewise-linear complex: points and polygon facets (the voxelizer reads
+    the facets' fan triangulation)."""
+
+    def __init__(self, _handle: Optional[int] = None) -> None:
+        self._handle = _handle if _handle is not None else _clib.cmg_plc_create()
+        if not self._handle:
+            raise MemoryError("cmg_plc_create failed")
+
+    @property
+    def num_points(self) -> int:
+        return int(_clib.cmg_plc_num_points(self._handle))
+
+    @property
+    def points(self) -> np.ndarray:
+        n = self.num_points
+        if not n:
+            return np.empty((0, 3), dtype=np.float64)
+        return np.ctypeslib.as_array(_clib.cmg_plc_points(self._handle), (n, 3)).astype(np.float64).copy()
+
+    @property
+    def triangles(self) -> np.ndarray:
+        m = int(_clib.cmg_plc_num_triangles(self._handle))
+        if not m:
+            return np.empty((0, 3), dtype=np.int32)
+        return np.ctypeslib.as_array(_clib.cmg_plc_triangles(self._handle), (m, 3)).astype(np.int32).copy()
+
+    def add_points(self, points) -> "PLC":
+        """Set the vertex cloud from an (N, 3) array (replaces any previous set)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        if pts.ndim != 2 or pts.shape[1] != 3:
+            raise ValueError("points must be an (N, 3) array")
+        _check(_clib.cmg_plc_set_points(self._handle, pts.ctypes.data_as(_L.c_double_p),
+                                       pts.shape[0]), ctypes.create_string_buffer(1))
+        return self
+
+    def add_facet(self, vertex_indices: Sequence[int], marker: int = 0) -> "PLC":
+        """Append a one-polygon facet (a triangle when three indices)."""
+        idx = np.ascontiguousarray(vertex_indices, dtype=np.int32).ravel()
+        if idx.size < 3:
+            raise ValueError("a facet needs at least 3 vertex indices")
+        _check(_clib.cmg_plc_add_facet(self._handle, idx.ctypes.data_as(_L.c_int_p), idx.size,
+                                      int(marker)), ctypes.create_string_buffer(1))
+        return self
+
+    def add_facets(self, triangles) -> "PLC":
+        """Append every row of an (M, k) index array as a facet."""
+        for row in np.asarray(triangles, dtype=np.int32):
+            self.add_facet(row)
+        return self
+
+    def add_hole(self, x: float, y: float, z: float) -> "PLC":
+        _check(_clib.cmg_plc_add_hole(self._handle, x, y, z), ctypes.create_string_buffer(1))
+        return self
+
+    def add_region(self, x: float, y: float, z: float, attribute: float = 0.0,
+                   max_volume: float = -1.0) -> "PLC":
+        _check(_clib.cmg_plc_add_region(self._handle, x, y, z, attribute, max_volume),
+               ctypes.create_string_buffer(1))
+        return self
+
+    @classmethod
+    def from_arrays(cls, points, triangles) -> "PLC":
+        return cls().add_points(points).add_facets(triangles)
+
+    def __del__(self) -> None:
+        h = getattr(self, "_handle", None)
+        if h:
+            _clib.cmg_plc_destroy(h)
+            self._handle = None
+
+
+@dataclass
+class VoxelGrid:
+    """A regular grid from :func:`voxelize`: ``grid`` is (nx, ny, nz), uint8
+    occupancy (1 inside) or float32 signed distance (negative inside); ``origin``
+    is the centre of cell (0, 0, 0) and ``spacing`` the cubic cell size."""
+
+    grid: np.ndarray
+    origin: np.ndarray
+    spacing: float
+    mode: str
+
+    @property
+    def dims(self) -> tuple:
+        return tuple(int(d) for d in self.grid.shape)
+
+
+_VOXEL_MODES = {"occupancy": 0, "sdf": 1}
+
+
+def _mode(mode):
+    if isinstance(mode, str):
+        try:
+            return _VOXEL_MODES[mode], mode
+        except KeyError:
+            raise ValueError(f"mode must be one of {sorted(_VOXEL_MODES)} or 0/1")
+    code = int(mode)
+    if code not in (0, 1):
+        raise ValueError("mode must be 'occupancy'/0 or 'sdf'/1")
+    return code, "occupancy" if code == 0 else "sdf"
+
+
+def _to_xyz(flat: np.ndarray, dims) -> np.ndarray:
+    nx, ny, nz = dims
+    # cells are laid out as idx = (k*ny + j)*nx + i: C order for (nz, ny, nx)
+    return flat.reshape((nz, ny, nx)).transpose(2, 1, 0).copy()
+
+
+def voxelize(plc: PLC, resolution: int = 64, mode="occupancy", pad: int = 1) -> VoxelGrid:
+    """Voxelize a PLC (reference semantics: resolution cells on the longest axis,
+    pad margin cells; "occupancy"/0 -> uint8, "sdf"/1 -> float32)."""
+    if not isinstance(plc, PLC):
+        raise TypeError("plc must be a PLC")
+    code, name = _mode(mode)
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(256)
+    _check(_clib.cmg_plc_voxelize(plc._handle, int(resolution), code, int(pad), ctypes.byref(out),
+                                 err, 256), err)
+    h = out.value
+    try:
+        dims, origin, spacing = _geometry(h)
+        n = dims[0] * dims[1] * dims[2]
+        if code == 0:
+            flat = np.ctypeslib.as_array(_clib.cmg_voxels_occupancy(h), (n,)).astype(np.uint8)
+        else:
+            flat = np.ctypeslib.as_array(_clib.cmg_voxels_distance(h), (n,)).astype(np.float32)
+        grid = _to_xyz(flat, dims)
+    finally:
+        _clib.cmg_voxels_destroy(h)
+    return VoxelGrid(grid=grid, origin=origin, spacing=spacing, mode=name)
+
+
+def _geometry(h):
+    nx, ny, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _clib.cmg_voxels_dims(h, ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nz))
+    ox, oy, oz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _clib.cmg_voxels_origin(h, ctypes.byref(ox), ctypes.byref(oy), ctypes.byref(oz))
+    return ((nx.value, ny.value, nz.value), np.array([ox.value, oy.value, oz.value]),
+            float(_clib.cmg_voxels_spacing(h)))
+
+
+@dataclass
+class VoxelResult:
+    """Outputs of :func:`voxelize_ex`, flat in the C layout idx = (k*ny + j)*nx + i
+    (``as_xyz`` reshapes to (nx, ny, nz))."""
+
+    dims: tuple
+    origin: np.ndarray
+    corner: np.ndarray
+    spacing: float
+    occupancy: Optional[np.ndarray] = None
+    sdf32: Optional[np.ndarray] = None
+    sdf64: Optional[np.ndarray] = None
+    nearest_triangle: Optional[np.ndarray] = None
+    nearest_region: Optional[np.ndarray] = None
+    error_bound: Optional[np.ndarray] = None
+    stats: Dict[str, float] = field(default_factory=dict)
+
+    def as_xyz(self, a: np.ndarray) -> np.ndarray:
+        return _to_xyz(a, self.dims)
+
+
+def make_opts(resolution: int = 64, pad: int = 1, outputs: int = OUT_OCCUPANCY,
+              precision: int = PREC_FP64, predicates: int = PRED_COMPAT, grid=None,
+              band: float = 1.0, brick: int = 0, autotune: bool = False) -> _L.VoxelOpts:
+    o = _L.VoxelOpts()
+    _clib.cmg_voxel_opts_init(ctypes.byref(o))
+    o.resolution, o.pad, o.outputs = int(resolution), int(pad), int(outputs)
+    o.precision, o.predicates = int(precision), int(predicates)
+    o.band, o.brick, o.autotune = float(band), int(brick), int(bool(autotune))
+    if grid is not None:
+        corner, spacing, dims = grid
+        o.explicit_grid = 1
+        for a in range(3):
+            o.corner[a] = float(corner[a])
+            o.dims[a] = int(dims[a])
+        o.spacing = float(spacing)
+    return o
+
+
+def _result_from_handle(h) -> VoxelResult:
+    dims, origin, spacing = _geometry(h)
+    cx, cy, cz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _clib.cmg_voxels_corner(h, ctypes.byref(cx), ctypes.byref(cy), ctypes.byref(cz))
+    n = dims[0] * dims[1] * dims[2]
+
+    def grab(fn, dtype):
+        p = fn(h)
+        return np.ctypeslib.as_array(p, (n,)).astype(dtype).copy() if p else None
+
+    st = _L.VoxelStats()
+    _clib.cmg_voxels_stats(h, ctypes.byref(st))
+    return VoxelResult(
+        dims=dims, origin=origin, corner=np.array([cx.value, cy.value, cz.value]), spacing=spacing,
+        occupancy=grab(_clib.cmg_voxels_occupancy, np.uint8),
+        sdf32=grab(_clib.cmg_voxels_distance, np.float32),
+        sdf64=grab(_clib.cmg_voxels_distance_f64, np.float64),
+        nearest_triangle=grab(_clib.cmg_voxels_nearest_triangle, np.int32),
+        nearest_region=grab(_clib.cmg_voxels_nearest_region, np.uint8),
+        error_bound=grab(_clib.cmg_voxels_error_bound, np.float32),
+        stats=st.as_dict())
+
+
+def voxelize_ex(plc: PLC, **kw) -> VoxelResult:
+    """Voxelize with explicit options (see :func:`make_opts`)."""
+    if not isinstance(plc, PLC):
+        raise TypeError("plc must be a PLC")
+    o = make_opts(**kw)
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    _check(_clib.cmg_plc_voxelize_ex(plc._handle, ctypes.byref(o), ctypes.byref(out), err, 512), err)
+    try:
+        return _result_from_handle(out.value)
+    finally:
+        _clib.cmg_voxels_destroy(out.value)
+
+
+class Batch:
+    """Many PLCs voxelized by one pipeline (occupancy and/or SDF), resident on the
+    GPU; ``run(graph=True)`` replays a captured CUDA graph after the first pass."""
+
+    def __init__(self, plcs: Sequence[PLC], resolutions=None, pads=None, **kw):
+        self._plcs = list(plcs)  # keep the handles alive
+        n = len(self._plcs)
+        res = np.ascontiguousarray(resolutions if resolutions is not None else [64] * n, dtype=np.int32)
+        pad = np.ascontiguousarray(pads if pads is not None else [1] * n, dtype=np.int32)
+        arr = (ctypes.c_void_p * n)(*[p._handle for p in self._plcs])
+        o = make_opts(**kw)
+        out = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_create(arr, res.ctypes.data_as(_L.c_int_p),
+                                     pad.ctypes.data_as(_L.c_int_p), n, ctypes.byref(o),
+                                     ctypes.byref(out), err, 512), err)
+        self._h = out.value
+
+    def __len__(self) -> int:
+        return int(_clib.cmg_batch_size(self._h))
+
+    @property
+    def cells(self) -> int:
+        return int(_clib.cmg_batch_cells(self._h))
+
+    def run(self, graph: bool = False) -> "Batch":
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_run(self._h, int(graph), err, 512), err)
+        return self
+
+    def sync(self) -> "Batch":
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_sync(self._h, err, 512), err)
+        return self
+
+    def result(self, i: int) -> VoxelResult:
+        out = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_get(self._h, int(i), ctypes.byref(out), err, 512), err)
+        try:
+            return _result_from_handle(out.value)
+        finally:
+            _clib.cmg_voxels_destroy(out.value)
+
+    def __del__(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            _clib.cmg_batch_destroy(h)
+            self._h = None
+
+
+def version() -> str:
+    return _clib.cmg_version().decode()
+
+
+def gpu_version() -> str:
+    return _clib.cmg_gpu_version().decode()
+
+
+def library_path() -> str:
+    return _L.library_path()
+
+
+__all__ = ["PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
+           "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
+           "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT"]

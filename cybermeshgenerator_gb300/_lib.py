@@ -1,0 +1,145 @@
+"""Loading and binding libcmg_c.so (the GPU voxelization library).
+
+The library is looked up as the reference binding does it
+(bindings/python/src/cybermesh/__init__.py:45-56): the ``CMG_C_LIB``
+environment variable first, then the copy built in this package directory.
+There is no fallback: if the library is missing, importing fails with the build
+command to run.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+IN_TREE = os.path.join(HERE, "libcmg_c.so")
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int_p = ctypes.POINTER(ctypes.c_int)
+c_void_pp = ctypes.POINTER(ctypes.c_void_p)
+c_ubyte_p = ctypes.POINTER(ctypes.c_ubyte)
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+
+
+class VoxelOpts(ctypes.Structure):
+    """Mirror of ``cmg_voxel_opts`` (include/cmg_c/cmg_gpu.h)."""
+    _fields_ = [("resolution", ctypes.c_int), ("pad", ctypes.c_int), ("mode", ctypes.c_int),
+                ("outputs", ctypes.c_int), ("precision", ctypes.c_int),
+                ("predicates", ctypes.c_int), ("explicit_grid", ctypes.c_int),
+                ("corner", ctypes.c_double * 3), ("spacing", ctypes.c_double),
+                ("dims", ctypes.c_int * 3), ("band", ctypes.c_double), ("brick", ctypes.c_int),
+                ("autotune", ctypes.c_int)]
+
+
+class VoxelStats(ctypes.Structure):
+    """Mirror of ``cmg_voxel_stats`` (include/cmg_c/cmg_gpu.h)."""
+    _fields_ = [("cells", ctypes.c_int64), ("flagged_columns", ctypes.c_int64),
+                ("nudged_columns", ctypes.c_int64), ("exhausted_columns", ctypes.c_int64),
+                ("exact_calls", ctypes.c_int64), ("bucket_entries", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("evaluations", ctypes.c_int64),
+                ("fp64_evaluations", ctypes.c_int64), ("band_cells", ctypes.c_int64),
+                ("brick", ctypes.c_int), ("max_error_bound", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def library_path() -> str:
+    return os.environ.get("CMG_C_LIB") or IN_TREE
+
+
+def _bind(lib: ctypes.CDLL) -> None:
+    V, I, D, S, Z = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t
+
+    def sig(name, res, args):
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+    # reference surface (bindings/python/src/cybermesh/__init__.py:58-159)
+    sig("cmg_plc_create", V, [])
+    sig("cmg_plc_destroy", None, [V])
+    sig("cmg_options_create", V, [])
+    sig("cmg_options_destroy", None, [V])
+    sig("cmg_mesh_destroy", None, [V])
+    sig("cmg_plc_set_points", I, [V, c_double_p, Z])
+    sig("cmg_plc_add_facet", I, [V, c_int_p, Z, I])
+    sig("cmg_plc_add_hole", I, [V, D, D, D])
+    sig("cmg_plc_add_region", I, [V, D, D, D, D, D])
+    sig("cmg_options_set_plc", I, [V, I])
+    sig("cmg_options_set_max_volume", I, [V, D])
+    sig("cmg_options_set_quality", I, [V, D, D])
+    sig("cmg_options_set_preserve_edges", I, [V, I])
+    sig("cmg_options_from_switches", I, [V, S, S, Z])
+    sig("cmg_tetrahedralize", I, [V, V, c_void_pp, S, Z])
+    sig("cmg_delaunay", I, [c_double_p, Z, V, c_void_pp, S, Z])
+    for n in ("cmg_mesh_num_points", "cmg_mesh_num_tets", "cmg_mesh_num_faces"):
+        sig(n, Z, [V])
+    sig("cmg_mesh_points", c_double_p, [V])
+    sig("cmg_mesh_tets", c_int_p, [V])
+    sig("cmg_mesh_faces", c_int_p, [V])
+    sig("cmg_mesh_tet_markers", c_int_p, [V])
+    sig("cmg_mesh_face_markers", c_int_p, [V])
+    for n in ("cmg_read_plc", "cmg_read_points", "cmg_read_mesh"):
+        sig(n, I, [S, c_void_pp, S, Z])
+    sig("cmg_write_mesh", I, [S, V, S, Z])
+    sig("cmg_write_plc", I, [S, V, S, Z])
+    sig("cmg_plc_num_points", Z, [V])
+    sig("cmg_plc_points", c_double_p, [V])
+    sig("cmg_plc_num_triangles", Z, [V])
+    sig("cmg_plc_triangles", c_int_p, [V])
+    sig("cmg_plc_simplify", I, [V, I, c_void_pp, S, Z])
+    sig("cmg_plc_voxelize", I, [V, I, I, I, c_void_pp, S, Z])
+    sig("cmg_voxels_destroy", None, [V])
+    sig("cmg_voxels_dims", None, [V, c_int_p, c_int_p, c_int_p])
+    sig("cmg_voxels_origin", None, [V, c_double_p, c_double_p, c_double_p])
+    sig("cmg_voxels_spacing", D, [V])
+    sig("cmg_voxels_occupancy", c_ubyte_p, [V])
+    sig("cmg_voxels_distance", c_float_p, [V])
+    sig("cmg_version", S, [])
+    # GPU additions (include/cmg_c/cmg_gpu.h)
+    sig("cmg_voxel_opts_init", None, [ctypes.POINTER(VoxelOpts)])
+    sig("cmg_plc_voxelize_ex", I, [V, ctypes.POINTER(VoxelOpts), c_void_pp, S, Z])
+    sig("cmg_voxels_distance_f64", c_double_p, [V])
+    sig("cmg_voxels_nearest_triangle", c_int_p, [V])
+    sig("cmg_voxels_nearest_region", c_ubyte_p, [V])
+    sig("cmg_voxels_error_bound", c_float_p, [V])
+    sig("cmg_voxels_corner", None, [V, c_double_p, c_double_p, c_double_p])
+    sig("cmg_voxels_stats", None, [V, ctypes.POINTER(VoxelStats)])
+    sig("cmg_batch_create", I, [ctypes.POINTER(V), c_int_p, c_int_p, I,
+                                ctypes.POINTER(VoxelOpts), c_void_pp, S, Z])
+    sig("cmg_batch_run", I, [V, I, S, Z])
+    sig("cmg_batch_sync", I, [V, S, Z])
+    sig("cmg_batch_get", I, [V, I, c_void_pp, S, Z])
+    sig("cmg_batch_size", I, [V])
+    sig("cmg_batch_cells", ctypes.c_int64, [V])
+    sig("cmg_batch_destroy", None, [V])
+    sig("cmg_gpu_version", S, [])
+
+
+_LIB = None
+
+
+class Lazy:
+    """Attribute access loads and binds the library on first use, so that the
+    package (and its build and workload modules) import without it; a call then
+    fails loudly if the library is missing."""
+
+    def __getattr__(self, name):
+        return getattr(load(), name)
+
+
+def load() -> ctypes.CDLL:
+    """The bound library (loaded once)."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise ImportError(
+                f"libcmg_c.so not found at {path}; build it with "
+                "`python -m cybermeshgenerator_gb300.build` (or set CMG_C_LIB)")
+        lib = ctypes.CDLL(path)
+        _bind(lib)
+        _LIB = lib
+    return _LIB

@@ -1,0 +1,616 @@
+// cmg_c.cpp — the C ABI of libcmg_c.so (include/cmg_c/cmg_c.h, cmg_gpu.h).
+//
+// Handle, status and error-buffer conventions follow the reference's C shim
+// (bindings/c/src/cmg_c.cpp): NULL handles and arguments answer
+// CMG_ERR_INVALID_INPUT, core validation errors carry the core's message, and
+// every C++ exception is caught at the boundary as CMG_ERR_INTERNAL. The
+// voxelization itself runs on the GPU (engine.h); there is no CPU path, and a
+// host without a CUDA device gets CMG_ERR_INTERNAL with the CUDA error text.
+//
+// Compile with -ffp-contract=off: make_grid must round like the reference.
+#include "../../include/cmg_c/cmg_c.h"
+#include "../../include/cmg_c/cmg_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cmg_util.h"
+#include "engine.h"
+
+namespace {
+
+using cmg::gpu::GridDesc;
+
+struct Region {
+    double x, y, z, attribute, max_volume;
+};
+
+}  // namespace
+
+struct cmg_plc {
+    std::vector<double> points;            // 3 per point
+    std::vector<std::vector<int>> facets;  // one polygon per facet
+    std::vector<int> markers;
+    std::vector<double> holes;
+    std::vector<Region> regions;
+    std::vector<double> pts_cache;
+    std::vector<int> tri_cache;
+};
+
+struct cmg_options {
+    int plc = 0;
+    double max_volume = -1.0;
+    double radius_edge = 0.0, min_dihedral = 0.0;
+    int quality = 0;
+    int preserve_edges = 0;
+};
+
+struct cmg_mesh {};
+
+struct cmg_voxels {
+    double corner[3] = {0, 0, 0};
+    double origin[3] = {0, 0, 0};
+    double spacing = 0;
+    int nx = 0, ny = 0, nz = 0;
+    cmg::gpu::HostResult r;
+    cmg_voxel_stats stats{};
+};
+
+struct cmg_batch {
+    std::unique_ptr<cmg::gpu::Batch> batch;
+    std::vector<GridDesc> grids;
+    int outputs = 0;
+    bool ran = false;
+};
+
+namespace {
+
+void set_err(char* buf, size_t len, const std::string& msg) {
+    if (buf && len) {
+        std::strncpy(buf, msg.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+}
+
+// The GPU entry points are serialised per process (one workspace per device).
+std::mutex& gpu_mutex() {
+    static std::mutex m;
+    return m;
+}
+
+cudaStream_t gpu_stream() {
+    static std::mutex mu;
+    static int dev_of_stream = -1;
+    static cudaStream_t st = nullptr;
+    int dev = 0;
+    CMG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    if (!st || dev != dev_of_stream) {
+        CMG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        dev_of_stream = dev;
+    }
+    return st;
+}
+
+// Fan triangulation (v0, v[i-1], v[i]) of every facet polygon
+// (src/voxelize/voxelize.cpp:29-38).
+std::vector<int> fan(const cmg_plc& p) {
+    std::vector<int> t;
+    for (const auto& f : p.facets)
+        for (size_t i = 2; i < f.size(); ++i) {
+            t.push_back(f[0]);
+            t.push_back(f[i - 1]);
+            t.push_back(f[i]);
+        }
+    return t;
+}
+
+// make_grid (src/voxelize/voxelize.cpp:52-74), same operations in the same order.
+bool make_grid(const std::vector<double>& pts, int resolution, int pad, GridDesc& g) {
+    const size_t n = pts.size() / 3;
+    double lo[3] = {pts[0], pts[1], pts[2]}, hi[3] = {pts[0], pts[1], pts[2]};
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            double v = pts[3 * i + a];
+            if (v < lo[a]) lo[a] = v;
+            if (v > hi[a]) hi[a] = v;
+        }
+    double ext = 0;
+    for (int a = 0; a < 3; ++a) ext = std::max(ext, hi[a] - lo[a]);
+    g = GridDesc{};
+    g.h = ext / resolution;
+    if (!(g.h > 0)) return false;
+    int* dims[3] = {&g.nx, &g.ny, &g.nz};
+    for (int a = 0; a < 3; ++a) {
+        double e = hi[a] - lo[a];
+        int core = std::max(1, static_cast<int>(std::ceil(e / g.h)));
+        double covered = core * g.h;
+        g.corner[a] = lo[a] - (covered - e) / 2.0 - pad * g.h;
+        *dims[a] = core + 2 * pad;
+    }
+    return true;
+}
+
+struct CoreError {
+    cmg_status code;
+    std::string msg;
+};
+
+// Validation of voxelize (src/voxelize/voxelize.cpp:362-379) plus index checks
+// (an out-of-range facet index is undefined behaviour in the reference; here it
+// is an InvalidInput error, since the GPU must never read outside its inputs).
+std::vector<int> checked_triangles(const cmg_plc& p) {
+    if (p.points.empty()) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no points"};
+    std::vector<int> t = fan(p);
+    if (t.empty())
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no boundary triangles"};
+    const int64_t np = static_cast<int64_t>(p.points.size() / 3);
+    for (int v : t)
+        if (v < 0 || v >= np)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: facet vertex index out of range"};
+    return t;
+}
+
+void check_grid_size(const GridDesc& g) {
+    if (g.nx <= 0 || g.ny <= 0 || g.nz <= 0)
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: grid has no cells (pad too negative)"};
+}
+
+cmg::gpu::VoxOpts to_vox(const cmg_voxel_opts& o, int outputs) {
+    cmg::gpu::VoxOpts v;
+    v.predicates = o.predicates == CMG_PRED_EXACT ? cmg::gpu::kPredExact : cmg::gpu::kPredCompat;
+    v.precision = o.precision == CMG_PREC_MIXED ? cmg::gpu::kPrecMixed : cmg::gpu::kPrecFP64;
+    v.brick = o.brick;
+    v.band = static_cast<float>(o.band);
+    v.want_occ = outputs & CMG_OUT_OCCUPANCY;
+    v.want_sdf32 = outputs & CMG_OUT_SDF_F32;
+    v.want_sdf64 = outputs & CMG_OUT_SDF_F64;
+    v.want_near = outputs & CMG_OUT_NEAREST;
+    v.want_err = outputs & CMG_OUT_ERROR_BOUND;
+    v.autotune = o.autotune != 0;
+    return v;
+}
+
+int effective_outputs(const cmg_voxel_opts& o) {
+    if (o.outputs) return o.outputs;
+    return o.mode == 1 ? CMG_OUT_SDF_F32 : CMG_OUT_OCCUPANCY;
+}
+
+void fill_stats(cmg_voxels* v, const cmg::gpu::RunInfo& ri) {
+    cmg_voxel_stats& s = v->stats;
+    s.cells = ri.cells;
+    s.flagged_columns = static_cast<int64_t>(ri.stats.flagged_columns);
+    s.nudged_columns = static_cast<int64_t>(ri.stats.nudged_columns);
+    s.exhausted_columns = static_cast<int64_t>(ri.stats.exhausted_columns);
+    s.exact_calls = static_cast<int64_t>(ri.stats.exact_calls);
+    s.bucket_entries = ri.pairs;
+    s.candidates = ri.candidates;
+    s.evaluations = static_cast<int64_t>(ri.stats.evaluations);
+    s.fp64_evaluations = static_cast<int64_t>(ri.stats.fp64_evaluations);
+    s.band_cells = static_cast<int64_t>(ri.stats.band_voxels);
+    s.brick = ri.brick;
+    double m = 0;
+    for (float e : v->r.err) m = std::max(m, static_cast<double>(e));
+    s.max_error_bound = m;
+}
+
+void set_geometry(cmg_voxels* v, const GridDesc& g) {
+    for (int a = 0; a < 3; ++a) {
+        v->corner[a] = g.corner[a];
+        v->origin[a] = g.corner[a] + 0.5 * g.h;  // voxelize.cpp:389-391
+    }
+    v->spacing = g.h;
+    v->nx = g.nx;
+    v->ny = g.ny;
+    v->nz = g.nz;
+}
+
+cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
+    if (!o.explicit_grid && o.resolution < 1)
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
+    std::vector<int> tris = checked_triangles(p);
+    GridDesc g{};
+    if (o.explicit_grid) {
+        for (int a = 0; a < 3; ++a) g.corner[a] = o.corner[a];
+        g.h = o.spacing;
+        g.nx = o.dims[0];
+        g.ny = o.dims[1];
+        g.nz = o.dims[2];
+        if (!(g.h > 0)) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: spacing must be > 0"};
+    } else if (!make_grid(p.points, o.resolution, o.pad, g)) {
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
+    }
+    check_grid_size(g);
+    const int outputs = effective_outputs(o);
+    cmg::gpu::VoxOpts vo = to_vox(o, outputs);
+    cmg::gpu::HostMesh m;
+    m.pts = p.points.data();
+    m.npts = static_cast<int64_t>(p.points.size() / 3);
+    m.tris = tris.data();
+    m.ntris = static_cast<int64_t>(tris.size() / 3);
+    m.g = g;
+    std::lock_guard<std::mutex> lk(gpu_mutex());
+    cudaStream_t st = gpu_stream();
+    if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick({m}, vo, st);
+    std::unique_ptr<cmg_voxels> v(new cmg_voxels);
+    set_geometry(v.get(), g);
+    cmg::gpu::Batch b({m}, vo, st, /*transient=*/true);
+    b.run();
+    std::vector<cmg::gpu::HostResult> res;
+    cmg::gpu::RunInfo ri;
+    b.download(res, &ri);
+    v->r = std::move(res[0]);
+    fill_stats(v.get(), ri);
+    return v.release();
+}
+
+template <typename F>
+cmg_status guarded(char* errbuf, size_t len, F&& f) {
+    try {
+        f();
+        return CMG_OK;
+    } catch (const CoreError& e) {
+        set_err(errbuf, len, e.msg);
+        return e.code;
+    } catch (const std::invalid_argument& e) {
+        set_err(errbuf, len, e.what());
+        return CMG_ERR_INVALID_INPUT;
+    } catch (const std::exception& e) {
+        set_err(errbuf, len, e.what());
+        return CMG_ERR_INTERNAL;
+    } catch (...) {
+        set_err(errbuf, len, "unknown error");
+        return CMG_ERR_INTERNAL;
+    }
+}
+
+const char* kNotHere = "not part of the GB300 voxelization library (meshing and file I/O stay in the reference)";
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ PLC
+cmg_plc* cmg_plc_create(void) { return new (std::nothrow) cmg_plc{}; }
+void cmg_plc_destroy(cmg_plc* p) { delete p; }
+
+cmg_status cmg_plc_set_points(cmg_plc* plc, const double* xyz, size_t count) {
+    if (!plc || (!xyz && count)) return CMG_ERR_INVALID_INPUT;
+    try {
+        plc->points.assign(xyz, xyz + 3 * count);
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
+cmg_status cmg_plc_add_facet(cmg_plc* plc, const int* idx, size_t count, int marker) {
+    if (!plc || (!idx && count)) return CMG_ERR_INVALID_INPUT;
+    if (count < 3) return CMG_ERR_INVALID_INPUT;
+    try {
+        plc->facets.emplace_back(idx, idx + count);
+        plc->markers.push_back(marker);
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
+cmg_status cmg_plc_add_hole(cmg_plc* plc, double x, double y, double z) {
+    if (!plc) return CMG_ERR_INVALID_INPUT;
+    plc->holes.insert(plc->holes.end(), {x, y, z});
+    return CMG_OK;
+}
+
+cmg_status cmg_plc_add_region(cmg_plc* plc, double x, double y, double z, double attribute,
+                              double max_volume) {
+    if (!plc) return CMG_ERR_INVALID_INPUT;
+    plc->regions.push_back({x, y, z, attribute, max_volume});
+    return CMG_OK;
+}
+
+size_t cmg_plc_num_points(const cmg_plc* p) { return p ? p->points.size() / 3 : 0; }
+
+const double* cmg_plc_points(cmg_plc* p) {
+    if (!p) return nullptr;
+    p->pts_cache = p->points;
+    return p->pts_cache.data();
+}
+
+size_t cmg_plc_num_triangles(cmg_plc* p) {
+    if (!p) return 0;
+    p->tri_cache = fan(*p);
+    return p->tri_cache.size() / 3;
+}
+
+const int* cmg_plc_triangles(cmg_plc* p) {
+    if (!p) return nullptr;
+    p->tri_cache = fan(*p);
+    return p->tri_cache.data();
+}
+
+// ------------------------------------------------------------------ voxelization
+void cmg_voxel_opts_init(cmg_voxel_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->resolution = 64;
+    o->pad = 1;
+    o->precision = CMG_PREC_FP64;
+    o->predicates = CMG_PRED_COMPAT;
+    o->band = 1.0;
+}
+
+cmg_status cmg_plc_voxelize(const cmg_plc* in, int resolution, int mode, int pad,
+                            cmg_voxels** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!in || !out) return CMG_ERR_INVALID_INPUT;
+    if (resolution < 1) {
+        set_err(errbuf, len, "resolution must be >= 1");
+        return CMG_ERR_INVALID_INPUT;
+    }
+    cmg_voxel_opts o;
+    cmg_voxel_opts_init(&o);
+    o.resolution = resolution;
+    o.pad = pad;
+    o.mode = mode == 1 ? 1 : 0;
+    return guarded(errbuf, len, [&] { *out = voxelize_one(*in, o); });
+}
+
+cmg_status cmg_plc_voxelize_ex(const cmg_plc* in, const cmg_voxel_opts* opts, cmg_voxels** out,
+                               char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!in || !out || !opts) return CMG_ERR_INVALID_INPUT;
+    if (!opts->explicit_grid && opts->resolution < 1) {
+        set_err(errbuf, len, "resolution must be >= 1");
+        return CMG_ERR_INVALID_INPUT;
+    }
+    if (opts->brick != 0 && opts->brick != 4 && opts->brick != 8) {
+        set_err(errbuf, len, "brick must be 0, 4 or 8");
+        return CMG_ERR_UNSUPPORTED_OPTION;
+    }
+    return guarded(errbuf, len, [&] { *out = voxelize_one(*in, *opts); });
+}
+
+void cmg_voxels_destroy(cmg_voxels* v) { delete v; }
+
+void cmg_voxels_dims(const cmg_voxels* v, int* nx, int* ny, int* nz) {
+    if (nx) *nx = v ? v->nx : 0;
+    if (ny) *ny = v ? v->ny : 0;
+    if (nz) *nz = v ? v->nz : 0;
+}
+
+void cmg_voxels_origin(const cmg_voxels* v, double* x, double* y, double* z) {
+    if (x) *x = v ? v->origin[0] : 0.0;
+    if (y) *y = v ? v->origin[1] : 0.0;
+    if (z) *z = v ? v->origin[2] : 0.0;
+}
+
+void cmg_voxels_corner(const cmg_voxels* v, double* x, double* y, double* z) {
+    if (x) *x = v ? v->corner[0] : 0.0;
+    if (y) *y = v ? v->corner[1] : 0.0;
+    if (z) *z = v ? v->corner[2] : 0.0;
+}
+
+double cmg_voxels_spacing(const cmg_voxels* v) { return v ? v->spacing : 0.0; }
+
+const unsigned char* cmg_voxels_occupancy(const cmg_voxels* v) {
+    return (v && !v->r.occ.empty()) ? v->r.occ.data() : nullptr;
+}
+const float* cmg_voxels_distance(const cmg_voxels* v) {
+    return (v && !v->r.sdf32.empty()) ? v->r.sdf32.data() : nullptr;
+}
+const double* cmg_voxels_distance_f64(const cmg_voxels* v) {
+    return (v && !v->r.sdf64.empty()) ? v->r.sdf64.data() : nullptr;
+}
+const int* cmg_voxels_nearest_triangle(const cmg_voxels* v) {
+    return (v && !v->r.near_tri.empty()) ? v->r.near_tri.data() : nullptr;
+}
+const unsigned char* cmg_voxels_nearest_region(const cmg_voxels* v) {
+    return (v && !v->r.near_reg.empty()) ? v->r.near_reg.data() : nullptr;
+}
+const float* cmg_voxels_error_bound(const cmg_voxels* v) {
+    return (v && !v->r.err.empty()) ? v->r.err.data() : nullptr;
+}
+void cmg_voxels_stats(const cmg_voxels* v, cmg_voxel_stats* out) {
+    if (!out) return;
+    if (!v) {
+        std::memset(out, 0, sizeof(*out));
+        return;
+    }
+    *out = v->stats;
+}
+
+// ------------------------------------------------------------------ batches
+cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, const int* pads,
+                            int n, const cmg_voxel_opts* opts, cmg_batch** out, char* errbuf,
+                            size_t len) {
+    if (out) *out = nullptr;
+    if (!plcs || !opts || !out || n < 1) return CMG_ERR_INVALID_INPUT;
+    if (!opts->explicit_grid && (!resolutions || !pads)) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::vector<std::vector<int>> tris(static_cast<size_t>(n));
+        std::vector<cmg::gpu::HostMesh> meshes(static_cast<size_t>(n));
+        std::unique_ptr<cmg_batch> b(new cmg_batch);
+        for (int i = 0; i < n; ++i) {
+            if (!plcs[i]) throw CoreError{CMG_ERR_INVALID_INPUT, "cmg_batch_create: NULL plc"};
+            const cmg_plc& p = *plcs[i];
+            tris[i] = checked_triangles(p);
+            GridDesc g{};
+            if (opts->explicit_grid) {
+                for (int a = 0; a < 3; ++a) g.corner[a] = opts->corner[a];
+                g.h = opts->spacing;
+                g.nx = opts->dims[0];
+                g.ny = opts->dims[1];
+                g.nz = opts->dims[2];
+            } else {
+                if (resolutions[i] < 1)
+                    throw CoreError{CMG_ERR_INVALID_INPUT, "resolution must be >= 1"};
+                if (!make_grid(p.points, resolutions[i], pads[i], g))
+                    throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
+            }
+            check_grid_size(g);
+            meshes[i].pts = p.points.data();
+            meshes[i].npts = static_cast<int64_t>(p.points.size() / 3);
+            meshes[i].tris = tris[i].data();
+            meshes[i].ntris = static_cast<int64_t>(tris[i].size() / 3);
+            meshes[i].g = g;
+            b->grids.push_back(g);
+        }
+        b->outputs = effective_outputs(*opts);
+        cmg::gpu::VoxOpts vo = to_vox(*opts, b->outputs);
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cudaStream_t st = gpu_stream();
+        if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick(meshes, vo, st);
+        b->batch.reset(new cmg::gpu::Batch(meshes, vo, st, /*transient=*/false));
+        *out = b.release();
+    });
+}
+
+cmg_status cmg_batch_run(cmg_batch* b, int use_graph, char* errbuf, size_t len) {
+    if (!b) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        if (use_graph) b->batch->run_graph();
+        else b->batch->run();
+        b->ran = true;
+    });
+}
+
+cmg_status cmg_batch_sync(cmg_batch* b, char* errbuf, size_t len) {
+    if (!b) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] { b->batch->synchronize(); });
+}
+
+cmg_status cmg_batch_get(cmg_batch* b, int i, cmg_voxels** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!b || !out || i < 0 || i >= b->batch->nmeshes()) return CMG_ERR_INVALID_INPUT;
+    if (!b->ran) {
+        set_err(errbuf, len, "cmg_batch_get: the batch has not run");
+        return CMG_ERR_INVALID_INPUT;
+    }
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        std::vector<cmg::gpu::HostResult> res;
+        cmg::gpu::RunInfo ri;
+        b->batch->download(res, &ri);
+        std::unique_ptr<cmg_voxels> v(new cmg_voxels);
+        set_geometry(v.get(), b->grids[static_cast<size_t>(i)]);
+        v->r = std::move(res[static_cast<size_t>(i)]);
+        fill_stats(v.get(), ri);
+        v->stats.cells = static_cast<int64_t>(v->nx) * v->ny * v->nz;
+        *out = v.release();
+    });
+}
+
+int cmg_batch_size(const cmg_batch* b) { return b ? b->batch->nmeshes() : 0; }
+int64_t cmg_batch_cells(const cmg_batch* b) { return b ? b->batch->total_cells() : 0; }
+void cmg_batch_destroy(cmg_batch* b) {
+    if (!b) return;
+    std::lock_guard<std::mutex> lk(gpu_mutex());
+    delete b;
+}
+
+const char* cmg_gpu_version(void) { return "cmg-gb300 0.1.0 sm_103a"; }
+
+// ------------------------------------------------------------------ options
+cmg_options* cmg_options_create(void) { return new (std::nothrow) cmg_options{}; }
+void cmg_options_destroy(cmg_options* o) { delete o; }
+cmg_status cmg_options_from_switches(cmg_options* o, const char* sw, char* errbuf, size_t len) {
+    if (!o || !sw) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_options_set_plc(cmg_options* o, int on) {
+    if (!o) return CMG_ERR_INVALID_INPUT;
+    o->plc = on != 0;
+    return CMG_OK;
+}
+cmg_status cmg_options_set_max_volume(cmg_options* o, double v) {
+    if (!o) return CMG_ERR_INVALID_INPUT;
+    o->max_volume = v;
+    return CMG_OK;
+}
+cmg_status cmg_options_set_quality(cmg_options* o, double radius_edge, double min_dihedral) {
+    if (!o) return CMG_ERR_INVALID_INPUT;
+    o->quality = 1;
+    o->radius_edge = radius_edge;
+    o->min_dihedral = min_dihedral;
+    return CMG_OK;
+}
+cmg_status cmg_options_set_preserve_edges(cmg_options* o, int on) {
+    if (!o) return CMG_ERR_INVALID_INPUT;
+    o->preserve_edges = on != 0;
+    return CMG_OK;
+}
+
+// ------------------------------------------------------------------ not in this library
+void cmg_mesh_destroy(cmg_mesh* m) { delete m; }
+cmg_status cmg_tetrahedralize(const cmg_plc* plc, const cmg_options* opts, cmg_mesh** out,
+                              char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!plc || !opts || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_delaunay(const double* xyz, size_t count, const cmg_options* opts, cmg_mesh** out,
+                        char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if ((!xyz && count) || !opts || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+size_t cmg_mesh_num_points(const cmg_mesh*) { return 0; }
+size_t cmg_mesh_num_tets(const cmg_mesh*) { return 0; }
+size_t cmg_mesh_num_faces(const cmg_mesh*) { return 0; }
+const double* cmg_mesh_points(const cmg_mesh*) { return nullptr; }
+const int* cmg_mesh_tets(const cmg_mesh*) { return nullptr; }
+const int* cmg_mesh_faces(const cmg_mesh*) { return nullptr; }
+const int* cmg_mesh_tet_markers(const cmg_mesh*) { return nullptr; }
+const int* cmg_mesh_face_markers(const cmg_mesh*) { return nullptr; }
+cmg_status cmg_read_plc(const char* path, cmg_plc** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!path || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_read_points(const char* path, cmg_plc** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!path || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_read_mesh(const char* path, cmg_mesh** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!path || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_write_mesh(const char* path, const cmg_mesh* m, char* errbuf, size_t len) {
+    if (!path || !m) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_write_plc(const char* path, const cmg_plc* p, char* errbuf, size_t len) {
+    if (!path || !p) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+cmg_status cmg_plc_simplify(const cmg_plc* in, int grid, cmg_plc** out, char* errbuf, size_t len) {
+    (void)grid;
+    if (out) *out = nullptr;
+    if (!in || !out) return CMG_ERR_INVALID_INPUT;
+    set_err(errbuf, len, kNotHere);
+    return CMG_ERR_NOT_IMPLEMENTED;
+}
+
+const char* cmg_version(void) { return "0.5.0"; }
+
+}  // extern "C"

@@ -1,0 +1,270 @@
+// cmg_exact.cuh — exact signs of orient3d and insphere on the device.
+//
+// Expansion arithmetic after J. R. Shewchuk, "Adaptive Precision Floating-Point
+// Arithmetic and Fast Robust Geometric Predicates" (CMU-CS-96-140): a number is a
+// sum of non-overlapping doubles sorted by magnitude; Two-Sum and Two-Product are
+// error-free (Two-Product here uses the fused multiply-add residual a*b - fl(a*b),
+// which is exact), sums merge by magnitude, and the sign of an expansion is the
+// sign of its largest component. Inputs must stay clear of overflow and underflow,
+// as for the reference's predicates.
+//
+// These routines run only in the compacted second passes (columns or queries the
+// FP64 filter could not decide), one thread per case, so their local arrays never
+// load the main kernels.
+#pragma once
+
+#include "cmg_device.cuh"
+
+namespace cmg::gpu::exact {
+
+__device__ __forceinline__ void two_sum(double a, double b, double& x, double& y) {
+    x = __dadd_rn(a, b);
+    double bv = __dsub_rn(x, a);
+    double av = __dsub_rn(x, bv);
+    y = __dadd_rn(__dsub_rn(a, av), __dsub_rn(b, bv));
+}
+__device__ __forceinline__ void fast_two_sum(double a, double b, double& x, double& y) {
+    x = __dadd_rn(a, b);
+    y = __dsub_rn(b, __dsub_rn(x, a));
+}
+__device__ __forceinline__ void two_prod(double a, double b, double& x, double& y) {
+    x = __dmul_rn(a, b);
+    y = __fma_rn(a, b, -x);
+}
+__device__ __forceinline__ void two_diff(double a, double b, double& x, double& y) {
+    two_sum(a, -b, x, y);
+}
+
+// h = e + f: merge by magnitude, then a Two-Sum sweep, zero-eliminated.
+// h holds elen + flen doubles and may not alias e or f.
+__device__ __noinline__ int sum(int elen, const double* e, int flen, const double* f,
+                                double* h) {
+    int i = 0, j = 0, hn = 0;
+    double q;
+    bool have = false;
+    while (i < elen || j < flen) {
+        double g;
+        if (j >= flen || (i < elen && fabs(e[i]) <= fabs(f[j]))) g = e[i++];
+        else g = f[j++];
+        if (!have) {
+            q = g;
+            have = true;
+            continue;
+        }
+        double qn, hh;
+        two_sum(q, g, qn, hh);
+        q = qn;
+        if (hh != 0.0) h[hn++] = hh;
+    }
+    if (!have) q = 0.0;
+    if (q != 0.0 || hn == 0) h[hn++] = q;
+    return hn;
+}
+
+// h = b * e, zero-eliminated; h holds 2 * elen doubles.
+__device__ __noinline__ int scale(int elen, const double* e, double b, double* h) {
+    double q, hh;
+    int hn = 0;
+    two_prod(e[0], b, q, hh);
+    if (hh != 0.0) h[hn++] = hh;
+    for (int i = 1; i < elen; ++i) {
+        double p1, p0, s;
+        two_prod(e[i], b, p1, p0);
+        two_sum(q, p0, s, hh);
+        if (hh != 0.0) h[hn++] = hh;
+        fast_two_sum(p1, s, q, hh);
+        if (hh != 0.0) h[hn++] = hh;
+    }
+    if (q != 0.0 || hn == 0) h[hn++] = q;
+    return hn;
+}
+
+// Renormalise in place (Shewchuk's Compress): same value, fewer components.
+__device__ __noinline__ int compress(int m, double* e) {
+    if (m <= 1) return m;
+    double q = e[m - 1];
+    int bottom = m - 1;
+    for (int i = m - 2; i >= 0; --i) {
+        double qn, lo;
+        fast_two_sum(q, e[i], qn, lo);
+        if (lo != 0.0) {
+            e[bottom--] = qn;
+            q = lo;
+        } else {
+            q = qn;
+        }
+    }
+    e[bottom] = q;
+    int top = 0;
+    for (int i = bottom + 1; i < m; ++i) {
+        double qn, lo;
+        fast_two_sum(e[i], q, qn, lo);
+        q = qn;
+        if (lo != 0.0) e[top++] = lo;
+    }
+    e[top++] = q;
+    return top;
+}
+
+__device__ __forceinline__ int sign_of(int n, const double* e) {
+    double t = e[n - 1];
+    return t > 0.0 ? 1 : (t < 0.0 ? -1 : 0);
+}
+
+// m(u, v) = ux*vy - vx*uy, exactly (<= 4 components).
+__device__ __forceinline__ int minor2(double ux, double uy, double vx, double vy, double* out) {
+    double p[2], q[2];
+    two_prod(ux, vy, p[1], p[0]);
+    two_prod(vx, uy, q[1], q[0]);
+    q[0] = -q[0];
+    q[1] = -q[1];
+    return sum(2, p, 2, q, out);
+}
+
+// |pqr| (rows of x, y, z) = pz*m(q,r) - qz*m(p,r) + rz*m(p,q), exactly (<= 24).
+__device__ __noinline__ int det3(const d3& p, const d3& q, const d3& r, double* out) {
+    double mqr[4], mpr[4], mpq[4], s1[8], s2[8], s3[8], t[16];
+    int n1 = minor2(q.x, q.y, r.x, r.y, mqr);
+    int n2 = minor2(p.x, p.y, r.x, r.y, mpr);
+    int n3 = minor2(p.x, p.y, q.x, q.y, mpq);
+    int l1 = scale(n1, mqr, p.z, s1);
+    int l2 = scale(n2, mpr, -q.z, s2);
+    int l3 = scale(n3, mpq, r.z, s3);
+    int lt = sum(l1, s1, l2, s2, t);
+    return sum(lt, t, l3, s3, out);
+}
+
+// Exact orient3d(a,b,c,d) with homogeneous coordinates (no rounding in the
+// differences): |abc| - |abd| + |acd| - |bcd| (<= 96 components).
+__device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b, const d3& c,
+                                                 const d3& d, double* out) {
+    double t1[24], t2[24], t3[24], t4[24], u[48], v[48];
+    int n1 = det3(a, b, c, t1);
+    int n2 = det3(a, b, d, t2);
+    int n3 = det3(a, c, d, t3);
+    int n4 = det3(b, c, d, t4);
+    for (int i = 0; i < n2; ++i) t2[i] = -t2[i];
+    for (int i = 0; i < n4; ++i) t4[i] = -t4[i];
+    int nu = sum(n1, t1, n2, t2, u);
+    int nv = sum(n3, t3, n4, t4, v);
+    return sum(nu, u, nv, v, out);
+}
+
+// Exact sign of orient3d(a, b, c, d).
+__device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c, const d3& d) {
+    double adx, ady, adz, bdx, bdy, bdz, cdx, cdy, cdz;
+    double t0, t1, t2, t3, t4, t5, t6, t7, t8;
+    two_diff(a.x, d.x, adx, t0);
+    two_diff(a.y, d.y, ady, t1);
+    two_diff(a.z, d.z, adz, t2);
+    two_diff(b.x, d.x, bdx, t3);
+    two_diff(b.y, d.y, bdy, t4);
+    two_diff(b.z, d.z, bdz, t5);
+    two_diff(c.x, d.x, cdx, t6);
+    two_diff(c.y, d.y, cdy, t7);
+    two_diff(c.z, d.z, cdz, t8);
+    if (t0 == 0.0 && t1 == 0.0 && t2 == 0.0 && t3 == 0.0 && t4 == 0.0 && t5 == 0.0 &&
+        t6 == 0.0 && t7 == 0.0 && t8 == 0.0) {
+        // the differences are exact: a 3x3 determinant suffices
+        double e[24];
+        int n = det3({adx, ady, adz}, {bdx, bdy, bdz}, {cdx, cdy, cdz}, e);
+        return sign_of(n, e);
+    }
+    double e[96];
+    int n = orient3d_homogeneous(a, b, c, d, e);
+    return sign_of(n, e);
+}
+
+// acc += s * w * x (w a short expansion, x up to 96 components); acc holds cap
+// doubles, work holds cap + 192. Returns the new length or -1 on overflow.
+__device__ __noinline__ int accumulate(int nacc, double* acc, int nw, const double* w, double s,
+                                       int nx, const double* x, double* work, int cap) {
+    double prod[192];
+    for (int c = 0; c < nw; ++c) {
+        int np = scale(nx, x, s * w[c], prod);
+        if (nacc + np > cap + 192) return -1;
+        int nn = sum(nacc, acc, np, prod, work);
+        nn = compress(nn, work);
+        if (nn > cap) return -1;
+        for (int i = 0; i < nn; ++i) acc[i] = work[i];
+        nacc = nn;
+    }
+    return nacc;
+}
+
+// Exact lift x^2 + y^2 + z^2 (<= 6 components).
+__device__ __forceinline__ int lift(const d3& p, double* out) {
+    double sx[2], sy[2], sz[2], t[4];
+    two_prod(p.x, p.x, sx[1], sx[0]);
+    two_prod(p.y, p.y, sy[1], sy[0]);
+    two_prod(p.z, p.z, sz[1], sz[0]);
+    int n = sum(2, sx, 2, sy, t);
+    return sum(n, t, 2, sz, out);
+}
+
+constexpr int kInsphereCap = 256;
+
+// Exact sign of insphere(a, b, c, d, e); sets *overflow when the accumulator
+// capacity is exceeded (the sign is then 0 and must not be trusted).
+__device__ __noinline__ int insphere_sign(const d3& a, const d3& b, const d3& c, const d3& d,
+                                          const d3& e, int* overflow) {
+    double acc[kInsphereCap], work[kInsphereCap + 192];
+    int nacc = 1;
+    acc[0] = 0.0;
+    double tails[12];
+    double aex, aey, aez, bex, bey, bez, cex, cey, cez, dex, dey, dez;
+    two_diff(a.x, e.x, aex, tails[0]);
+    two_diff(a.y, e.y, aey, tails[1]);
+    two_diff(a.z, e.z, aez, tails[2]);
+    two_diff(b.x, e.x, bex, tails[3]);
+    two_diff(b.y, e.y, bey, tails[4]);
+    two_diff(b.z, e.z, bez, tails[5]);
+    two_diff(c.x, e.x, cex, tails[6]);
+    two_diff(c.y, e.y, cey, tails[7]);
+    two_diff(c.z, e.z, cez, tails[8]);
+    two_diff(d.x, e.x, dex, tails[9]);
+    two_diff(d.y, e.y, dey, tails[10]);
+    two_diff(d.z, e.z, dez, tails[11]);
+    bool exact_diff = true;
+    for (int i = 0; i < 12; ++i) exact_diff = exact_diff && tails[i] == 0.0;
+    if (exact_diff) {
+        // translated form: det4 = -la|bcd| + lb|acd| - lc|abd| + ld|abc|
+        const d3 P[4] = {{aex, aey, aez}, {bex, bey, bez}, {cex, cey, cez}, {dex, dey, dez}};
+        for (int i = 0; i < 4; ++i) {
+            const d3* q[3];
+            int k = 0;
+            for (int j = 0; j < 4; ++j)
+                if (j != i) q[k++] = &P[j];
+            double m[24], w[6];
+            int nm = det3(*q[0], *q[1], *q[2], m);
+            int nw = lift(P[i], w);
+            double s = (i % 2 == 0) ? -1.0 : 1.0;
+            nacc = accumulate(nacc, acc, nw, w, s, nm, m, work, kInsphereCap);
+            if (nacc < 0) {
+                *overflow = 1;
+                return 0;
+            }
+        }
+        return sign_of(nacc, acc);
+    }
+    // homogeneous form: det5 = sum_i (-1)^(i+1) w_i O(others), i over a..e
+    const d3 P[5] = {a, b, c, d, e};
+    for (int i = 0; i < 5; ++i) {
+        const d3* q[4];
+        int k = 0;
+        for (int j = 0; j < 5; ++j)
+            if (j != i) q[k++] = &P[j];
+        double o[96], w[6];
+        int no = orient3d_homogeneous(*q[0], *q[1], *q[2], *q[3], o);
+        int nw = lift(P[i], w);
+        double s = (i % 2 == 0) ? -1.0 : 1.0;
+        nacc = accumulate(nacc, acc, nw, w, s, no, o, work, kInsphereCap);
+        if (nacc < 0) {
+            *overflow = 1;
+            return 0;
+        }
+    }
+    return sign_of(nacc, acc);
+}
+
+}  // namespace cmg::gpu::exact

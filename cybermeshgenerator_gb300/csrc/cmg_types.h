@@ -1,0 +1,54 @@
+// cmg_types.h — plain data shared by the host engine and the device kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace cmg::gpu {
+
+// Regular grid: cell (i,j,k) has its centre at corner + (i+0.5, j+0.5, k+0.5)*h
+// and flat index (k*ny + j)*nx + i (include/cmg/voxelize/voxelize.hpp:36-52).
+struct GridDesc {
+    double corner[3];
+    double h;
+    int nx, ny, nz;
+    int pad_;
+};
+
+// One mesh of a batch. Every index range is global (into the concatenated
+// arrays of the batch), so kernels over a flattened index space recover the mesh
+// by a binary search on the corresponding *_begin field.
+struct MeshSeg {
+    GridDesc g;
+    int64_t tri_begin, tri_end;     // triangles
+    int64_t col_begin;              // xy columns (nx*ny)
+    int64_t row_begin;              // occupancy work rows: ny * ceil(nx/32)
+    int64_t vox_begin;              // cells (nx*ny*nz)
+    int64_t brick_begin;            // SDF bricks (also the triangle bins)
+    int bnx, bny, bnz;              // bricks per axis
+    int brick;                      // brick edge in cells
+    int64_t large_begin, large_end; // always-considered triangles (global list)
+    float emax;                     // max centroid-to-vertex distance of binned triangles
+    float scale;                    // max |coordinate| of the mesh and grid (error bounds)
+};
+
+// Counters written by the kernels (device memory, one per batch).
+struct Stats {
+    unsigned long long flagged_columns;    // occupancy columns sent to the exact pass
+    unsigned long long nudged_columns;     // first attempt grazed
+    unsigned long long exhausted_columns;  // every nudge grazed
+    unsigned long long exact_calls;        // orient3d resolved in exact arithmetic
+    unsigned long long height_overflow;    // columns whose crossings overflowed shared memory
+    unsigned long long candidates;         // SDF candidate (brick, triangle) pairs
+    unsigned long long evaluations;        // SDF (voxel, triangle) distance evaluations
+    unsigned long long fp64_evaluations;   // of which in FP64
+    unsigned long long band_voxels;        // mixed precision: voxels refined in FP64
+    unsigned long long error_flags;        // nonzero: a kernel hit a capacity limit
+};
+
+enum : int { kPredCompat = 0, kPredExact = 1 };
+enum : int { kPrecFP64 = 0, kPrecMixed = 1 };
+
+// Triangle record in the soup: 9 coordinates + 1 pad (80 bytes, 16-byte aligned).
+constexpr int kSoupStride = 10;
+
+}  // namespace cmg::gpu

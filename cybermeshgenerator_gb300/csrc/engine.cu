@@ -1,0 +1,451 @@
+// engine.cu — host orchestration of the voxelization pipeline (see engine.h).
+#include "engine.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "cmg_util.h"
+#include "engine_kernels.h"
+
+namespace cmg::gpu {
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    CMG_CUDA(cudaGetDevice(&dev));
+    CMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+}
+
+namespace {
+
+template <typename T>
+T* carve(Arena& a, size_t n) {
+    T* p = a.take<T>(n ? n : 1);
+    return p;
+}
+
+int pick_brick(const VoxOpts& o) { return o.brick == 4 ? 4 : 8; }
+
+}  // namespace
+
+// Workspace arenas shared by transient batches on a device (one call at a time,
+// serialised by the caller), so repeated single calls do not re-allocate.
+struct Pool {
+    Arena a[4];
+};
+Pool& pool_for_device() {
+    static std::mutex mu;
+    static std::map<int, std::unique_ptr<Pool>> pools;
+    int dev = 0;
+    CMG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    auto& p = pools[dev];
+    if (!p) p.reset(new Pool);
+    return *p;
+}
+
+struct Batch::Impl {
+    Arena own[4];
+    Arena& fixed;    // inputs, sized-up-front workspace
+    Arena& pairs;    // (triangle, column) bucket entries and their scratch
+    Arena& cands;    // brick candidate lists
+    Arena& outs;     // outputs
+    // a == nullptr: the batch owns its arenas
+    explicit Impl(Arena* a)
+        : fixed(a ? a[0] : own[0]), pairs(a ? a[1] : own[1]), cands(a ? a[2] : own[2]),
+          outs(a ? a[3] : own[3]) {}
+    // workspace
+    double* soup = nullptr;
+    int4* xybox = nullptr;
+    int64_t* pairs_n = nullptr;
+    int64_t* pair_off = nullptr;
+    int* colcnt = nullptr;
+    int64_t* col_off = nullptr;
+    int64_t* flagged = nullptr;
+    int64_t* scan_tmp = nullptr;
+    uint8_t* occ_internal = nullptr;
+    int* col_list = nullptr;
+    double* hs = nullptr;
+    uint8_t* hv = nullptr;
+    // sdf
+    float4* tinfo = nullptr;
+    float4* tlo = nullptr;
+    float4* thi = nullptr;
+    int64_t* tbin = nullptr;
+    int* bincnt = nullptr;
+    int64_t* bin_off = nullptr;
+    int* bin_list = nullptr;
+    int* large_cnt = nullptr;
+    int64_t* large_off = nullptr;
+    int* large_list = nullptr;
+    unsigned* emax_bits = nullptr;
+    float* bound = nullptr;
+    int* cand_cnt = nullptr;
+    int64_t* cand_off = nullptr;
+    float* brick_emax = nullptr;
+    uint32_t* work_keys = nullptr;
+    uint32_t* work = nullptr;
+    void* sort_tmp = nullptr;
+    int* cand = nullptr;
+    int grid_exact = 0;
+    int grid_eval = 0;
+    cudaGraph_t graph = nullptr;
+};
+
+Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream,
+             bool transient)
+    : opts_(opts), stream_(stream) {
+    impl_.reset(new Impl(transient ? pool_for_device().a : nullptr));
+    const int brick = pick_brick(opts);
+    opts_.brick = brick;
+    const int rc = occ_row_cols();
+    int64_t tb = 0, pb = 0;
+    for (const HostMesh& m : meshes) {
+        if (m.g.nx <= 0 || m.g.ny <= 0 || m.g.nz <= 0)
+            throw std::invalid_argument("voxelize: empty grid");
+        MeshSeg s{};
+        s.g = m.g;
+        s.tri_begin = tb;
+        s.tri_end = tb + m.ntris;
+        s.col_begin = ncol_;
+        s.row_begin = nrow_;
+        s.vox_begin = nvox_;
+        s.brick_begin = nbrick_;
+        s.brick = brick;
+        s.bnx = (m.g.nx + brick - 1) / brick;
+        s.bny = (m.g.ny + brick - 1) / brick;
+        s.bnz = (m.g.nz + brick - 1) / brick;
+        double sc = 0.0;
+        for (int64_t i = 0; i < m.npts; ++i)
+            for (int a = 0; a < 3; ++a) sc = std::max(sc, std::fabs(m.pts[3 * i + a] - m.g.corner[a]));
+        sc = std::max(sc, m.g.h * std::max(m.g.nx, std::max(m.g.ny, m.g.nz)));
+        s.scale = static_cast<float>(sc * 1.0001);
+        segs_.push_back(s);
+        tb += m.ntris;
+        pb += m.npts;
+        ncol_ += static_cast<int64_t>(m.g.nx) * m.g.ny;
+        nrow_ += static_cast<int64_t>(m.g.ny) * ((m.g.nx + rc - 1) / rc);
+        nvox_ += static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
+        nbrick_ += static_cast<int64_t>(s.bnx) * s.bny * s.bnz;
+    }
+    ntris_ = tb;
+    npts_ = pb;
+    if (nbrick_ >= (int64_t(1) << 32)) throw std::invalid_argument("voxelize: grid too large");
+    const int nseg = static_cast<int>(segs_.size());
+    const bool sdf = opts_.want_sdf32 || opts_.want_sdf64 || opts_.want_near;
+
+    // ---- fixed workspace
+    Arena& A = impl_->fixed;
+    auto plan = [&](bool commit) {
+        A.reset();
+        pts_ = carve<double>(A, 3 * npts_);
+        tris_ = carve<int>(A, 3 * ntris_);
+        dsegs_ = carve<MeshSeg>(A, nseg);
+        stats_ = carve<Stats>(A, 1);
+        queue_ = carve<unsigned long long>(A, 1);
+        impl_->soup = carve<double>(A, kSoupStride * ntris_);
+        impl_->xybox = carve<int4>(A, ntris_);
+        impl_->pairs_n = carve<int64_t>(A, ntris_ + 1);
+        impl_->pair_off = carve<int64_t>(A, ntris_ + 1);
+        impl_->colcnt = carve<int>(A, ncol_);
+        impl_->col_off = carve<int64_t>(A, ncol_ + 1);
+        impl_->flagged = carve<int64_t>(A, ncol_);
+        int64_t smax = std::max(std::max(ntris_, ncol_), std::max(nbrick_, int64_t(nseg)));
+        impl_->scan_tmp = carve<int64_t>(A, scan_tmp_elems(smax));
+        if (!opts_.want_occ) impl_->occ_internal = carve<uint8_t>(A, nvox_);
+        if (sdf) {
+            impl_->tinfo = carve<float4>(A, ntris_);
+            impl_->tlo = carve<float4>(A, ntris_);
+            impl_->thi = carve<float4>(A, ntris_);
+            impl_->tbin = carve<int64_t>(A, ntris_);
+            impl_->bincnt = carve<int>(A, nbrick_);
+            impl_->bin_off = carve<int64_t>(A, nbrick_ + 1);
+            impl_->bin_list = carve<int>(A, ntris_);
+            impl_->large_cnt = carve<int>(A, 2 * nseg);
+            impl_->large_off = carve<int64_t>(A, nseg + 1);
+            impl_->large_list = carve<int>(A, ntris_);
+            impl_->emax_bits = carve<unsigned>(A, nseg);
+            impl_->bound = carve<float>(A, nbrick_);
+            impl_->cand_cnt = carve<int>(A, nbrick_);
+            impl_->cand_off = carve<int64_t>(A, nbrick_ + 1);
+            impl_->brick_emax = carve<float>(A, nbrick_);
+            impl_->work_keys = carve<uint32_t>(A, nbrick_);
+            impl_->work = carve<uint32_t>(A, nbrick_);
+            impl_->sort_tmp = carve<char>(A, radix_sort_tmp_bytes(nbrick_));
+        }
+        if (commit) return;
+    };
+    A.clear_need();
+    plan(false);
+    if (A.overflowed()) {
+        A.reserve(A.need());
+        plan(true);
+    }
+    // ---- outputs
+    Arena& O = impl_->outs;
+    auto plan_out = [&]() {
+        O.reset();
+        occ_ = opts_.want_occ ? carve<uint8_t>(O, nvox_) : nullptr;
+        sdf32_ = opts_.want_sdf32 ? carve<float>(O, nvox_) : nullptr;
+        sdf64_ = opts_.want_sdf64 ? carve<double>(O, nvox_) : nullptr;
+        near_tri_ = opts_.want_near ? carve<int>(O, nvox_) : nullptr;
+        near_reg_ = opts_.want_near ? carve<uint8_t>(O, nvox_) : nullptr;
+        err_ = (opts_.want_err && opts_.precision == kPrecMixed) ? carve<float>(O, nvox_) : nullptr;
+    };
+    O.clear_need();
+    plan_out();
+    if (O.overflowed()) {
+        O.reserve(O.need());
+        plan_out();
+    }
+    if (!opts_.want_occ) occ_ = nullptr;
+
+    // ---- upload inputs (indices rebased to the concatenated point array)
+    std::vector<double> hp(static_cast<size_t>(3 * npts_));
+    std::vector<int> ht(static_cast<size_t>(3 * ntris_));
+    int64_t po = 0, to = 0;
+    for (const HostMesh& m : meshes) {
+        std::memcpy(hp.data() + 3 * po, m.pts, sizeof(double) * 3 * m.npts);
+        for (int64_t i = 0; i < 3 * m.ntris; ++i) ht[3 * to + i] = m.tris[i] + static_cast<int>(po);
+        po += m.npts;
+        to += m.ntris;
+    }
+    CMG_CUDA(cudaMemcpyAsync(pts_, hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice, stream_));
+    CMG_CUDA(cudaMemcpyAsync(tris_, ht.data(), sizeof(int) * ht.size(), cudaMemcpyHostToDevice, stream_));
+    CMG_CUDA(cudaMemcpyAsync(dsegs_, segs_.data(), sizeof(MeshSeg) * segs_.size(),
+                             cudaMemcpyHostToDevice, stream_));
+    CMG_CUDA(cudaStreamSynchronize(stream_));  // host vectors go out of scope
+    h2d_bytes_ = static_cast<int64_t>(sizeof(double) * hp.size() + sizeof(int) * ht.size());
+
+    const int sms = device_sms();
+    impl_->grid_exact = 2 * sms;
+    int per_sm = 1;
+    if (sdf) {
+        // persistent evaluation grid: resident CTAs per SM for the chosen kernel
+        per_sm = brick == 4 ? 8 : 3;
+    }
+    impl_->grid_eval = per_sm * sms;
+}
+
+Batch::~Batch() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (impl_ && impl_->graph) cudaGraphDestroy(impl_->graph);
+}
+
+void Batch::update_points(const std::vector<HostMesh>& meshes) {
+    std::vector<double> hp(static_cast<size_t>(3 * npts_));
+    int64_t po = 0;
+    for (const HostMesh& m : meshes) {
+        std::memcpy(hp.data() + 3 * po, m.pts, sizeof(double) * 3 * m.npts);
+        po += m.npts;
+    }
+    CMG_CUDA(cudaMemcpyAsync(pts_, hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice, stream_));
+    CMG_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Batch::update_points_device(const double* d_pts) {
+    CMG_CUDA(cudaMemcpyAsync(pts_, d_pts, sizeof(double) * 3 * npts_, cudaMemcpyDeviceToDevice, stream_));
+}
+
+void Batch::run() { run_impl(pairs_cap_ < 0 || cand_cap_ < 0); }
+
+void Batch::run_graph() {
+    if (pairs_cap_ < 0 || cand_cap_ < 0) {  // size first, outside the capture
+        run_impl(true);
+        CMG_CUDA(cudaStreamSynchronize(stream_));
+    }
+    if (!graph_) {
+        CMG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        run_impl(false);
+        CMG_CUDA(cudaStreamEndCapture(stream_, &impl_->graph));
+        CMG_CUDA(cudaGraphInstantiate(&graph_, impl_->graph, 0));
+    }
+    CMG_CUDA(cudaGraphLaunch(graph_, stream_));
+}
+
+void Batch::synchronize() { CMG_CUDA(cudaStreamSynchronize(stream_)); }
+
+void Batch::run_impl(bool sizing) {
+    Impl& I = *impl_;
+    cudaStream_t st = stream_;
+    const int nseg = static_cast<int>(segs_.size());
+    const bool sdf = opts_.want_sdf32 || opts_.want_sdf64 || opts_.want_near;
+    uint8_t* occ = opts_.want_occ ? occ_ : I.occ_internal;
+
+    CMG_CUDA(cudaMemsetAsync(stats_, 0, sizeof(Stats), st));
+    launch_tri_prep(dsegs_, nseg, ntris_, pts_, tris_, I.soup, I.xybox, I.pairs_n, st);
+    exclusive_scan(I.pairs_n, I.pair_off, ntris_, I.scan_tmp, st);
+    if (sizing) {
+        int64_t P = 0;
+        CMG_CUDA(cudaMemcpyAsync(&P, I.pair_off + ntris_, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        Arena& B = I.pairs;
+        auto planb = [&]() {
+            B.reset();
+            I.col_list = carve<int>(B, P);
+            I.hs = carve<double>(B, P);
+            I.hv = carve<uint8_t>(B, P);
+        };
+        B.clear_need();
+        planb();
+        if (B.overflowed()) {
+            B.reserve(B.need());
+            planb();
+        }
+        pairs_cap_ = P;
+    }
+    const int pair_grid = 4 * device_sms();
+    CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), st));
+    launch_col_pairs(false, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, nullptr, nullptr,
+                     pair_grid, st);
+    exclusive_scan(I.colcnt, I.col_off, ncol_, I.scan_tmp, st);
+    CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), st));
+    launch_col_pairs(true, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, I.col_off,
+                     I.col_list, pair_grid, st);
+    launch_occ_filter(opts_.predicates, dsegs_, nseg, nrow_, I.soup, I.col_off, I.col_list, occ,
+                      I.flagged, stats_, st);
+    launch_occ_exact(opts_.predicates, dsegs_, nseg, I.soup, I.col_off, I.col_list, I.flagged,
+                     I.hs, I.hv, occ, stats_, I.grid_exact, st);
+    if (!sdf) return;
+
+    CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
+    CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
+    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * nseg, st));
+    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tlo, I.thi, I.tbin, I.bincnt,
+                        I.large_cnt, I.emax_bits, st);
+    exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);
+    exclusive_scan(I.large_cnt, I.large_off, nseg, I.scan_tmp, st);
+    launch_seg_finish(dsegs_, nseg, I.large_off, I.emax_bits, st);
+    CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
+    CMG_CUDA(cudaMemsetAsync(I.large_cnt + nseg, 0, sizeof(int) * nseg, st));
+    launch_bin_fill(ntris_, I.tbin, I.bin_off, I.bincnt, I.bin_list, dsegs_, nseg,
+                    I.large_cnt + nseg, I.large_list, st);
+    launch_brick_walk(false, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
+                      I.bin_list, I.large_list, I.bound, I.cand_cnt, nullptr, nullptr, nullptr,
+                      stats_, st);
+    exclusive_scan(I.cand_cnt, I.cand_off, nbrick_, I.scan_tmp, st);
+    if (sizing) {
+        int64_t C = 0;
+        CMG_CUDA(cudaMemcpyAsync(&C, I.cand_off + nbrick_, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        Arena& Cn = I.cands;
+        auto planc = [&]() {
+            Cn.reset();
+            I.cand = carve<int>(Cn, C);
+        };
+        Cn.clear_need();
+        planc();
+        if (Cn.overflowed()) {
+            Cn.reserve(Cn.need());
+            planc();
+        }
+        cand_cap_ = C;
+    }
+    launch_brick_walk(true, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
+                      I.bin_list, I.large_list, I.bound, I.cand_cnt, I.cand_off, I.cand,
+                      I.brick_emax, stats_, st);
+    launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
+    radix_sort_pairs(I.work_keys, I.work, nbrick_, 32, I.sort_tmp, st);
+    CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
+    launch_sdf_eval(opts_.precision, opts_.brick, dsegs_, nseg, I.work, nbrick_, queue_, I.soup,
+                    I.tinfo, I.cand_off, I.cand, I.brick_emax, opts_.band, occ, sdf32_, sdf64_,
+                    near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
+}
+
+int64_t Batch::d2h_bytes() const {
+    int64_t b = 0;
+    if (occ_) b += nvox_;
+    if (sdf32_) b += 4 * nvox_;
+    if (sdf64_) b += 8 * nvox_;
+    if (near_tri_) b += 5 * nvox_;
+    if (err_) b += 4 * nvox_;
+    return b;
+}
+
+RunInfo Batch::info() {
+    RunInfo r;
+    CMG_CUDA(cudaMemcpyAsync(&r.stats, stats_, sizeof(Stats), cudaMemcpyDeviceToHost, stream_));
+    CMG_CUDA(cudaStreamSynchronize(stream_));
+    r.brick = opts_.brick;
+    r.cells = nvox_;
+    r.pairs = pairs_cap_;
+    r.candidates = cand_cap_;
+    return r;
+}
+
+void Batch::download(std::vector<HostResult>& out, RunInfo* info) {
+    out.resize(segs_.size());
+    for (size_t m = 0; m < segs_.size(); ++m) {
+        const MeshSeg& s = segs_[m];
+        const int64_t n = static_cast<int64_t>(s.g.nx) * s.g.ny * s.g.nz;
+        HostResult& r = out[m];
+        auto get = [&](auto* dev, auto& vec) {
+            if (!dev) return;
+            vec.resize(static_cast<size_t>(n));
+            CMG_CUDA(cudaMemcpyAsync(vec.data(), dev + s.vox_begin, sizeof(vec[0]) * n,
+                                     cudaMemcpyDeviceToHost, stream_));
+        };
+        get(occ_, r.occ);
+        get(sdf32_, r.sdf32);
+        get(sdf64_, r.sdf64);
+        get(near_tri_, r.near_tri);
+        get(near_reg_, r.near_reg);
+        get(err_, r.err);
+    }
+    CMG_CUDA(cudaStreamSynchronize(stream_));
+    if (info) *info = this->info();
+}
+
+// ------------------------------------------------------------------ autotuner
+int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int>, int> cache;
+    int64_t tris = 0, cells = 0;
+    for (const HostMesh& m : meshes) {
+        tris += m.ntris;
+        cells += static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
+    }
+    auto lg = [](int64_t v) { return v > 0 ? static_cast<int>(std::log2(static_cast<double>(v)) * 2) : 0; };
+    auto key = std::make_tuple(opts.precision, lg(tris), lg(cells), static_cast<int>(meshes.size() > 1));
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    float best_ms = 0.f;
+    int best = 8;
+    cudaEvent_t e0, e1;
+    CMG_CUDA(cudaEventCreate(&e0));
+    CMG_CUDA(cudaEventCreate(&e1));
+    for (int b : {4, 8}) {
+        VoxOpts o = opts;
+        o.brick = b;
+        o.autotune = false;
+        Batch bt(meshes, o, stream);
+        bt.run();  // sizing run (warms up as well)
+        bt.synchronize();
+        CMG_CUDA(cudaEventRecord(e0, stream));
+        bt.run();
+        CMG_CUDA(cudaEventRecord(e1, stream));
+        CMG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (b == 4 || ms < best_ms) {
+            best_ms = ms;
+            best = b;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> g(mu);
+    cache[key] = best;
+    return best;
+}
+
+}  // namespace cmg::gpu

@@ -1,0 +1,141 @@
+// engine.h — host orchestration of the voxelization pipeline on one GPU.
+//
+// A Batch holds one or more meshes (each with its own grid) resident on the
+// device, the workspace sized for them, and the device outputs. run() enqueues
+// the whole pipeline on a stream:
+//   occupancy: triangle prep -> per-column buckets -> FP64 filter -> exact pass
+//   SDF:       triangle bins -> brick candidate lists -> LPT work order ->
+//              persistent evaluation (plain FP64 or mixed FP32 + FP64 band)
+// The first run sizes the workspace (it reads two totals back from the device);
+// later runs allocate nothing and synchronise nothing, so they can be captured in
+// a CUDA graph and replayed.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "cmg_types.h"
+
+namespace cmg::gpu {
+
+struct VoxOpts {
+    int predicates = kPredCompat;  // kPredCompat (reference semantics) | kPredExact
+    int precision = kPrecFP64;     // kPrecFP64 (plain, bit-exact) | kPrecMixed
+    int brick = 0;                 // 4 or 8 cells per brick edge; 0 = tuned/default
+    float band = 1.0f;             // mixed: FP64 refinement band, in cells
+    bool want_occ = true;
+    bool want_sdf32 = false;
+    bool want_sdf64 = false;
+    bool want_near = false;        // nearest triangle id + Ericson region per cell
+    bool want_err = false;         // mixed: stated per-cell FP32 error bound
+    bool autotune = false;
+};
+
+struct HostMesh {
+    const double* pts = nullptr;  // 3*npts
+    int64_t npts = 0;
+    const int* tris = nullptr;    // 3*ntris, indices into pts
+    int64_t ntris = 0;
+    GridDesc g{};
+};
+
+struct HostResult {
+    std::vector<uint8_t> occ;
+    std::vector<float> sdf32;
+    std::vector<double> sdf64;
+    std::vector<int> near_tri;
+    std::vector<uint8_t> near_reg;
+    std::vector<float> err;
+};
+
+struct RunInfo {
+    Stats stats{};
+    int brick = 0;
+    int64_t cells = 0;
+    int64_t pairs = 0;       // (triangle, column) bucket entries
+    int64_t candidates = 0;  // (brick, triangle) candidate entries
+};
+
+class Batch {
+public:
+    // Uploads the meshes (host buffers) and plans the workspace. Grids must be set.
+    // A transient batch borrows the device's shared workspace (at most one alive
+    // per device at a time); otherwise the batch owns its memory.
+    Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream,
+          bool transient = false);
+    ~Batch();
+    Batch(const Batch&) = delete;
+    Batch& operator=(const Batch&) = delete;
+
+    // Re-uploads point coordinates (same topology and grids), e.g. between
+    // forward passes of an optimisation.
+    void update_points(const std::vector<HostMesh>& meshes);
+    // Device-pointer form: the coordinates already live on the device
+    // (concatenated, 3 doubles per point, triangle indices unchanged).
+    void update_points_device(const double* d_pts);
+
+    // Enqueues the pipeline. The first call sizes the workspace (synchronising);
+    // later calls only enqueue.
+    void run();
+    // Captures run() into a CUDA graph once, then replays it.
+    void run_graph();
+    void synchronize();
+    void download(std::vector<HostResult>& out, RunInfo* info);
+    RunInfo info();
+
+    int nmeshes() const { return static_cast<int>(segs_.size()); }
+    const std::vector<MeshSeg>& segs() const { return segs_; }
+    int64_t total_cells() const { return nvox_; }
+    int64_t total_points() const { return npts_; }
+    int64_t total_tris() const { return ntris_; }
+    const VoxOpts& opts() const { return opts_; }
+    cudaStream_t stream() const { return stream_; }
+    // device outputs (nullptr unless requested)
+    uint8_t* d_occ() const { return occ_; }
+    float* d_sdf32() const { return sdf32_; }
+    double* d_sdf64() const { return sdf64_; }
+    int* d_near_tri() const { return near_tri_; }
+    uint8_t* d_near_reg() const { return near_reg_; }
+    const double* d_points() const { return pts_; }
+    const int* d_tris() const { return tris_; }
+    // Bytes moved host->device by construction / update_points and device->host by
+    // download (the e2e accounting).
+    int64_t h2d_bytes() const { return h2d_bytes_; }
+    int64_t d2h_bytes() const;
+
+private:
+    struct Impl;
+    std::unique_ptr<Impl> impl_;
+    VoxOpts opts_;
+    cudaStream_t stream_;
+    std::vector<MeshSeg> segs_;
+    int64_t npts_ = 0, ntris_ = 0, ncol_ = 0, nrow_ = 0, nvox_ = 0, nbrick_ = 0;
+    int64_t pairs_cap_ = -1, cand_cap_ = -1;
+    double* pts_ = nullptr;
+    int* tris_ = nullptr;
+    MeshSeg* dsegs_ = nullptr;
+    uint8_t* occ_ = nullptr;
+    float* sdf32_ = nullptr;
+    double* sdf64_ = nullptr;
+    int* near_tri_ = nullptr;
+    uint8_t* near_reg_ = nullptr;
+    float* err_ = nullptr;
+    Stats* stats_ = nullptr;
+    unsigned long long* queue_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    int64_t h2d_bytes_ = 0;
+    void run_impl(bool sizing);
+};
+
+// Chooses the brick edge for a workload by timing both on the device (cached per
+// process by workload shape). Returns 4 or 8.
+int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream);
+
+// Number of SMs of the current device.
+int device_sms();
+
+}  // namespace cmg::gpu

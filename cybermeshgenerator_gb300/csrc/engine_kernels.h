@@ -1,0 +1,50 @@
+// engine_kernels.h — host launchers of the device kernels (one per .cu file).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "cmg_types.h"
+
+namespace cmg::gpu {
+
+// occupancy.cu
+void launch_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* pts,
+                     const int* tris, double* soup, int4* xybox, int64_t* pairs, cudaStream_t st);
+void launch_col_pairs(bool fill, const MeshSeg* segs, int nseg, int64_t ntris, const int4* xybox,
+                      const int64_t* pair_off, int* colcnt, const int64_t* col_off, int* col_list,
+                      int grid, cudaStream_t st);
+void launch_occ_filter(int mode, const MeshSeg* segs, int nseg, int64_t nrows, const double* soup,
+                       const int64_t* col_off, const int* col_list, uint8_t* occ, int64_t* flagged,
+                       Stats* stats, cudaStream_t st);
+void launch_occ_exact(int mode, const MeshSeg* segs, int nseg, const double* soup,
+                      const int64_t* col_off, const int* col_list, const int64_t* flagged,
+                      double* hs, uint8_t* hv, uint8_t* occ, Stats* stats, int grid,
+                      cudaStream_t st);
+int occ_row_cols();
+
+// sdf.cu
+void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
+                         float4* tinfo, float4* tlo, float4* thi, int64_t* tbin, int* bincnt,
+                         int* large_cnt, unsigned* emax_bits, cudaStream_t st);
+void launch_bin_fill(int64_t ntris, const int64_t* tbin, const int64_t* bin_off, int* bincur,
+                     int* bin_list, const MeshSeg* segs, int nseg, int* large_cur, int* large_list,
+                     cudaStream_t st);
+void launch_seg_finish(MeshSeg* segs, int nseg, const int64_t* large_off, const unsigned* emax_bits,
+                       cudaStream_t st);
+void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks, const double* soup,
+                       const float4* tinfo, const float4* tlo, const float4* thi,
+                       const int64_t* bin_off, const int* bin_list, const int* large_list,
+                       float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
+                       float* brick_emax, Stats* stats, cudaStream_t st);
+void launch_work_keys(const int* cand_cnt, int64_t n, uint32_t* keys, uint32_t* vals,
+                      cudaStream_t st);
+void launch_sdf_eval(int precision, int brick, const MeshSeg* segs, int nseg, const uint32_t* work,
+                     int64_t nwork, unsigned long long* queue, const double* soup,
+                     const float4* tinfo, const int64_t* cand_off, const int* cand,
+                     const float* brick_emax, float band_cells, const uint8_t* occ, float* sdf32,
+                     double* sdf64, int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats,
+                     int grid, cudaStream_t st);
+
+}  // namespace cmg::gpu

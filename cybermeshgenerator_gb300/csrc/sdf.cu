@@ -1,0 +1,912 @@
+// sdf.cu — signed distance field: nearest boundary triangle per cell.
+//
+// The reference computes, per cell centre, the minimum of point_tri_dist2
+// (Ericson, src/voxelize/voxelize.cpp:202-247) over the triangles found by a
+// Chebyshev ring search of 3-D buckets (:251-326); its pruning is exact, so the
+// result equals the brute-force minimum over all triangles. Here:
+//
+//   k_sdf_tri_prep   centroid c_t, radius e_t = max |v - c_t| (rounded up), bin of
+//                    c_t in the brick grid; triangles larger than two bricks (or
+//                    degenerate) go to a per-mesh "always considered" list
+//   k_bin_fill       bin -> triangle CSR
+//   k_brick_walk     one warp per brick: a ring walk over bins gives an upper bound
+//                    U on the distance from the brick centre to the surface, then
+//                    the candidate list = every triangle whose lower bound
+//                    |c - c_t| - e_t - r_B can be <= U + r_B (r_B = brick radius),
+//                    with margins far above FP32 and FP64 rounding
+//   k_sdf_fp64       one CTA per brick, candidates staged through shared memory;
+//                    each thread owns voxels and evaluates Ericson in the reference
+//                    operation order (FP64, no FMA): bit-identical to the reference
+//   k_sdf_mixed      same walk in FP32 on brick-recentred coordinates (normals from
+//                    FP64) with a stated error bound; cells within a band of the
+//                    surface are re-evaluated in FP64 over the candidates whose
+//                    FP32 distance is within twice the bound of the best, which
+//                    reproduces the FP64 minimum exactly there.
+// Both evaluation kernels skip a candidate for a whole warp when no lane's cells
+// can reach it (bounding sphere of the triangle vs the current best).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <climits>
+
+#include "cmg_device.cuh"
+#include "cmg_seg.cuh"
+#include "cmg_types.h"
+#include "cmg_util.h"
+#include "engine_kernels.h"
+
+namespace cmg::gpu {
+
+namespace {
+
+constexpr float kU32 = 5.9604645e-8f;  // 2^-24
+
+// ------------------------------------------------------------------ FP64 Ericson
+// Squared distance and region, reference operation order (voxelize.cpp:202-247).
+__device__ __forceinline__ double dot3r(double ax, double ay, double az, double bx, double by,
+                                        double bz) {
+    return dadd(dadd(dmul(ax, bx), dmul(ay, by)), dmul(az, bz));
+}
+__device__ __forceinline__ double d2r(const d3& p, double qx, double qy, double qz) {
+    double dx = dsub(p.x, qx), dy = dsub(p.y, qy), dz = dsub(p.z, qz);
+    return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+
+__device__ __noinline__ double ericson(const d3& p, const d3& a, const d3& b, const d3& c,
+                                       int* region) {
+    double abx = dsub(b.x, a.x), aby = dsub(b.y, a.y), abz = dsub(b.z, a.z);
+    double acx = dsub(c.x, a.x), acy = dsub(c.y, a.y), acz = dsub(c.z, a.z);
+    double apx = dsub(p.x, a.x), apy = dsub(p.y, a.y), apz = dsub(p.z, a.z);
+    double d1 = dot3r(abx, aby, abz, apx, apy, apz), d2 = dot3r(acx, acy, acz, apx, apy, apz);
+    if (d1 <= 0 && d2 <= 0) { *region = 0; return d2r(p, a.x, a.y, a.z); }
+    double bpx = dsub(p.x, b.x), bpy = dsub(p.y, b.y), bpz = dsub(p.z, b.z);
+    double d3v = dot3r(abx, aby, abz, bpx, bpy, bpz), d4 = dot3r(acx, acy, acz, bpx, bpy, bpz);
+    if (d3v >= 0 && d4 <= d3v) { *region = 1; return d2r(p, b.x, b.y, b.z); }
+    double vc = dsub(dmul(d1, d4), dmul(d3v, d2));
+    if (vc <= 0 && d1 >= 0 && d3v <= 0) {
+        double v = ddiv(d1, dsub(d1, d3v));
+        *region = 2;
+        return d2r(p, dadd(a.x, dmul(v, abx)), dadd(a.y, dmul(v, aby)), dadd(a.z, dmul(v, abz)));
+    }
+    double cpx = dsub(p.x, c.x), cpy = dsub(p.y, c.y), cpz = dsub(p.z, c.z);
+    double d5 = dot3r(abx, aby, abz, cpx, cpy, cpz), d6 = dot3r(acx, acy, acz, cpx, cpy, cpz);
+    if (d6 >= 0 && d5 <= d6) { *region = 3; return d2r(p, c.x, c.y, c.z); }
+    double vb = dsub(dmul(d5, d2), dmul(d1, d6));
+    if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+        double w = ddiv(d2, dsub(d2, d6));
+        *region = 4;
+        return d2r(p, dadd(a.x, dmul(w, acx)), dadd(a.y, dmul(w, acy)), dadd(a.z, dmul(w, acz)));
+    }
+    double va = dsub(dmul(d3v, d6), dmul(d5, d4));
+    double d43 = dsub(d4, d3v), d56 = dsub(d5, d6);
+    if (va <= 0 && d43 >= 0 && d56 >= 0) {
+        double w = ddiv(d43, dadd(d43, d56));
+        *region = 5;
+        return d2r(p, dadd(b.x, dmul(w, dsub(c.x, b.x))), dadd(b.y, dmul(w, dsub(c.y, b.y))),
+                   dadd(b.z, dmul(w, dsub(c.z, b.z))));
+    }
+    double denom = ddiv(1.0, dadd(dadd(va, vb), vc));
+    double v = dmul(vb, denom), w = dmul(vc, denom);
+    *region = 6;
+    return d2r(p, dadd(dadd(a.x, dmul(abx, v)), dmul(acx, w)),
+               dadd(dadd(a.y, dmul(aby, v)), dmul(acy, w)),
+               dadd(dadd(a.z, dmul(abz, v)), dmul(acz, w)));
+}
+
+__device__ __forceinline__ void load_soup(const double* __restrict__ soup, int64_t t, d3& a, d3& b,
+                                          d3& c) {
+    const double2* r = reinterpret_cast<const double2*>(soup + t * kSoupStride);
+    double2 v0 = __ldg(r), v1 = __ldg(r + 1), v2 = __ldg(r + 2), v3 = __ldg(r + 3), v4 = __ldg(r + 4);
+    a = {v0.x, v0.y, v1.x};
+    b = {v1.y, v2.x, v2.y};
+    c = {v3.x, v3.y, v4.x};
+}
+
+__device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
+
+// ------------------------------------------------------------------ triangle prep
+// tinfo (float4 per triangle): centroid relative to the mesh grid corner (FP32,
+// nearest) and the radius e_t rounded up (plus the rounding of the centroid).
+__global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64_t ntris,
+                               const double* __restrict__ soup, float4* __restrict__ tinfo,
+                               float4* __restrict__ tlo, float4* __restrict__ thi,
+                               int64_t* __restrict__ tbin, int* __restrict__ bincnt,
+                               int* __restrict__ large_cnt, unsigned* __restrict__ emax_bits) {
+    int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    const int si = find_seg<&MeshSeg::tri_begin>(segs, nseg, t);
+    const MeshSeg& s = segs[si];
+    d3 a, b, c;
+    load_soup(soup, t, a, b, c);
+    const double* K = s.g.corner;
+    // centroid in FP64 (any rounding is covered by the radius padding below)
+    double cx = (a.x + b.x + c.x) / 3.0, cy = (a.y + b.y + c.y) / 3.0, cz = (a.z + b.z + c.z) / 3.0;
+    double r2 = 0.0;
+    const d3 V[3] = {a, b, c};
+    double lo[3] = {a.x, a.y, a.z}, hi[3] = {a.x, a.y, a.z};
+    for (int k = 0; k < 3; ++k) {
+        double dx = V[k].x - cx, dy = V[k].y - cy, dz = V[k].z - cz;
+        r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+        lo[0] = fmin(lo[0], V[k].x); hi[0] = fmax(hi[0], V[k].x);
+        lo[1] = fmin(lo[1], V[k].y); hi[1] = fmax(hi[1], V[k].y);
+        lo[2] = fmin(lo[2], V[k].z); hi[2] = fmax(hi[2], V[k].z);
+    }
+    float4 ci;
+    ci.x = static_cast<float>(cx - K[0]);
+    ci.y = static_cast<float>(cy - K[1]);
+    ci.z = static_cast<float>(cz - K[2]);
+    // radius: sqrt rounded up, padded for the FP32 centroid (|err| <= u*|c - K|*sqrt3)
+    double pad = 2.0 * kU32 * (fabs(cx - K[0]) + fabs(cy - K[1]) + fabs(cz - K[2])) + 1e-300;
+    ci.w = round_up_f(sqrt(r2) * (1.0 + 1e-12) + pad);
+    tinfo[t] = ci;
+    tlo[t] = make_float4(__double2float_rd(lo[0] - K[0]), __double2float_rd(lo[1] - K[1]),
+                         __double2float_rd(lo[2] - K[2]), 0.f);
+    thi[t] = make_float4(__double2float_ru(hi[0] - K[0]), __double2float_ru(hi[1] - K[1]),
+                         __double2float_ru(hi[2] - K[2]), 0.f);
+    // degenerate (zero-area) or larger than two bricks: always considered
+    double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
+    double vx = c.x - a.x, vy = c.y - a.y, vz = c.z - a.z;
+    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    bool degenerate = !(nx * nx + ny * ny + nz * nz > 0.0);
+    const double bw = static_cast<double>(s.brick) * s.g.h;
+    bool large = degenerate || sqrt(r2) > 2.0 * bw;
+    if (large) {
+        tbin[t] = -1;
+        atomicAdd(&large_cnt[si], 1);
+        return;
+    }
+    atomicMax(&emax_bits[si], __float_as_uint(ci.w));
+    int bx = static_cast<int>(floor((cx - K[0]) / bw));
+    int by = static_cast<int>(floor((cy - K[1]) / bw));
+    int bz = static_cast<int>(floor((cz - K[2]) / bw));
+    bx = min(max(bx, 0), s.bnx - 1);
+    by = min(max(by, 0), s.bny - 1);
+    bz = min(max(bz, 0), s.bnz - 1);
+    int64_t bin = s.brick_begin + (static_cast<int64_t>(bz) * s.bny + by) * s.bnx + bx;
+    tbin[t] = bin;
+    atomicAdd(&bincnt[bin], 1);
+}
+
+__global__ void k_bin_fill(int64_t ntris, const int64_t* __restrict__ tbin,
+                           const int64_t* __restrict__ bin_off, int* __restrict__ bincur,
+                           int* __restrict__ bin_list, const MeshSeg* __restrict__ segs, int nseg,
+                           int* __restrict__ large_cur, int* __restrict__ large_list) {
+    int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    int64_t b = tbin[t];
+    if (b >= 0) {
+        int slot = atomicAdd(&bincur[b], 1);
+        bin_list[bin_off[b] + slot] = static_cast<int>(t);
+    } else {
+        const int si = find_seg<&MeshSeg::tri_begin>(segs, nseg, t);
+        int slot = atomicAdd(&large_cur[si], 1);
+        large_list[segs[si].large_begin + slot] = static_cast<int>(t);
+    }
+}
+
+// Writes each mesh's always-considered range and emax into its segment.
+__global__ void k_seg_finish(MeshSeg* segs, int nseg, const int64_t* __restrict__ large_off,
+                             const unsigned* __restrict__ emax_bits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nseg) return;
+    segs[i].large_begin = large_off[i];
+    segs[i].large_end = large_off[i + 1];
+    segs[i].emax = __uint_as_float(emax_bits[i]);
+}
+
+// ------------------------------------------------------------------ brick geometry
+struct BrickGeo {
+    int bx, by, bz;
+    int x0, y0, z0, x1, y1, z1;  // cell range [x0, x1)
+    float cx, cy, cz;            // centre of the cell-centre box, relative to the corner
+    float rb;                    // half-diagonal of that box (rounded up)
+};
+
+__device__ __forceinline__ BrickGeo brick_geo(const MeshSeg& s, int64_t lb) {
+    BrickGeo q;
+    q.bx = static_cast<int>(lb % s.bnx);
+    q.by = static_cast<int>((lb / s.bnx) % s.bny);
+    q.bz = static_cast<int>(lb / (static_cast<int64_t>(s.bnx) * s.bny));
+    const int B = s.brick;
+    q.x0 = q.bx * B; q.x1 = min(q.x0 + B, s.g.nx);
+    q.y0 = q.by * B; q.y1 = min(q.y0 + B, s.g.ny);
+    q.z0 = q.bz * B; q.z1 = min(q.z0 + B, s.g.nz);
+    const float h = static_cast<float>(s.g.h);
+    q.cx = 0.5f * (q.x0 + q.x1) * h;
+    q.cy = 0.5f * (q.y0 + q.y1) * h;
+    q.cz = 0.5f * (q.z0 + q.z1) * h;
+    double hx = 0.5 * (q.x1 - q.x0 - 1) * s.g.h, hy = 0.5 * (q.y1 - q.y0 - 1) * s.g.h,
+           hz = 0.5 * (q.z1 - q.z0 - 1) * s.g.h;
+    q.rb = __double2float_ru(sqrt(hx * hx + hy * hy + hz * hz) * (1.0 + 1e-9));
+    return q;
+}
+
+// Shell q of Chebyshev radius r -> offset (dx, dy, dz).
+__device__ __forceinline__ void shell_offset(int r, int q, int& dx, int& dy, int& dz) {
+    if (r == 0) { dx = dy = dz = 0; return; }
+    const int w = 2 * r + 1, v = 2 * r - 1;
+    const int A = w * w, Bn = w * v;
+    if (q < 2 * A) {
+        dz = (q / A) ? r : -r;
+        int rem = q % A;
+        dy = rem / w - r;
+        dx = rem % w - r;
+        return;
+    }
+    q -= 2 * A;
+    if (q < 2 * Bn) {
+        dy = (q / Bn) ? r : -r;
+        int rem = q % Bn;
+        dz = rem / w - (r - 1);
+        dx = rem % w - r;
+        return;
+    }
+    q -= 2 * Bn;
+    const int C = v * v;
+    dx = (q / C) ? r : -r;
+    int rem = q % C;
+    dz = rem / v - (r - 1);
+    dy = rem % v - (r - 1);
+}
+
+__device__ __forceinline__ int shell_count(int r) { return r == 0 ? 1 : 24 * r * r + 2; }
+
+// Upper bound on the distance from point c (corner-relative) to a large triangle:
+// the distance to its nearest edge point (segments), plus rounding margin.
+__device__ __forceinline__ float seg_dist(float px, float py, float pz, float ax, float ay, float az,
+                                          float bx, float by, float bz) {
+    float ex = bx - ax, ey = by - ay, ez = bz - az;
+    float qx = px - ax, qy = py - ay, qz = pz - az;
+    float ee = ex * ex + ey * ey + ez * ez;
+    float t = ee > 0.f ? __saturatef((qx * ex + qy * ey + qz * ez) / ee) : 0.f;
+    qx -= t * ex; qy -= t * ey; qz -= t * ez;
+    return sqrtf(qx * qx + qy * qy + qz * qz);
+}
+
+__device__ __forceinline__ float large_upper(const double* __restrict__ soup, int64_t t,
+                                             const double* K, float cx, float cy, float cz,
+                                             float tol) {
+    d3 a, b, c;
+    load_soup(soup, t, a, b, c);
+    float ax = static_cast<float>(a.x - K[0]), ay = static_cast<float>(a.y - K[1]),
+          az = static_cast<float>(a.z - K[2]);
+    float bx = static_cast<float>(b.x - K[0]), by = static_cast<float>(b.y - K[1]),
+          bz = static_cast<float>(b.z - K[2]);
+    float qx = static_cast<float>(c.x - K[0]), qy = static_cast<float>(c.y - K[1]),
+          qz = static_cast<float>(c.z - K[2]);
+    float d = fminf(seg_dist(cx, cy, cz, ax, ay, az, bx, by, bz),
+                    fminf(seg_dist(cx, cy, cz, bx, by, bz, qx, qy, qz),
+                          seg_dist(cx, cy, cz, qx, qy, qz, ax, ay, az)));
+    return d * (1.f + 16.f * kU32) + tol;
+}
+
+__device__ __forceinline__ float aabb_dist(float cx, float cy, float cz, float4 lo, float4 hi) {
+    float dx = fmaxf(0.f, fmaxf(lo.x - cx, cx - hi.x));
+    float dy = fmaxf(0.f, fmaxf(lo.y - cy, cy - hi.y));
+    float dz = fmaxf(0.f, fmaxf(lo.z - cz, cz - hi.z));
+    return sqrtf(dx * dx + dy * dy + dz * dz) * (1.f - 8.f * kU32);
+}
+
+// One warp per brick. FILL=false: computes U (stored) and the candidate count;
+// FILL=true: writes the candidates in walk order.
+template <bool FILL>
+__global__ void __launch_bounds__(128)
+k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
+             const double* __restrict__ soup, const float4* __restrict__ tinfo,
+             const float4* __restrict__ tlo, const float4* __restrict__ thi,
+             const int64_t* __restrict__ bin_off, const int* __restrict__ bin_list,
+             const int* __restrict__ large_list, float* __restrict__ bound,
+             int* __restrict__ cand_cnt, const int64_t* __restrict__ cand_off,
+             int* __restrict__ cand, float* __restrict__ brick_emax,
+             Stats* __restrict__ st) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gb = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (gb >= nbricks) return;
+    const int si = find_seg<&MeshSeg::brick_begin>(segs, nseg, gb);
+    const MeshSeg& s = segs[si];
+    const BrickGeo q = brick_geo(s, gb - s.brick_begin);
+    const float bw = static_cast<float>(s.brick * s.g.h);
+    const float tol = 8.f * kU32 * s.scale + 1e-30f;
+    const float emax = s.emax;
+    const int rmax = max(s.bnx, max(s.bny, s.bnz));
+    float U;
+    if (!FILL) {
+        // ---- upper bound on the distance from the brick centre to the surface
+        U = FLT_MAX;
+        for (int64_t e = s.large_begin + lane; e < s.large_end; e += 32)
+            U = fminf(U, large_upper(soup, large_list[e], s.g.corner, q.cx, q.cy, q.cz, tol));
+        for (int r = 0; r <= rmax; ++r) {
+            U = warp_min(U);
+            if (r > 0 && (r - 1) * bw > U) break;  // farther bins cannot lower U
+            const int n = shell_count(r);
+            bool inside = false;
+            for (int k = lane; k < n; k += 32) {
+                int dx, dy, dz;
+                shell_offset(r, k, dx, dy, dz);
+                int x = q.bx + dx, y = q.by + dy, z = q.bz + dz;
+                if (x < 0 || y < 0 || z < 0 || x >= s.bnx || y >= s.bny || z >= s.bnz) continue;
+                inside = true;
+                int64_t bin = s.brick_begin + (static_cast<int64_t>(z) * s.bny + y) * s.bnx + x;
+                for (int64_t e = bin_off[bin]; e < bin_off[bin + 1]; ++e) {
+                    float4 ti = tinfo[bin_list[e]];
+                    float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
+                    float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f + 4.f * kU32);
+                    U = fminf(U, d + ti.w + tol);
+                }
+            }
+            if (r > 0 && !__any_sync(0xffffffffu, inside)) {
+                U = warp_min(U);
+                break;
+            }
+        }
+        U = warp_min(U);
+        if (lane == 0) bound[gb] = U;
+    } else {
+        U = bound[gb];
+    }
+    // ---- candidates: lower bound <= U + 2 r_B (+ margins)
+    const float lim = (U + 2.f * q.rb) * (1.f + 1e-5f) + 2.f * tol;
+    int count = 0;
+    int64_t out = FILL ? cand_off[gb] : 0;
+    float bemax = 0.f;
+    auto emit = [&](bool take, int t, float et) {
+        unsigned m = __ballot_sync(0xffffffffu, take);
+        if (FILL && take) cand[out + count + __popc(m & ((1u << lane) - 1u))] = t;
+        if (take) bemax = fmaxf(bemax, et);
+        count += __popc(m);
+    };
+    for (int64_t e0 = s.large_begin; e0 < s.large_end; e0 += 32) {
+        int64_t e = e0 + lane;
+        bool take = false;
+        int t = 0;
+        float et = 0.f;
+        if (e < s.large_end) {
+            t = large_list[e];
+            float4 lo = tlo[t], hi = thi[t];
+            float d = aabb_dist(q.cx, q.cy, q.cz, lo, hi);
+            take = d <= lim;  // d(v,t) >= d - r_B must reach U + r_B
+            et = tinfo[t].w;
+        }
+        emit(take, t, et);
+    }
+    for (int r = 0; r <= rmax; ++r) {
+        if (r > 0 && (r - 1) * bw - emax > lim) break;
+        const int n = shell_count(r);
+        bool any_inside = false;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            int k = k0 + lane;
+            int64_t bin = -1;
+            if (k < n) {
+                int dx, dy, dz;
+                shell_offset(r, k, dx, dy, dz);
+                int x = q.bx + dx, y = q.by + dy, z = q.bz + dz;
+                if (!(x < 0 || y < 0 || z < 0 || x >= s.bnx || y >= s.bny || z >= s.bnz))
+                    bin = s.brick_begin + (static_cast<int64_t>(z) * s.bny + y) * s.bnx + x;
+            }
+            any_inside |= bin >= 0;
+            int64_t e = bin >= 0 ? bin_off[bin] : 0, eend = bin >= 0 ? bin_off[bin + 1] : 0;
+            // all lanes loop until every lane has drained its bin (ballot-ordered emits)
+            while (__any_sync(0xffffffffu, e < eend)) {
+                bool take = false;
+                int t = 0;
+                float et = 0.f;
+                if (e < eend) {
+                    t = bin_list[e];
+                    float4 ti = tinfo[t];
+                    float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
+                    float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f - 4.f * kU32);
+                    take = d - ti.w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
+                    et = ti.w;
+                    ++e;
+                }
+                emit(take, t, et);
+            }
+        }
+        if (r > 0 && !__any_sync(0xffffffffu, any_inside)) break;
+    }
+    if (!FILL && lane == 0) {
+        cand_cnt[gb] = count;
+        atomicAdd(&st->candidates, static_cast<unsigned long long>(count));
+    }
+    if (FILL) {
+        bemax = warp_min(-bemax);
+        if (lane == 0) brick_emax[gb] = -bemax;
+    }
+}
+
+// ------------------------------------------------------------------ evaluation
+constexpr int kChunk = 64;  // candidates staged per round
+
+// Cell owned by (thread, slot) inside a brick of edge B.
+template <int B, int THREADS>
+struct CellMap {
+    static constexpr int VPT = B * B * B / THREADS;
+    __device__ static void cell(int tid, int v, int& x, int& y, int& z) {
+        // threads tile x (fastest), then y, then z-slabs; each thread owns VPT cells in z
+        x = tid % B;
+        y = (tid / B) % B;
+        int zslab = tid / (B * B);
+        z = zslab * VPT + v;
+    }
+};
+
+struct Out {
+    const uint8_t* occ;
+    float* sdf32;
+    double* sdf64;
+    int* near_tri;
+    uint8_t* near_reg;
+    float* errbound;   // mixed: per-cell stated FP32 error bound (nullable)
+};
+
+__device__ __forceinline__ void write_cell(const Out& o, int64_t idx, double d, int tri, int reg) {
+    const bool in = o.occ[idx] != 0;
+    const double sd = in ? -d : d;
+    if (o.sdf64) o.sdf64[idx] = sd;
+    if (o.sdf32) o.sdf32[idx] = __double2float_rn(sd);
+    if (o.near_tri) o.near_tri[idx] = tri;
+    if (o.near_reg) o.near_reg[idx] = static_cast<uint8_t>(reg);
+}
+
+// Plain FP64: CTA per brick (persistent over a work list), THREADS threads.
+template <int B, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_sdf_fp64(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict__ work,
+           int64_t nwork, unsigned long long* __restrict__ queue, const double* __restrict__ soup,
+           const float4* __restrict__ tinfo, const int64_t* __restrict__ cand_off,
+           const int* __restrict__ cand, Out o, Stats* __restrict__ st) {
+    using M = CellMap<B, THREADS>;
+    constexpr int VPT = M::VPT;
+    __shared__ double sv[kChunk][12];  // a, b, c, centroid (FP64)
+    __shared__ double srad[kChunk];
+    __shared__ int sid[kChunk];
+    __shared__ int64_t s_item;
+    const int tid = threadIdx.x;
+    unsigned long long evals = 0;
+    for (;;) {
+        if (tid == 0) s_item = static_cast<int64_t>(atomicAdd(queue, 1ull));
+        __syncthreads();
+        const int64_t item = s_item;
+        __syncthreads();
+        if (item >= nwork) break;
+        const int64_t gb = static_cast<int64_t>(work[item]);
+        const int si = find_seg<&MeshSeg::brick_begin>(segs, nseg, gb);
+        const MeshSeg& s = segs[si];
+        const BrickGeo q = brick_geo(s, gb - s.brick_begin);
+        const GridDesc g = s.g;
+        d3 p[VPT];
+        bool valid[VPT];
+        double best[VPT], bestd[VPT];
+        int bt[VPT], br[VPT];
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            int x, y, z;
+            M::cell(tid, v, x, y, z);
+            x += q.x0; y += q.y0; z += q.z0;
+            valid[v] = x < q.x1 && y < q.y1 && z < q.z1;
+            p[v] = {cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
+                    cell_center(g.corner[2], z, g.h)};
+            best[v] = DBL_MAX;
+            bestd[v] = DBL_MAX;
+            bt[v] = INT_MAX;
+            br[v] = 0;
+        }
+        const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
+        for (int64_t base = c0; base < c1; base += kChunk) {
+            const int n = static_cast<int>(c1 - base < kChunk ? c1 - base : kChunk);
+            __syncthreads();
+            for (int k = tid; k < n; k += THREADS) {
+                int t = cand[base + k];
+                d3 a, b, c;
+                load_soup(soup, t, a, b, c);
+                sv[k][0] = a.x; sv[k][1] = a.y; sv[k][2] = a.z;
+                sv[k][3] = b.x; sv[k][4] = b.y; sv[k][5] = b.z;
+                sv[k][6] = c.x; sv[k][7] = c.y; sv[k][8] = c.z;
+                float4 ti = tinfo[t];
+                sv[k][9] = g.corner[0] + ti.x;
+                sv[k][10] = g.corner[1] + ti.y;
+                sv[k][11] = g.corner[2] + ti.z;
+                srad[k] = static_cast<double>(ti.w) * (1.0 + 1e-6) + 1e-9 * s.scale;
+                sid[k] = t;
+            }
+            __syncthreads();
+            for (int k = 0; k < n; ++k) {
+                // warp-uniform skip: the bounding sphere is beyond every lane's best
+                bool need = false;
+#pragma unroll
+                for (int v = 0; v < VPT; ++v) {
+                    double dx = p[v].x - sv[k][9], dy = p[v].y - sv[k][10], dz = p[v].z - sv[k][11];
+                    double lim = bestd[v] + srad[k];
+                    need |= valid[v] && (bestd[v] == DBL_MAX || dx * dx + dy * dy + dz * dz <= lim * lim);
+                }
+                if (!__any_sync(0xffffffffu, need)) continue;
+                const d3 a{sv[k][0], sv[k][1], sv[k][2]}, b{sv[k][3], sv[k][4], sv[k][5]},
+                    c{sv[k][6], sv[k][7], sv[k][8]};
+                const int t = sid[k];
+#pragma unroll
+                for (int v = 0; v < VPT; ++v) {
+                    if (!valid[v]) continue;
+                    int reg;
+                    double d2 = ericson(p[v], a, b, c, &reg);
+                    ++evals;
+                    if (d2 < best[v] || (d2 == best[v] && t < bt[v])) {
+                        best[v] = d2;
+                        bt[v] = t;
+                        br[v] = reg;
+                        bestd[v] = sqrt(d2) * (1.0 + 1e-9);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            if (!valid[v]) continue;
+            int x, y, z;
+            M::cell(tid, v, x, y, z);
+            x += q.x0; y += q.y0; z += q.z0;
+            int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+            write_cell(o, idx, __dsqrt_rn(best[v]), bt[v], br[v]);
+        }
+    }
+    long long ev = warp_sum(static_cast<long long>(evals));
+    if ((tid & 31) == 0 && ev) {
+        atomicAdd(&st->evaluations, static_cast<unsigned long long>(ev));
+        atomicAdd(&st->fp64_evaluations, static_cast<unsigned long long>(ev));
+    }
+}
+
+// FP32 record of a candidate, recentred on the brick centre.
+struct alignas(16) Rec32 {
+    float v0[3], v1[3], v2[3];   // vertices
+    float e0[3], e1[3], e2[3];   // edges v1-v0, v2-v1, v0-v2
+    float nn[3];                 // unit normal (from FP64)
+    float m0[3], m1[3], m2[3];   // in-plane inward edge normals
+    float inv[3];                // 1 / |e_k|^2 (0 for a degenerate edge)
+    float cen[3], rad;           // bounding sphere
+    float ok;                    // 1: plane branch allowed (non-degenerate)
+    int tid;
+    float pad_[1];
+};
+static_assert(sizeof(Rec32) == 160, "record layout");
+
+__device__ __forceinline__ void make_rec(Rec32& r, const d3& a, const d3& b, const d3& c,
+                                         const double* cb, float rad, int t) {
+    float v[9] = {static_cast<float>(a.x - cb[0]), static_cast<float>(a.y - cb[1]),
+                  static_cast<float>(a.z - cb[2]), static_cast<float>(b.x - cb[0]),
+                  static_cast<float>(b.y - cb[1]), static_cast<float>(b.z - cb[2]),
+                  static_cast<float>(c.x - cb[0]), static_cast<float>(c.y - cb[1]),
+                  static_cast<float>(c.z - cb[2])};
+    for (int k = 0; k < 3; ++k) {
+        r.v0[k] = v[k]; r.v1[k] = v[3 + k]; r.v2[k] = v[6 + k];
+        r.e0[k] = v[3 + k] - v[k];
+        r.e1[k] = v[6 + k] - v[3 + k];
+        r.e2[k] = v[k] - v[6 + k];
+    }
+    // normal in FP64 from the FP64 vertices, then normalised in FP32
+    double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
+    double wx = c.x - a.x, wy = c.y - a.y, wz = c.z - a.z;
+    double nx = uy * wz - uz * wy, ny = uz * wx - ux * wz, nz = ux * wy - uy * wx;
+    double nl = sqrt(nx * nx + ny * ny + nz * nz);
+    float ok = nl > 0.0 ? 1.f : 0.f;
+    float n3[3] = {0.f, 0.f, 0.f};
+    if (nl > 0.0) {
+        n3[0] = static_cast<float>(nx / nl);
+        n3[1] = static_cast<float>(ny / nl);
+        n3[2] = static_cast<float>(nz / nl);
+    }
+    r.nn[0] = n3[0]; r.nn[1] = n3[1]; r.nn[2] = n3[2];
+    const float* E[3] = {r.e0, r.e1, r.e2};
+    float* Mv[3] = {r.m0, r.m1, r.m2};
+    for (int k = 0; k < 3; ++k) {
+        const float* e = E[k];
+        // n x e points into the triangle for a counter-clockwise (about n) edge
+        Mv[k][0] = n3[1] * e[2] - n3[2] * e[1];
+        Mv[k][1] = n3[2] * e[0] - n3[0] * e[2];
+        Mv[k][2] = n3[0] * e[1] - n3[1] * e[0];
+        float ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+        r.inv[k] = ee > 0.f ? 1.f / ee : 0.f;
+    }
+    r.cen[0] = (v[0] + v[3] + v[6]) * (1.f / 3.f);
+    r.cen[1] = (v[1] + v[4] + v[7]) * (1.f / 3.f);
+    r.cen[2] = (v[2] + v[5] + v[8]) * (1.f / 3.f);
+    r.rad = rad * (1.f + 64.f * kU32);
+    r.ok = ok;
+    r.tid = t;
+}
+
+// FP32 squared distance from p to the recorded triangle; region in Ericson's
+// numbering (0 a, 1 b, 2 ab, 3 c, 4 ac, 5 bc, 6 interior).
+__device__ __forceinline__ float dist32(const Rec32& r, float px, float py, float pz, int* reg) {
+    float pax = px - r.v0[0], pay = py - r.v0[1], paz = pz - r.v0[2];
+    float pbx = px - r.v1[0], pby = py - r.v1[1], pbz = pz - r.v1[2];
+    float pcx = px - r.v2[0], pcy = py - r.v2[1], pcz = pz - r.v2[2];
+    float s0 = r.m0[0] * pax + r.m0[1] * pay + r.m0[2] * paz;
+    float s1 = r.m1[0] * pbx + r.m1[1] * pby + r.m1[2] * pbz;
+    float s2 = r.m2[0] * pcx + r.m2[1] * pcy + r.m2[2] * pcz;
+    if (r.ok > 0.f && s0 >= 0.f && s1 >= 0.f && s2 >= 0.f) {
+        float dp = r.nn[0] * pax + r.nn[1] * pay + r.nn[2] * paz;
+        *reg = 6;
+        return dp * dp;
+    }
+    float t0 = __saturatef((pax * r.e0[0] + pay * r.e0[1] + paz * r.e0[2]) * r.inv[0]);
+    float qx = pax - t0 * r.e0[0], qy = pay - t0 * r.e0[1], qz = paz - t0 * r.e0[2];
+    float d0 = qx * qx + qy * qy + qz * qz;
+    float t1 = __saturatef((pbx * r.e1[0] + pby * r.e1[1] + pbz * r.e1[2]) * r.inv[1]);
+    qx = pbx - t1 * r.e1[0]; qy = pby - t1 * r.e1[1]; qz = pbz - t1 * r.e1[2];
+    float d1 = qx * qx + qy * qy + qz * qz;
+    float t2 = __saturatef((pcx * r.e2[0] + pcy * r.e2[1] + pcz * r.e2[2]) * r.inv[2]);
+    qx = pcx - t2 * r.e2[0]; qy = pcy - t2 * r.e2[1]; qz = pcz - t2 * r.e2[2];
+    float d2 = qx * qx + qy * qy + qz * qz;
+    float d = d0;
+    int g = t0 <= 0.f ? 0 : (t0 >= 1.f ? 1 : 2);
+    if (d1 < d) { d = d1; g = t1 <= 0.f ? 1 : (t1 >= 1.f ? 3 : 5); }
+    if (d2 < d) { d = d2; g = t2 <= 0.f ? 3 : (t2 >= 1.f ? 0 : 4); }
+    *reg = g;
+    return d;
+}
+
+template <int B, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_sdf_mixed(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict__ work,
+            int64_t nwork, unsigned long long* __restrict__ queue, const double* __restrict__ soup,
+            const float4* __restrict__ tinfo, const int64_t* __restrict__ cand_off,
+            const int* __restrict__ cand, const float* __restrict__ brick_emax, float band_cells,
+            Out o, Stats* __restrict__ st) {
+    using M = CellMap<B, THREADS>;
+    constexpr int VPT = M::VPT;
+    __shared__ Rec32 rec[kChunk];
+    __shared__ int64_t s_item;
+    __shared__ int s_band;
+    const int tid = threadIdx.x;
+    unsigned long long evals = 0, evals64 = 0, bandc = 0;
+    for (;;) {
+        if (tid == 0) {
+            s_item = static_cast<int64_t>(atomicAdd(queue, 1ull));
+            s_band = 0;
+        }
+        __syncthreads();
+        const int64_t item = s_item;
+        if (item >= nwork) break;
+        const int64_t gb = static_cast<int64_t>(work[item]);
+        const int si = find_seg<&MeshSeg::brick_begin>(segs, nseg, gb);
+        const MeshSeg& s = segs[si];
+        const BrickGeo q = brick_geo(s, gb - s.brick_begin);
+        const GridDesc g = s.g;
+        // brick centre in FP64 (the recentring origin)
+        const double cb[3] = {g.corner[0] + 0.5 * (q.x0 + q.x1) * g.h,
+                              g.corner[1] + 0.5 * (q.y0 + q.y1) * g.h,
+                              g.corner[2] + 0.5 * (q.z0 + q.z1) * g.h};
+        float px[VPT], py[VPT], pz[VPT], best[VPT], bestd[VPT];
+        int bt[VPT], br[VPT];
+        bool valid[VPT];
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            int x, y, z;
+            M::cell(tid, v, x, y, z);
+            x += q.x0; y += q.y0; z += q.z0;
+            valid[v] = x < q.x1 && y < q.y1 && z < q.z1;
+            px[v] = static_cast<float>(cell_center(g.corner[0], x, g.h) - cb[0]);
+            py[v] = static_cast<float>(cell_center(g.corner[1], y, g.h) - cb[1]);
+            pz[v] = static_cast<float>(cell_center(g.corner[2], z, g.h) - cb[2]);
+            best[v] = FLT_MAX;
+            bestd[v] = FLT_MAX;
+            bt[v] = INT_MAX;
+            br[v] = 0;
+        }
+        const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
+        for (int64_t base = c0; base < c1; base += kChunk) {
+            const int n = static_cast<int>(c1 - base < kChunk ? c1 - base : kChunk);
+            __syncthreads();
+            for (int k = tid; k < n; k += THREADS) {
+                int t = cand[base + k];
+                d3 a, b, c;
+                load_soup(soup, t, a, b, c);
+                make_rec(rec[k], a, b, c, cb, tinfo[t].w, t);
+            }
+            __syncthreads();
+            for (int k = 0; k < n; ++k) {
+                const Rec32& r = rec[k];
+                bool need = false;
+#pragma unroll
+                for (int v = 0; v < VPT; ++v) {
+                    float dx = px[v] - r.cen[0], dy = py[v] - r.cen[1], dz = pz[v] - r.cen[2];
+                    float lim = bestd[v] + r.rad;
+                    need |= valid[v] && dx * dx + dy * dy + dz * dz <= lim * lim;
+                }
+                if (!__any_sync(0xffffffffu, need)) continue;
+#pragma unroll
+                for (int v = 0; v < VPT; ++v) {
+                    if (!valid[v]) continue;
+                    int reg;
+                    float d2 = dist32(r, px[v], py[v], pz[v], &reg);
+                    ++evals;
+                    if (d2 < best[v] || (d2 == best[v] && r.tid < bt[v])) {
+                        best[v] = d2;
+                        bt[v] = r.tid;
+                        br[v] = reg;
+                        bestd[v] = sqrtf(d2) * (1.f + 4.f * kU32) + 1e-30f;
+                    }
+                }
+            }
+        }
+        // stated FP32 error bound per cell and the FP64 band
+        const float emx = brick_emax[gb];
+        const float bandw = band_cells * static_cast<float>(g.h);
+        float eb[VPT];
+        bool inband[VPT];
+        bool any_band = false;
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            float d = sqrtf(best[v]);
+            eb[v] = 48.f * kU32 * (d + 2.f * emx + 2.f * q.rb) + 1e-30f;
+            inband[v] = valid[v] && d <= bandw + eb[v];
+            any_band |= inband[v];
+        }
+        if (any_band) s_band = 1;
+        __syncthreads();
+        double best64[VPT];
+        int bt64[VPT], br64[VPT];
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            best64[v] = DBL_MAX;
+            bt64[v] = INT_MAX;
+            br64[v] = 0;
+        }
+        if (s_band) {
+            // FP64 refinement over candidates within 2*eb of the FP32 best
+            for (int64_t base = c0; base < c1; base += kChunk) {
+                const int n = static_cast<int>(c1 - base < kChunk ? c1 - base : kChunk);
+                __syncthreads();
+                for (int k = tid; k < n; k += THREADS) {
+                    int t = cand[base + k];
+                    d3 a, b, c;
+                    load_soup(soup, t, a, b, c);
+                    make_rec(rec[k], a, b, c, cb, tinfo[t].w, t);
+                }
+                __syncthreads();
+                for (int k = 0; k < n; ++k) {
+                    const Rec32& r = rec[k];
+#pragma unroll
+                    for (int v = 0; v < VPT; ++v) {
+                        if (!inband[v]) continue;
+                        int reg;
+                        float d2 = dist32(r, px[v], py[v], pz[v], &reg);
+                        float lim = sqrtf(best[v]) + 2.f * eb[v];
+                        if (sqrtf(d2) > lim * (1.f + 1e-6f)) continue;
+                        d3 a, b, c;
+                        load_soup(soup, r.tid, a, b, c);
+                        int x, y, z;
+                        M::cell(tid, v, x, y, z);
+                        x += q.x0; y += q.y0; z += q.z0;
+                        const d3 P{cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
+                                   cell_center(g.corner[2], z, g.h)};
+                        int r64;
+                        double e2 = ericson(P, a, b, c, &r64);
+                        ++evals64;
+                        if (e2 < best64[v] || (e2 == best64[v] && r.tid < bt64[v])) {
+                            best64[v] = e2;
+                            bt64[v] = r.tid;
+                            br64[v] = r64;
+                        }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            if (!valid[v]) continue;
+            int x, y, z;
+            M::cell(tid, v, x, y, z);
+            x += q.x0; y += q.y0; z += q.z0;
+            int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+            if (inband[v]) {
+                ++bandc;
+                write_cell(o, idx, __dsqrt_rn(best64[v]), bt64[v], br64[v]);
+                if (o.errbound) o.errbound[idx] = 0.f;
+            } else {
+                write_cell(o, idx, static_cast<double>(sqrtf(best[v])), bt[v], br[v]);
+                if (o.errbound) o.errbound[idx] = eb[v];
+            }
+        }
+        __syncthreads();
+    }
+    long long ev = warp_sum(static_cast<long long>(evals));
+    long long ev64 = warp_sum(static_cast<long long>(evals64));
+    long long bc = warp_sum(static_cast<long long>(bandc));
+    if ((tid & 31) == 0) {
+        if (ev) atomicAdd(&st->evaluations, static_cast<unsigned long long>(ev));
+        if (ev64) atomicAdd(&st->fp64_evaluations, static_cast<unsigned long long>(ev64));
+        if (bc) atomicAdd(&st->band_voxels, static_cast<unsigned long long>(bc));
+    }
+}
+
+// LPT order of the bricks: key = ~count so an ascending sort puts the most
+// expensive bricks first.
+__global__ void k_work_keys(const int* __restrict__ cand_cnt, int64_t n, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+    int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    keys[b] = ~static_cast<uint32_t>(cand_cnt[b]);
+    vals[b] = static_cast<uint32_t>(b);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
+                         float4* tinfo, float4* tlo, float4* thi, int64_t* tbin, int* bincnt,
+                         int* large_cnt, unsigned* emax_bits, cudaStream_t st) {
+    if (ntris == 0) return;
+    k_sdf_tri_prep<<<static_cast<unsigned>((ntris + 255) / 256), 256, 0, st>>>(
+        segs, nseg, ntris, soup, tinfo, tlo, thi, tbin, bincnt, large_cnt, emax_bits);
+    CMG_LAUNCH();
+}
+
+void launch_bin_fill(int64_t ntris, const int64_t* tbin, const int64_t* bin_off, int* bincur,
+                     int* bin_list, const MeshSeg* segs, int nseg, int* large_cur, int* large_list,
+                     cudaStream_t st) {
+    if (ntris == 0) return;
+    k_bin_fill<<<static_cast<unsigned>((ntris + 255) / 256), 256, 0, st>>>(
+        ntris, tbin, bin_off, bincur, bin_list, segs, nseg, large_cur, large_list);
+    CMG_LAUNCH();
+}
+
+void launch_seg_finish(MeshSeg* segs, int nseg, const int64_t* large_off, const unsigned* emax_bits,
+                       cudaStream_t st) {
+    k_seg_finish<<<(nseg + 127) / 128, 128, 0, st>>>(segs, nseg, large_off, emax_bits);
+    CMG_LAUNCH();
+}
+
+void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks, const double* soup,
+                       const float4* tinfo, const float4* tlo, const float4* thi,
+                       const int64_t* bin_off, const int* bin_list, const int* large_list,
+                       float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
+                       float* brick_emax, Stats* stats, cudaStream_t st) {
+    if (nbricks == 0) return;
+    unsigned grid = static_cast<unsigned>((nbricks + 3) / 4);
+    if (fill)
+        k_brick_walk<true><<<grid, 128, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi, bin_off,
+                                                 bin_list, large_list, bound, cand_cnt, cand_off,
+                                                 cand, brick_emax, stats);
+    else
+        k_brick_walk<false><<<grid, 128, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi,
+                                                  bin_off, bin_list, large_list, bound, cand_cnt,
+                                                  cand_off, cand, brick_emax, stats);
+    CMG_LAUNCH();
+}
+
+void launch_work_keys(const int* cand_cnt, int64_t n, uint32_t* keys, uint32_t* vals,
+                      cudaStream_t st) {
+    if (n == 0) return;
+    k_work_keys<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(cand_cnt, n, keys, vals);
+    CMG_LAUNCH();
+}
+
+void launch_sdf_eval(int precision, int brick, const MeshSeg* segs, int nseg, const uint32_t* work,
+                     int64_t nwork, unsigned long long* queue, const double* soup,
+                     const float4* tinfo, const int64_t* cand_off, const int* cand,
+                     const float* brick_emax, float band_cells, const uint8_t* occ, float* sdf32,
+                     double* sdf64, int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats,
+                     int grid, cudaStream_t st) {
+    if (nwork == 0) return;
+    Out o{occ, sdf32, sdf64, near_tri, near_reg, errbound};
+    if (precision == kPrecMixed) {
+        if (brick == 4)
+            k_sdf_mixed<4, 64><<<grid, 64, 0, st>>>(segs, nseg, work, nwork, queue, soup, tinfo,
+                                                    cand_off, cand, brick_emax, band_cells, o, stats);
+        else
+            k_sdf_mixed<8, 128><<<grid, 128, 0, st>>>(segs, nseg, work, nwork, queue, soup, tinfo,
+                                                      cand_off, cand, brick_emax, band_cells, o,
+                                                      stats);
+    } else {
+        if (brick == 4)
+            k_sdf_fp64<4, 64><<<grid, 64, 0, st>>>(segs, nseg, work, nwork, queue, soup, tinfo,
+                                                   cand_off, cand, o, stats);
+        else
+            k_sdf_fp64<8, 128><<<grid, 128, 0, st>>>(segs, nseg, work, nwork, queue, soup, tinfo,
+                                                     cand_off, cand, o, stats);
+    }
+    CMG_LAUNCH();
+}
+
+}  // namespace cmg::gpu

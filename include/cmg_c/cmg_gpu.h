@@ -1,0 +1,112 @@
+/* cmg_gpu.h — GB300 additions to the reference C ABI (libcmg_c.so).
+ *
+ * None of these has a counterpart in the reference's bindings/c/include/cmg_c/
+ * cmg_c.h; they expose what the GPU path adds: an explicit grid, the FP64 and
+ * mixed-precision distance fields, exact-predicate occupancy, the nearest-feature
+ * checkpoint used by the adjoint, run statistics, and batches of meshes.
+ * cmg_plc_voxelize (cmg_c.h) keeps the reference's semantics exactly.
+ */
+#ifndef CMG_GPU_H
+#define CMG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cmg_c.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Output selection bits for cmg_voxel_opts.outputs. */
+#define CMG_OUT_OCCUPANCY 1   /* uint8 occupancy */
+#define CMG_OUT_SDF_F32 2     /* float signed distance (the reference's output) */
+#define CMG_OUT_SDF_F64 4     /* double signed distance (before the float cast) */
+#define CMG_OUT_NEAREST 8     /* nearest triangle id (int) + Ericson region (uint8) */
+#define CMG_OUT_ERROR_BOUND 16 /* mixed precision: stated per-cell bound (float) */
+
+/* Distance arithmetic. */
+#define CMG_PREC_FP64 0   /* all FP64, reference operation order: bit-identical */
+#define CMG_PREC_MIXED 1  /* FP32 on brick-recentred coordinates + FP64 band */
+
+/* Predicate semantics for occupancy. */
+#define CMG_PRED_COMPAT 0 /* the reference as initialised: sign of the rounded
+                             determinant unless it is exactly zero */
+#define CMG_PRED_EXACT 1  /* sign of the exact determinant */
+
+typedef struct cmg_voxel_opts {
+    int resolution;      /* cells along the longest bbox axis (>= 1), as cmg_plc_voxelize */
+    int pad;             /* margin cells per side */
+    int mode;            /* 0 occupancy, 1 signed distance: the outputs when outputs == 0 */
+    int outputs;         /* CMG_OUT_* bits; 0 = as `mode` selects */
+    int precision;       /* CMG_PREC_* */
+    int predicates;      /* CMG_PRED_* */
+    int explicit_grid;   /* nonzero: corner/spacing/dims replace resolution/pad */
+    double corner[3];    /* min corner of cell (0,0,0) */
+    double spacing;      /* cubic cell edge */
+    int dims[3];         /* nx, ny, nz */
+    double band;         /* mixed: FP64 refinement band around the surface, in cells */
+    int brick;           /* SDF brick edge: 0 = default, 4 or 8 */
+    int autotune;        /* nonzero: time brick edges on this input and keep the faster */
+} cmg_voxel_opts;
+
+/* Counters of one voxelization. */
+typedef struct cmg_voxel_stats {
+    int64_t cells;
+    int64_t flagged_columns;   /* occupancy columns resolved by the exact pass */
+    int64_t nudged_columns;    /* columns whose first attempt grazed an edge/vertex */
+    int64_t exhausted_columns; /* columns where every nudge grazed (partial result kept) */
+    int64_t exact_calls;       /* orient3d evaluations that needed exact arithmetic */
+    int64_t bucket_entries;    /* (triangle, column) pairs */
+    int64_t candidates;        /* (brick, triangle) SDF candidates */
+    int64_t evaluations;       /* (cell, triangle) distance evaluations */
+    int64_t fp64_evaluations;  /* of which in FP64 */
+    int64_t band_cells;        /* mixed: cells refined in FP64 */
+    int brick;                 /* brick edge used */
+    double max_error_bound;    /* mixed: largest stated per-cell bound (0 for FP64) */
+} cmg_voxel_stats;
+
+/* Defaults: resolution 64, pad 1, occupancy, FP64, compat predicates, band 1. */
+void cmg_voxel_opts_init(cmg_voxel_opts* opts);
+
+/* Voxelizes with explicit options. Same handle and error conventions as
+ * cmg_plc_voxelize; the grid holds every requested output. */
+cmg_status cmg_plc_voxelize_ex(const cmg_plc*, const cmg_voxel_opts* opts, cmg_voxels** out,
+                               char* errbuf, size_t errbuf_len);
+
+/* Extra views of a grid (NULL when not requested). */
+const double* cmg_voxels_distance_f64(const cmg_voxels*);
+const int* cmg_voxels_nearest_triangle(const cmg_voxels*);
+const unsigned char* cmg_voxels_nearest_region(const cmg_voxels*);
+const float* cmg_voxels_error_bound(const cmg_voxels*);
+/* Corner of cell (0,0,0) (the origin is its centre). */
+void cmg_voxels_corner(const cmg_voxels*, double* x, double* y, double* z);
+void cmg_voxels_stats(const cmg_voxels*, cmg_voxel_stats* out);
+
+/* ---- batches: many meshes, one pipeline ---------------------------------- */
+typedef struct cmg_batch cmg_batch;
+
+/* Plans a batch of n PLCs, mesh i voxelized with resolutions[i] and pads[i] (or,
+ * when opts->explicit_grid, every mesh on opts' grid). Inputs are uploaded once. */
+cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, const int* pads,
+                            int n, const cmg_voxel_opts* opts, cmg_batch** out, char* errbuf,
+                            size_t errbuf_len);
+/* Enqueues one pass over every mesh on the batch's stream. use_graph != 0
+ * captures the pass in a CUDA graph on first use and replays it afterwards. */
+cmg_status cmg_batch_run(cmg_batch*, int use_graph, char* errbuf, size_t errbuf_len);
+/* Waits for the batch's stream. */
+cmg_status cmg_batch_sync(cmg_batch*, char* errbuf, size_t errbuf_len);
+/* Copies mesh i's results into a new grid handle (cmg_voxels_destroy frees it). */
+cmg_status cmg_batch_get(cmg_batch*, int i, cmg_voxels** out, char* errbuf, size_t errbuf_len);
+int cmg_batch_size(const cmg_batch*);
+int64_t cmg_batch_cells(const cmg_batch*);
+void cmg_batch_destroy(cmg_batch*);
+
+/* Library build identification, e.g. "cmg-gb300 sm_103a". */
+const char* cmg_gpu_version(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* CMG_GPU_H */

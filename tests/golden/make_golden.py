@@ -1,0 +1,137 @@
+"""Generate the golden fixtures from the reference's own code.
+
+Run where the reference sources are available (it builds oracle/_ref from them):
+
+    python tests/golden/make_golden.py
+
+Every fixture stores its input mesh as raw float64/int32 bits (so hosts whose
+libm differs still see identical inputs) and the reference's outputs:
+  - occupancy through the public cmg::voxelize::voxelize (or classify_occupancy
+    on an explicit grid), bit-packed;
+  - float SDF through the public entry point (full, or its SHA-256 for big grids);
+  - FP64 squared distances at sampled cells from the reference's point_tri_dist2
+    (brute force, i.e. before the float cast);
+  - orient3d / insphere signs as the reference initialises them (robust::*) and
+    exact (predicates::*exact).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from cybermeshgenerator_gb300 import workloads as W  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
+def api_case(ref, name, pts, tris, resolution, pad, full_sdf=True, nsample=512, seed=0):
+    facets = [list(t) for t in tris]
+    st, origin, sp, dims, occ = ref.voxelize(pts, facets, resolution, pad, 0)
+    assert st == 0, (name, st)
+    st2, _, _, _, sdf = ref.voxelize(pts, facets, resolution, pad, 1)
+    assert st2 == 0
+    rc, corner, sp2, dims2 = ref.make_grid(pts, resolution, pad)
+    assert dims2 == dims and sp2 == sp
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(seed)
+    vox = np.sort(rng.choice(n, size=min(nsample, n), replace=False)).astype(np.int64)
+    d2 = ref.dist2_brute(pts, tris, corner, sp, dims, vox)
+    out = dict(points=pts, triangles=tris.astype(np.int32), resolution=np.int32(resolution),
+               pad=np.int32(pad), dims=np.array(dims, np.int32), corner=corner,
+               spacing=np.float64(sp), origin=origin, occ_bits=np.packbits(occ),
+               sdf32_sha=np.array(sha(sdf)), sample_vox=vox, sample_d2=d2)
+    if full_sdf:
+        out["sdf32"] = sdf
+    save(name, **out)
+    return occ, sdf
+
+
+def grid_case(ref, name, pts, tris, corner, spacing, dims, nsample=512, seed=0):
+    occ = ref.occupancy_grid(pts, tris, corner, spacing, dims)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(seed)
+    vox = np.sort(rng.choice(n, size=min(nsample, n), replace=False)).astype(np.int64)
+    d2 = ref.dist2_brute(pts, tris, corner, spacing, dims, vox)
+    save(name, points=pts, triangles=tris.astype(np.int32), dims=np.array(dims, np.int32),
+         corner=np.asarray(corner, np.float64), spacing=np.float64(spacing),
+         occ_bits=np.packbits(occ), occ_sha=np.array(sha(occ)), sample_vox=vox, sample_d2=d2)
+    return occ
+
+
+def pred_case(ref, name, n, seed):
+    out = {}
+    for kind, npt in (("orient3d", 4), ("insphere", 5)):
+        S = W.predicate_stream(n, kind, degenerate=0.25, near=0.25, seed=seed)
+        comp = np.zeros(n, np.int8)
+        ex = np.zeros(n, np.int8)
+        for i in range(n):
+            p = [S[3 * k:3 * k + 3, i] for k in range(npt)]
+            comp[i] = np.sign(ref.pred(kind, *p))
+            ex[i] = np.sign(ref.pred(kind + "exact", *p))
+        out[kind + "_soa"] = S
+        out[kind + "_compat"] = comp
+        out[kind + "_exact"] = ex
+    save(name, **out)
+
+
+def main():
+    O.build(ref=True)
+    ref = O.Reference()
+    manifest = {}
+
+    pts, tris = W.jittered_icosphere(3, 0.02, seed=1)
+    api_case(ref, "icosphere_s3_r58p3", pts, tris, 58, 3, nsample=2048)
+    manifest["icosphere_s3_r58p3"] = "icosphere subdivision 3, radial jitter 2% (seed 1); resolution 58, pad 3 (64^3)"
+
+    pts, tris = W.subdivided_cube(4)
+    api_case(ref, "cube4_r16p1", pts, tris, 16, 1)
+    manifest["cube4_r16p1"] = "reference test fixture subdivided_cube(4); resolution 16, pad 1 (exact 16^3 block)"
+
+    pts, tris = W.uv_sphere(1.0, 16, 16)
+    api_case(ref, "uvsphere16_r20p1", pts, tris, 20, 1)
+    manifest["uvsphere16_r20p1"] = "reference test fixture sphere_plc(1,16,16); resolution 20, pad 1"
+
+    pts, tris = W.brick(3.0, 1.0, 2.0)
+    api_case(ref, "brick312_r20p1", pts, tris, 20, 1)
+    manifest["brick312_r20p1"] = "box [0,3]x[0,1]x[0,2]; resolution 20, pad 1 (axis order)"
+
+    pts, tris = W.sh_sphere(nlon=64, nlat=32, seed=3)
+    api_case(ref, "shsphere64_r30p1", pts, tris, 30, 1)
+    manifest["shsphere64_r30p1"] = "SH star surface on a 64x32-band UV sphere (seed 3); resolution 30, pad 1"
+
+    pts, tris = W.box_and_torus(64, 32)
+    h = 2.0 ** -5
+    grid_case(ref, "boxtorus64_facegrid", pts, tris, [-16.5 * h, -16.5 * h, -10.5 * h], h, (64, 64, 64))
+    manifest["boxtorus64_facegrid"] = ("unit box + torus(R .35, r .12, 64x32) on an explicit 64^3 grid, h=2^-5, "
+                                       "cell centres exactly on the box faces (forces grazes)")
+    api_case(ref, "boxtorus64_r62p1", pts, tris, 62, 1, full_sdf=False)
+    manifest["boxtorus64_r62p1"] = "same mesh through the API, resolution 62, pad 1"
+
+    pts, tris = W.subdivided_cube(3)
+    grid_case(ref, "cube3_facegrid", pts, tris, [-4.5 / 12, -4.5 / 12, -4.5 / 12], 1.0 / 12, (20, 20, 20))
+    manifest["cube3_facegrid"] = "subdivided_cube(3) on a 20^3 grid, h=1/12, centres on faces and shared edges"
+
+    pred_case(ref, "predicates", 4096, seed=21)
+    manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
+
+    with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,133 @@
+"""The C ABI surface on the CPU: the library loads, exports every symbol the
+headers declare, and answers the reference's validation errors without touching
+a GPU (no compute call is made here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", "cmg_c", h) for h in ("cmg_c.h", "cmg_gpu.h")]
+
+# the 41 symbols the reference's ctypes binding touches at import
+# (bindings/python/src/cybermesh/__init__.py:58-157)
+REFERENCE_BOUND = """cmg_delaunay cmg_mesh_destroy cmg_mesh_face_markers cmg_mesh_faces
+cmg_mesh_num_faces cmg_mesh_num_points cmg_mesh_num_tets cmg_mesh_points cmg_mesh_tet_markers
+cmg_mesh_tets cmg_options_create cmg_options_destroy cmg_options_set_max_volume
+cmg_options_set_plc cmg_options_set_preserve_edges cmg_options_set_quality cmg_plc_add_facet
+cmg_plc_add_hole cmg_plc_add_region cmg_plc_create cmg_plc_destroy cmg_plc_num_points
+cmg_plc_num_triangles cmg_plc_points cmg_plc_set_points cmg_plc_simplify cmg_plc_triangles
+cmg_plc_voxelize cmg_read_mesh cmg_read_plc cmg_read_points cmg_tetrahedralize cmg_version
+cmg_voxels_destroy cmg_voxels_dims cmg_voxels_distance cmg_voxels_occupancy cmg_voxels_origin
+cmg_voxels_spacing cmg_write_mesh cmg_write_plc""".split()
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cybermeshgenerator_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def declared():
+    names = set()
+    for h in HEADERS:
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"\b(cmg_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_reference_symbols_declared():
+    assert len(REFERENCE_BOUND) == 41
+    assert set(REFERENCE_BOUND) <= set(declared())
+
+
+def test_every_declared_symbol_exported(lib):
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing
+
+
+def test_null_and_resolution_errors(lib):
+    out = ctypes.c_void_p(123)
+    err = ctypes.create_string_buffer(64)
+    assert lib.cmg_plc_voxelize(None, 8, 0, 1, ctypes.byref(out), err, 64) == 1
+    assert out.value is None
+    plc = lib.cmg_plc_create()
+    try:
+        assert lib.cmg_plc_voxelize(plc, 0, 0, 1, ctypes.byref(out), err, 64) == 1
+        assert err.value == b"resolution must be >= 1"
+        small = ctypes.create_string_buffer(8)
+        assert lib.cmg_plc_voxelize(plc, 0, 0, 1, ctypes.byref(out), small, 8) == 1
+        assert small.value == b"resolut"  # truncated to len-1 chars, NUL-terminated
+        assert lib.cmg_plc_voxelize(plc, 8, 0, 1, None, err, 64) == 1
+    finally:
+        lib.cmg_plc_destroy(plc)
+
+
+def test_empty_plc_is_invalid_input(lib):
+    # voxelize.cpp:366-372: no points / no boundary triangles -> InvalidInput,
+    # answered before any GPU work
+    from cybermeshgenerator_gb300 import _lib as L
+    plc = lib.cmg_plc_create()
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(128)
+    try:
+        assert lib.cmg_plc_voxelize(plc, 8, 0, 1, ctypes.byref(out), err, 128) == 1
+        assert err.value == b"voxelize: PLC has no points"
+        pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], dtype=np.float64)
+        lib.cmg_plc_set_points(plc, pts.ctypes.data_as(L.c_double_p), 3)
+        assert lib.cmg_plc_voxelize(plc, 8, 0, 1, ctypes.byref(out), err, 128) == 1
+        assert err.value == b"voxelize: PLC has no boundary triangles"
+        bad = np.array([0, 1, 7], dtype=np.int32)
+        lib.cmg_plc_add_facet(plc, bad.ctypes.data_as(L.c_int_p), 3, 0)
+        assert lib.cmg_plc_voxelize(plc, 8, 0, 1, ctypes.byref(out), err, 128) == 1
+        assert b"out of range" in err.value
+    finally:
+        lib.cmg_plc_destroy(plc)
+
+
+def test_facet_validation_and_readback(lib):
+    from cybermeshgenerator_gb300 import _lib as L
+    plc = lib.cmg_plc_create()
+    try:
+        pts = np.arange(15, dtype=np.float64).reshape(5, 3)
+        assert lib.cmg_plc_set_points(plc, pts.ctypes.data_as(L.c_double_p), 5) == 0
+        two = np.array([0, 1], dtype=np.int32)
+        assert lib.cmg_plc_add_facet(plc, two.ctypes.data_as(L.c_int_p), 2, 0) == 1
+        quad = np.array([0, 1, 2, 3, 4], dtype=np.int32)
+        assert lib.cmg_plc_add_facet(plc, quad.ctypes.data_as(L.c_int_p), 5, 7) == 0
+        n = lib.cmg_plc_num_triangles(plc)
+        tri = np.ctypeslib.as_array(lib.cmg_plc_triangles(plc), (n * 3,))
+        # fan (v0, v[i-1], v[i]) as voxelize.cpp:29-38
+        assert tri.tolist() == [0, 1, 2, 0, 2, 3, 0, 3, 4]
+        assert lib.cmg_plc_num_points(plc) == 5
+        back = np.ctypeslib.as_array(lib.cmg_plc_points(plc), (15,))
+        assert np.array_equal(back, pts.ravel())
+    finally:
+        lib.cmg_plc_destroy(plc)
+
+
+def test_out_of_scope_entry_points(lib):
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(256)
+    opts = lib.cmg_options_create()
+    plc = lib.cmg_plc_create()
+    try:
+        assert lib.cmg_tetrahedralize(plc, opts, ctypes.byref(out), err, 256) == 5
+        assert lib.cmg_read_plc(b"x.stl", ctypes.byref(out), err, 256) == 5
+        assert lib.cmg_mesh_num_points(None) == 0 and not lib.cmg_mesh_points(None)
+        assert lib.cmg_options_set_plc(opts, 1) == 0
+    finally:
+        lib.cmg_plc_destroy(plc)
+        lib.cmg_options_destroy(opts)
+
+
+def test_getters_tolerate_null(lib):
+    nx = ctypes.c_int(5)
+    lib.cmg_voxels_dims(None, ctypes.byref(nx), None, None)
+    assert nx.value == 0 and lib.cmg_voxels_spacing(None) == 0.0
+    assert not lib.cmg_voxels_occupancy(None) and not lib.cmg_voxels_distance(None)
+    assert lib.cmg_version() == b"0.5.0"

@@ -1,0 +1,104 @@
+"""The oracle restatement against outputs of the reference itself (tests/golden,
+made by tests/golden/make_golden.py from the reference's sources). Bit for bit."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import unpack_occ
+
+API_CASES = ["icosphere_s3_r58p3", "cube4_r16p1", "uvsphere16_r20p1", "brick312_r20p1",
+             "shsphere64_r30p1", "boxtorus64_r62p1"]
+GRID_CASES = ["boxtorus64_facegrid", "cube3_facegrid"]
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", API_CASES)
+def test_grid_setup(orc, golden, name):
+    g = golden(name)
+    grid = orc.make_grid(g["points"], int(g["resolution"]), int(g["pad"]))
+    assert grid.dims == tuple(int(d) for d in g["dims"])
+    assert grid.spacing == float(g["spacing"])
+    assert np.array_equal(np.array(grid.corner), g["corner"])
+
+
+@pytest.mark.parametrize("name", API_CASES)
+def test_occupancy_compat(orc, golden, name):
+    g = golden(name)
+    grid = orc.make_grid(g["points"], int(g["resolution"]), int(g["pad"]))
+    occ, _ = orc.occupancy(g["points"], g["triangles"], grid)
+    assert np.array_equal(occ, unpack_occ(g))
+
+
+@pytest.mark.parametrize("name", GRID_CASES)
+def test_occupancy_explicit_grid(orc, golden, name):
+    g = golden(name)
+    grid = orc.grid(g["corner"], g["spacing"], g["dims"])
+    occ, st = orc.occupancy(g["points"], g["triangles"], grid)
+    assert np.array_equal(occ, unpack_occ(g))
+    assert _sha(occ) == str(g["occ_sha"])
+
+
+def test_face_grid_forces_nudges(orc, golden):
+    g = golden("boxtorus64_facegrid")
+    grid = orc.grid(g["corner"], g["spacing"], g["dims"])
+    _, st = orc.occupancy(g["points"], g["triangles"], grid)
+    assert st["nudged_columns"] > 0
+    assert st["exact_calls"] > 0
+
+
+def test_known_answer_cube_block(golden):
+    # tests/test_voxelize.cpp:140-163: R=16, pad=1 -> exactly the 16^3 interior block
+    g = golden("cube4_r16p1")
+    nx, ny, nz = (int(d) for d in g["dims"])
+    occ = unpack_occ(g).reshape(nz, ny, nx)
+    block = np.zeros_like(occ)
+    block[1:17, 1:17, 1:17] = 1
+    assert np.array_equal(occ, block)
+
+
+@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "cube4_r16p1", "uvsphere16_r20p1",
+                                  "brick312_r20p1", "shsphere64_r30p1"])
+def test_sdf_float_bits(orc, golden, name):
+    g = golden(name)
+    grid = orc.make_grid(g["points"], int(g["resolution"]), int(g["pad"]))
+    occ = unpack_occ(g)
+    _, s32 = orc.sdf_ring(g["points"], g["triangles"], grid, occ)
+    assert _sha(s32) == str(g["sdf32_sha"])
+    if "sdf32" in g:
+        assert np.array_equal(s32.view(np.uint32), g["sdf32"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", API_CASES + GRID_CASES)
+def test_sdf64_samples_bruteforce(orc, golden, name):
+    g = golden(name)
+    grid = orc.grid(g["corner"], g["spacing"], g["dims"])
+    d2, _, _ = orc.sdf_brute(g["points"], g["triangles"], grid, g["sample_vox"])
+    assert np.array_equal(d2.view(np.uint64), g["sample_d2"].view(np.uint64))
+
+
+def test_ring_equals_bruteforce(orc, golden):
+    g = golden("uvsphere16_r20p1")
+    grid = orc.grid(g["corner"], g["spacing"], g["dims"])
+    vox = np.arange(grid.ncell)
+    d_ring = orc.sdf_ring_sample(g["points"], g["triangles"], grid, vox)
+    d_brute, _, _ = orc.sdf_brute(g["points"], g["triangles"], grid, vox)
+    assert np.array_equal(d_ring, d_brute)
+
+
+@pytest.mark.parametrize("kind", ["orient3d", "insphere"])
+@pytest.mark.parametrize("mode", ["compat", "exact"])
+def test_predicate_signs(orc, golden, kind, mode):
+    import oracle as O
+    g = golden("predicates")
+    got = orc.stream(kind, g[kind + "_soa"], O.COMPAT if mode == "compat" else O.EXACT)
+    assert np.array_equal(got, g[kind + "_" + mode])
+
+
+def test_compat_differs_from_exact(golden):
+    # the reference's as-initialised signs are not the exact ones on near cases
+    g = golden("predicates")
+    assert (g["orient3d_compat"] != g["orient3d_exact"]).sum() > 0
