@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Voxel-queries/s of the GB300 voxelization path (occupancy + signed distance).
+
+Workload: the star-shaped spherical-harmonic surface of 65,024 triangles (UV
+sphere, 256 x 128 bands, radius 1 + 8 real harmonics of degree <= 6, seed 3),
+voxelized with 256 cells on its longest axis (resolution 254, pad 1). One step =
+occupancy (exact ray parity, reference predicates) + the mixed-precision signed
+distance field (FP32 on brick-recentred coordinates, FP64 within one cell of the
+surface) for every cell; a voxel query = one cell's occupancy bit + SDF value.
+The plain all-FP64 path (bit-identical to the reference) is timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs its own replica (weak scaling; the path shares
+nothing between meshes), the timed region is bracketed by barriers and the
+slowest rank's time is used. --impl reference times the CPU restatement of the
+reference algorithm (oracle/, the reference's own code cannot travel to the GPU
+host) on this host's cores, on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "voxel-queries/s, 256³ grid/65k tris: mixed vs FP64 GPU at SDF err≤1e-6·diag"
+UNIT = "voxel-queries/s"
+RESOLUTION, PAD = 254, 1
+PT_FLOPS = 79      # FP64 flops of one Ericson point-triangle evaluation (interior path)
+O3D_FLOPS = 23     # flops of one rounded orient3d determinant
+PZ_FLOPS = 22      # flops of one plane_z
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload():
+    from cybermeshgenerator_gb300 import workloads as W
+    return W.sh_sphere(nlon=256, nlat=128, seed=3)
+
+
+def workload_desc(dims, ntris):
+    return {"workload": f"SH star surface, {ntris} triangles, resolution {RESOLUTION} pad {PAD} "
+                        f"({dims[0]}x{dims[1]}x{dims[2]} cells): occupancy + mixed SDF",
+            "triangles": int(ntris), "grid": [int(d) for d in dims],
+            "precision": "FP32 SDF on brick-recentred coordinates, FP64 band of 1 cell, FP64 predicates",
+            "l2": "flushed between timed steps (256 MB device write on the same stream)"}
+
+
+# --------------------------------------------------------------------------- dist
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM clock + throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.f.name) as fh:
+                for line in fh:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) >= 9 and p[1].isdigit():
+                        rows.append(p)
+            os.unlink(self.f.name)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [int(r[1]) for r in rows]
+        mx = int(rows[0][2])
+        loaded = [s for s, r in zip(sm, rows) if float(r[3] or 0) > 200.0] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v == "Active"})
+        return {"sm_mhz": float(statistics.median(loaded)), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------- ours
+def time_batch(cm, torch, batch, steps, warmup, flush):
+    """Device time of `steps` passes (CUDA events on the batch's stream), L2
+    flushed between passes outside the timed events."""
+    stream = torch.cuda.ExternalStream(batch.stream)
+    for _ in range(warmup):
+        batch.run()
+    batch.sync()
+    times = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch.run()
+            e1.record(stream)
+            times.append((e0, e1))
+    batch.sync()
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in times]
+
+
+def fraction_of_peak(work_flops, ms, peak):
+    achieved = work_flops / (ms * 1e-3)
+    return achieved, achieved / peak
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the evaluation kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_sdf_mixed_shsphere256.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None):
+    """The oracle (CPU restatement of the reference algorithm) on this host: full
+    occupancy plus the ring-search SDF on a uniform sample of cells, scaled to
+    the grid."""
+    import oracle
+    orc = oracle.Oracle()
+    threads = threads or os.cpu_count() or 1
+    corner, spacing, dims = dims_grid
+    g = orc.grid(corner, spacing, dims)
+    n = g.ncell
+    t0 = time.perf_counter()
+    orc.occupancy(pts, tris, g, threads=threads)
+    t_occ = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    t0 = time.perf_counter()
+    orc.sdf_ring_sample(pts, tris, g, np.array([n // 2]), threads=threads)
+    t_build = time.perf_counter() - t0
+    # size the sample from a small probe so the run stays near `seconds`
+    probe = rng.choice(n, size=2000, replace=False)
+    t0 = time.perf_counter()
+    orc.sdf_ring_sample(pts, tris, g, probe, threads=threads)
+    per = max((time.perf_counter() - t0 - t_build) / len(probe), 1e-9)
+    m = int(min(n, max(2000, (seconds - t_occ - 2 * t_build) / per)))
+    vox = rng.choice(n, size=m, replace=False)
+    t0 = time.perf_counter()
+    orc.sdf_ring_sample(pts, tris, g, vox, threads=threads)
+    t_s = time.perf_counter() - t0
+    t_full = t_occ + t_build + (t_s - t_build) * n / m
+    return {"value": n / t_full, "unit": UNIT, "cores": int(threads), "kind": "port",
+            "sample": f"occupancy on all {n} cells; ring-search SDF on {m} uniformly sampled cells "
+                      f"+ the 3-D bucket build, scaled to {n} cells (extrapolated)"}
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    pts, tris = workload()
+    plc = cm.PLC.from_arrays(pts, tris)
+    outs = cm.OUT_OCCUPANCY | cm.OUT_SDF_F32
+    mixed = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_MIXED, band=1.0,
+                     brick=args.brick)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    mixed.run().sync()  # sizing pass
+    cells = mixed.cells
+    r0 = mixed.result(0)
+    dims = r0.dims
+
+    l0 = cm.gpu_launches()
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ms = time_batch(cm, torch, mixed, args.steps, args.warmup, flush)
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // (args.steps + args.warmup)
+    total_ms = max_over_ranks(sum(ms), world)
+    value = cells * world * args.steps / (total_ms * 1e-3)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+            "config": dict(workload_desc(dims, len(tris)), parallelism=f"replicas x{world}"),
+            "gpu_launches": int(launches)}
+    clocks = clk.summary()
+    line["clocks"] = clocks
+
+    if rank == 0:
+        # phase times + cost model (one timed pass of each path)
+        mixed.set_timing(True)
+        mixed.run().sync()
+        tm = mixed.timing()
+        wm = mixed.work_model()
+        st = mixed.stats()
+        plain = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64,
+                         brick=args.brick)
+        plain.run().sync()
+        p_ms = time_batch(cm, torch, plain, max(1, min(3, args.steps)), 1, flush)
+        plain.set_timing(True)
+        plain.run().sync()
+        tp = plain.timing()
+        p_value = cells * len(p_ms) / (sum(p_ms) * 1e-3)
+        # accuracy of this run: mixed vs plain (FP64, bit-identical to the reference)
+        rm, rp = mixed.result(0), plain.result(0)
+        diag = float(np.linalg.norm(pts.max(0) - pts.min(0)))
+        err = np.abs(rm.sdf32.astype(np.float64) - rp.sdf32.astype(np.float64))
+        occ_same = bool(np.array_equal(rm.occupancy, rp.occupancy))
+        p32 = cm.peak_flops(False)
+        p64 = cm.peak_flops(True)
+        w_sdf = wm["sum_k"] * PT_FLOPS
+        ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
+        ach64, frac64 = fraction_of_peak(w_sdf, tp["eval_ms"], p64)
+        line["roofline"] = {
+            "bound": "fp32", "kernel": "k_sdf_mixed (distance evaluation)",
+            "achieved": ach / 1e12, "peak": p32 / 1e12, "unit": "TFLOP/s", "frac": frac,
+            "traffic": traffic_from_profile(),
+            "work": f"sum_v K(v) * {PT_FLOPS} = {w_sdf:.4g} flops per launch; K(v) = triangles whose "
+                    f"bounding sphere reaches the cell's distance sphere",
+            "peak_source": "measured FFMA microbenchmark on this GPU (no FP32 entry in MEASURED_PEAKS.json)",
+            "eval_ms": tm["eval_ms"], "phase_ms": tm,
+            "fp64_kernel": {"kernel": "k_sdf_fp64", "achieved": ach64 / 1e12, "peak": p64 / 1e12,
+                            "frac": frac64, "eval_ms": tp["eval_ms"], "phase_ms": tp,
+                            "peak_source": "measured DFMA microbenchmark (FMA = 2 flops)"}}
+        line["mixed_vs_fp64"] = {"fp64_value": p_value, "speedup": value / world / p_value,
+                                 "max_abs_err": float(err.max()), "rms_err": float(np.sqrt((err ** 2).mean())),
+                                 "tol": 1e-6 * diag, "within_tol": bool(err.max() <= 1e-6 * diag),
+                                 "occupancy_identical": occ_same,
+                                 "band_cells": int(st["band_cells"]),
+                                 "evaluations": int(st["evaluations"]),
+                                 "fp64_evaluations": int(st["fp64_evaluations"]),
+                                 "candidates": int(st["candidates"])}
+        # end to end through the C ABI with host buffers (upload, pipeline, download)
+        e2e_t = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            r = cm.voxelize_ex(plc, resolution=RESOLUTION, pad=PAD, outputs=outs,
+                               precision=cm.PREC_MIXED, band=1.0, brick=args.brick)
+            if i >= args.warmup:
+                e2e_t.append(time.perf_counter() - t0)
+        line["e2e"] = {"value": cells / (sum(e2e_t) / len(e2e_t)), "unit": UNIT,
+                       "h2d_bytes_per_step": int(pts.nbytes + tris.nbytes),
+                       "d2h_bytes_per_step": int(cells * (1 + 4)),
+                       "call": "cmg_plc_voxelize_ex (mixed, occupancy + float SDF), host buffers"}
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(pts, tris, (r0.corner, r0.spacing, r0.dims),
+                                                seconds=args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    barrier(world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------- reference
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    from cybermeshgenerator_gb300 import workloads as W  # noqa: F401
+    pts, tris = workload()
+    orc = oracle.Oracle()
+    g = orc.make_grid(pts, RESOLUTION, PAD)
+    budget = max(5.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        base = cpu_baseline(pts, tris, (tuple(g.corner), g.spacing, g.dims), seconds=budget)
+        if i >= args.warmup:
+            vals.append(base["value"])
+    value = float(statistics.median(vals))
+    base["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": g.ncell / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": dict(workload_desc(g.dims, len(tris)), parallelism="cpu threads"),
+            "cpu_baseline": base,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--brick", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

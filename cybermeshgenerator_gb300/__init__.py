@@ -304,11 +304,51 @@ class Batch:
         finally:
             _clib.cmg_voxels_destroy(out.value)
 
+    @property
+    def stream(self) -> int:
+        """The cudaStream_t (as an integer) the batch's kernels run on."""
+        return int(_clib.cmg_batch_stream(self._h) or 0)
+
+    def set_timing(self, on: bool = True) -> "Batch":
+        _clib.cmg_batch_set_timing(self._h, int(on))
+        return self
+
+    def timing(self) -> Dict[str, float]:
+        t = _L.BatchTiming()
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_get_timing(self._h, ctypes.byref(t), err, 512), err)
+        return t.as_dict()
+
+    def work_model(self) -> Dict[str, float]:
+        w = _L.WorkModel()
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_work_model(self._h, ctypes.byref(w), err, 512), err)
+        return w.as_dict()
+
+    def stats(self) -> Dict[str, float]:
+        st = _L.VoxelStats()
+        err = ctypes.create_string_buffer(512)
+        _check(_clib.cmg_batch_stats(self._h, ctypes.byref(st), err, 512), err)
+        return st.as_dict()
+
     def __del__(self) -> None:
         h = getattr(self, "_h", None)
         if h:
             _clib.cmg_batch_destroy(h)
             self._h = None
+
+
+def gpu_launches() -> int:
+    """Kernels launched by the library in this process."""
+    return int(_clib.cmg_gpu_launches())
+
+
+def peak_flops(fp64: bool) -> float:
+    """Measured FMA throughput of the current GPU in FLOP/s (FMA = 2)."""
+    v = ctypes.c_double()
+    err = ctypes.create_string_buffer(512)
+    _check(_clib.cmg_gpu_peak_flops(int(fp64), ctypes.byref(v), err, 512), err)
+    return v.value
 
 
 def version() -> str:

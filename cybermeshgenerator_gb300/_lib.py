@@ -45,6 +45,23 @@ class VoxelStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchTiming(ctypes.Structure):
+    _fields_ = [("occupancy_ms", ctypes.c_float), ("sdf_prep_ms", ctypes.c_float),
+                ("eval_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: float(getattr(self, k)) for k, _ in self._fields_}
+
+
+class WorkModel(ctypes.Structure):
+    _fields_ = [("sum_k", ctypes.c_double), ("sum_k_band", ctypes.c_double),
+                ("band_cells", ctypes.c_double), ("orient_calls", ctypes.c_double),
+                ("crossings", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: float(getattr(self, k)) for k, _ in self._fields_}
+
+
 def library_path() -> str:
     return os.environ.get("CMG_C_LIB") or IN_TREE
 
@@ -116,6 +133,13 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_batch_cells", ctypes.c_int64, [V])
     sig("cmg_batch_destroy", None, [V])
     sig("cmg_gpu_version", S, [])
+    sig("cmg_batch_stream", V, [V])
+    sig("cmg_batch_set_timing", I, [V, I])
+    sig("cmg_batch_get_timing", I, [V, ctypes.POINTER(BatchTiming), S, Z])
+    sig("cmg_batch_work_model", I, [V, ctypes.POINTER(WorkModel), S, Z])
+    sig("cmg_batch_stats", I, [V, ctypes.POINTER(VoxelStats), S, Z])
+    sig("cmg_gpu_launches", ctypes.c_longlong, [])
+    sig("cmg_gpu_peak_flops", I, [I, c_double_p, S, Z])
 
 
 _LIB = None

@@ -24,6 +24,7 @@
 
 #include "cmg_util.h"
 #include "engine.h"
+#include "engine_kernels.h"
 
 namespace {
 
@@ -516,6 +517,58 @@ void cmg_batch_destroy(cmg_batch* b) {
     if (!b) return;
     std::lock_guard<std::mutex> lk(gpu_mutex());
     delete b;
+}
+
+void* cmg_batch_stream(const cmg_batch* b) { return b ? static_cast<void*>(b->batch->stream()) : nullptr; }
+
+cmg_status cmg_batch_set_timing(cmg_batch* b, int on) {
+    if (!b) return CMG_ERR_INVALID_INPUT;
+    b->batch->set_timing(on != 0);
+    return CMG_OK;
+}
+
+cmg_status cmg_batch_get_timing(cmg_batch* b, cmg_batch_timing* out, char* errbuf, size_t len) {
+    if (!b || !out) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        cmg::gpu::Timing t = b->batch->timing();
+        out->occupancy_ms = t.occupancy_ms;
+        out->sdf_prep_ms = t.sdf_prep_ms;
+        out->eval_ms = t.eval_ms;
+        out->total_ms = t.total_ms;
+    });
+}
+
+cmg_status cmg_batch_work_model(cmg_batch* b, cmg_work_model* out, char* errbuf, size_t len) {
+    if (!b || !out) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cmg::gpu::WorkModel w = b->batch->work_model();
+        out->sum_k = w.sum_k;
+        out->sum_k_band = w.sum_k_band;
+        out->band_cells = w.band_cells;
+        out->orient_calls = w.orient_calls;
+        out->crossings = w.crossings;
+    });
+}
+
+cmg_status cmg_batch_stats(cmg_batch* b, cmg_voxel_stats* out, char* errbuf, size_t len) {
+    if (!b || !out) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        cmg_voxels v;
+        fill_stats(&v, b->batch->info());
+        *out = v.stats;
+        out->cells = b->batch->total_cells();
+    });
+}
+
+long long cmg_gpu_launches(void) { return cmg::gpu::launches(); }
+
+cmg_status cmg_gpu_peak_flops(int fp64, double* flops, char* errbuf, size_t len) {
+    if (!flops) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        *flops = cmg::gpu::peak_flops(fp64 != 0);
+    });
 }
 
 const char* cmg_gpu_version(void) { return "cmg-gb300 0.1.0 sm_103a"; }

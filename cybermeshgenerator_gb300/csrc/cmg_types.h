@@ -43,6 +43,8 @@ struct Stats {
     unsigned long long fp64_evaluations;   // of which in FP64
     unsigned long long band_voxels;        // mixed precision: voxels refined in FP64
     unsigned long long error_flags;        // nonzero: a kernel hit a capacity limit
+    unsigned long long orient_calls;       // occupancy filter: orient3d evaluations
+    unsigned long long crossings;          // occupancy filter: plane_z evaluations
 };
 
 enum : int { kPredCompat = 0, kPredExact = 1 };

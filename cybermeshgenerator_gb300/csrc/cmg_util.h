@@ -22,7 +22,14 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
                                std::to_string(line) + ")");
 }
 #define CMG_CUDA(x) ::cmg::gpu::cuda_check((x), #x, __FILE__, __LINE__)
-#define CMG_LAUNCH() ::cmg::gpu::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+// Kernels launched by this library (process-wide), for launch accounting.
+void note_launch(int n = 1);
+long long launches();
+#define CMG_LAUNCH()                                                                  \
+    do {                                                                              \
+        ::cmg::gpu::note_launch();                                                    \
+        ::cmg::gpu::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__); \
+    } while (0)
 
 // exclusive prefix sum: out[i] = sum_{j<i} in[j] for i in [0, n], out[n] = total.
 // tmp holds scan_tmp_elems(n) int64 values.

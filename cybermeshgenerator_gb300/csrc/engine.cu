@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -14,6 +15,12 @@
 #include "engine_kernels.h"
 
 namespace cmg::gpu {
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sms() {
     int dev = 0, sms = 0;
@@ -234,6 +241,8 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
 }
 
 Batch::~Batch() {
+    for (cudaEvent_t& e : ev_)
+        if (e) cudaEventDestroy(e);
     if (graph_) cudaGraphExecDestroy(graph_);
     if (impl_ && impl_->graph) cudaGraphDestroy(impl_->graph);
 }
@@ -277,6 +286,12 @@ void Batch::run_impl(bool sizing) {
     const int nseg = static_cast<int>(segs_.size());
     const bool sdf = opts_.want_sdf32 || opts_.want_sdf64 || opts_.want_near;
     uint8_t* occ = opts_.want_occ ? occ_ : I.occ_internal;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CMG_CUDA(cudaStreamIsCapturing(st, &cap));
+    const bool timed = timing_ && cap == cudaStreamCaptureStatusNone;
+    if (timed && !ev_[0])
+        for (cudaEvent_t& e : ev_) CMG_CUDA(cudaEventCreate(&e));
+    if (timed) CMG_CUDA(cudaEventRecord(ev_[0], st));
 
     CMG_CUDA(cudaMemsetAsync(stats_, 0, sizeof(Stats), st));
     launch_tri_prep(dsegs_, nseg, ntris_, pts_, tris_, I.soup, I.xybox, I.pairs_n, st);
@@ -312,7 +327,14 @@ void Batch::run_impl(bool sizing) {
                       I.flagged, stats_, st);
     launch_occ_exact(opts_.predicates, dsegs_, nseg, I.soup, I.col_off, I.col_list, I.flagged,
                      I.hs, I.hv, occ, stats_, I.grid_exact, st);
-    if (!sdf) return;
+    if (timed) CMG_CUDA(cudaEventRecord(ev_[1], st));
+    if (!sdf) {
+        if (timed) {
+            CMG_CUDA(cudaEventRecord(ev_[2], st));
+            CMG_CUDA(cudaEventRecord(ev_[3], st));
+        }
+        return;
+    }
 
     CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
     CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
@@ -353,9 +375,44 @@ void Batch::run_impl(bool sizing) {
     launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
     radix_sort_pairs(I.work_keys, I.work, nbrick_, 32, I.sort_tmp, st);
     CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
+    if (timed) CMG_CUDA(cudaEventRecord(ev_[2], st));
     launch_sdf_eval(opts_.precision, opts_.brick, dsegs_, nseg, I.work, nbrick_, queue_, I.soup,
                     I.tinfo, I.cand_off, I.cand, I.brick_emax, opts_.band, occ, sdf32_, sdf64_,
                     near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
+    if (timed) CMG_CUDA(cudaEventRecord(ev_[3], st));
+}
+
+Timing Batch::timing() {
+    Timing t;
+    if (!ev_[0]) return t;
+    CMG_CUDA(cudaEventSynchronize(ev_[3]));
+    CMG_CUDA(cudaEventElapsedTime(&t.occupancy_ms, ev_[0], ev_[1]));
+    CMG_CUDA(cudaEventElapsedTime(&t.sdf_prep_ms, ev_[1], ev_[2]));
+    CMG_CUDA(cudaEventElapsedTime(&t.eval_ms, ev_[2], ev_[3]));
+    CMG_CUDA(cudaEventElapsedTime(&t.total_ms, ev_[0], ev_[3]));
+    return t;
+}
+
+WorkModel Batch::work_model() {
+    WorkModel w;
+    Impl& I = *impl_;
+    RunInfo ri = info();
+    w.orient_calls = static_cast<double>(ri.stats.orient_calls);
+    w.crossings = static_cast<double>(ri.stats.crossings);
+    if (!(sdf32_ || sdf64_) || !I.cand) return w;
+    unsigned long long* d = nullptr;
+    CMG_CUDA(cudaMalloc(&d, 3 * sizeof(unsigned long long)));
+    CMG_CUDA(cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), stream_));
+    launch_count_K(opts_.brick, dsegs_, static_cast<int>(segs_.size()), nbrick_, I.tinfo, I.cand_off,
+                   I.cand, sdf64_, sdf32_, opts_.band, d, stream_);
+    unsigned long long h[3];
+    CMG_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, stream_));
+    CMG_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(d);
+    w.sum_k = static_cast<double>(h[0]);
+    w.sum_k_band = static_cast<double>(h[1]);
+    w.band_cells = static_cast<double>(h[2]);
+    return w;
 }
 
 int64_t Batch::d2h_bytes() const {

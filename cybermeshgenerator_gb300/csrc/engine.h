@@ -52,6 +52,23 @@ struct HostResult {
     std::vector<float> err;
 };
 
+// Phase times of the last run(), from CUDA events on the batch's stream.
+struct Timing {
+    float occupancy_ms = 0.f;  // triangle prep .. exact pass
+    float sdf_prep_ms = 0.f;   // bins, candidate lists, work order
+    float eval_ms = 0.f;       // the distance evaluation kernel
+    float total_ms = 0.f;
+};
+
+// Cost model counts of a finished run (see k_count_K).
+struct WorkModel {
+    double sum_k = 0;       // sum over cells of K(v)
+    double sum_k_band = 0;  // over the FP64 band cells
+    double band_cells = 0;
+    double orient_calls = 0;
+    double crossings = 0;
+};
+
 struct RunInfo {
     Stats stats{};
     int brick = 0;
@@ -86,6 +103,11 @@ public:
     void synchronize();
     void download(std::vector<HostResult>& out, RunInfo* info);
     RunInfo info();
+    // Records CUDA events around the phases of each run() (not in graph replays).
+    void set_timing(bool on) { timing_ = on; }
+    Timing timing();
+    // Runs the K(v) counting pass over the last run's outputs (needs an SDF output).
+    WorkModel work_model();
 
     int nmeshes() const { return static_cast<int>(segs_.size()); }
     const std::vector<MeshSeg>& segs() const { return segs_; }
@@ -128,6 +150,8 @@ private:
     unsigned long long* queue_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
     int64_t h2d_bytes_ = 0;
+    bool timing_ = false;
+    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     void run_impl(bool sizing);
 };
 

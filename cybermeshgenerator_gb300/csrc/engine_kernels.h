@@ -38,6 +38,10 @@ void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks
                        const int64_t* bin_off, const int* bin_list, const int* large_list,
                        float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
                        float* brick_emax, Stats* stats, cudaStream_t st);
+void launch_count_K(int brick, const MeshSeg* segs, int nseg, int64_t nbricks, const float4* tinfo,
+                    const int64_t* cand_off, const int* cand, const double* sdf64,
+                    const float* sdf32, float band_cells, unsigned long long* out,
+                    cudaStream_t st);
 void launch_work_keys(const int* cand_cnt, int64_t n, uint32_t* keys, uint32_t* vals,
                       cudaStream_t st);
 void launch_sdf_eval(int precision, int brick, const MeshSeg* segs, int nseg, const uint32_t* work,
@@ -46,5 +50,8 @@ void launch_sdf_eval(int precision, int brick, const MeshSeg* segs, int nseg, co
                      const float* brick_emax, float band_cells, const uint8_t* occ, float* sdf32,
                      double* sdf64, int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats,
                      int grid, cudaStream_t st);
+
+// peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
+double peak_flops(bool fp64);
 
 }  // namespace cmg::gpu

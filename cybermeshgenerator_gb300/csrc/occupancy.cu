@@ -81,12 +81,15 @@ __device__ __forceinline__ int o3d_sign(const d3& a, const d3& b, const d3& c, c
 // undecided (filter).
 template <bool FULL, int MODE>
 __device__ __forceinline__ int column_tri(const d3& P, const d3& Q, const d3& a, const d3& b,
-                                          const d3& c, double* h, unsigned* exact_calls) {
+                                          const d3& c, double* h, unsigned* exact_calls,
+                                          unsigned* orients = nullptr) {
     int sa = o3d_sign<FULL, MODE>(P, a, b, c, exact_calls);
     if (sa == 2 || sa == 0) return 2;
     int sb = o3d_sign<FULL, MODE>(Q, a, b, c, exact_calls);
     if (sb == 2 || sb == 0) return 2;
+    if (orients) *orients += 2;
     if (sa == sb) return 0;
+    if (orients) *orients += 3;
     int s1 = o3d_sign<FULL, MODE>(P, Q, a, b, exact_calls);
     if (s1 == 2 || s1 == 0) return 2;
     int s2 = o3d_sign<FULL, MODE>(P, Q, b, c, exact_calls);
@@ -193,7 +196,7 @@ k_occ_filter(const MeshSeg* __restrict__ segs, int nseg, const double* __restric
     const double zmin = dsub(g.corner[2], g.h);
     const double zmax = dadd(g.corner[2], dmul(static_cast<double>(g.nz + 1), g.h));
     const double cy = cell_center(g.corner[1], j, g.h);
-    unsigned dummy = 0;
+    unsigned dummy = 0, orients = 0, crossings = 0;
     for (int c = warp; c < kRowCols; c += kOccThreads / 32) {
         const int i = i0 + c;
         if (i >= g.nx) break;
@@ -205,10 +208,11 @@ k_occ_filter(const MeshSeg* __restrict__ segs, int nseg, const double* __restric
             d3 a, b, cc;
             load_tri(soup, col_list[e], a, b, cc);
             double hgt;
-            int r = column_tri<false, MODE>(P, Q, a, b, cc, &hgt, &dummy);
+            int r = column_tri<false, MODE>(P, Q, a, b, cc, &hgt, &dummy, &orients);
             if (r == 2) {
                 undecided = 1;
             } else if (r == 1) {
+                ++crossings;
                 int slot = atomicAdd(&hcnt[c], 1);
                 if (slot < kHCap) hts[c][slot] = hgt;
                 else undecided = 1;
@@ -235,6 +239,12 @@ k_occ_filter(const MeshSeg* __restrict__ segs, int nseg, const double* __restric
             for (int q = 0; q < m; ++q) par ^= (nbelow[c][q] > k);
             base[k * kstride] = static_cast<uint8_t>(par);
         }
+    }
+    {
+        long long o = warp_sum(static_cast<long long>(orients));
+        long long x = warp_sum(static_cast<long long>(crossings));
+        if (lane == 0 && o) atomicAdd(&st->orient_calls, static_cast<unsigned long long>(o));
+        if (lane == 0 && x) atomicAdd(&st->crossings, static_cast<unsigned long long>(x));
     }
     if (warp == 0) {
         const int i = i0 + lane;

@@ -105,6 +105,8 @@ void exclusive_scan_impl(const T* in, int64_t* out, int64_t n, int64_t* tmp, cud
     k_tile_sums<T><<<static_cast<unsigned>(tiles), kScanThreads, 0, st>>>(in, n, tmp);
     k_scan_sums<<<1, kScanThreads, 0, st>>>(tmp, tiles);
     k_tile_scan<T><<<static_cast<unsigned>(tiles), kScanThreads, 0, st>>>(in, n, tmp, out);
+    note_launch(2);
+    CMG_LAUNCH();
 }
 
 // ------------------------------------------------------------------ radix sort
@@ -212,8 +214,10 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, int64_t n, int key_bits, v
         int shift = 8 * pss;
         k_digit_hist<<<static_cast<unsigned>(ntiles), kSortThreads, 0, st>>>(ka, n, shift, ntiles, hist);
         exclusive_scan(hist, start, hn, stmp, st);
+        note_launch();
         k_digit_scatter<<<static_cast<unsigned>(ntiles), kSortThreads, 0, st>>>(
             ka, va, n, shift, ntiles, start, kb, vb);
+        CMG_LAUNCH();
         uint32_t* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }

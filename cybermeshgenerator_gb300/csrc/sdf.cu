@@ -820,6 +820,57 @@ k_sdf_mixed(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restri
     }
 }
 
+// Work model: per cell, K(v) = #{t : |p - c_t| - e_t <= |sdf(v)|}, the triangles
+// whose bounding sphere reaches the distance sphere of the cell -- the minimal
+// candidate set of any bounding-sphere-pruned exact search. out[0] = sum K over
+// all cells, out[1] = sum K over cells with |sdf| <= band, out[2] = those cells.
+template <int B, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_count_K(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
+          const float4* __restrict__ tinfo, const int64_t* __restrict__ cand_off,
+          const int* __restrict__ cand, const double* __restrict__ sdf64,
+          const float* __restrict__ sdf32, float band_cells, unsigned long long* __restrict__ out) {
+    using M = CellMap<B, THREADS>;
+    constexpr int VPT = M::VPT;
+    const int64_t gb = blockIdx.x;
+    if (gb >= nbricks) return;
+    const int si = find_seg<&MeshSeg::brick_begin>(segs, nseg, gb);
+    const MeshSeg& s = segs[si];
+    const BrickGeo q = brick_geo(s, gb - s.brick_begin);
+    const GridDesc g = s.g;
+    const float h = static_cast<float>(g.h);
+    unsigned long long k_all = 0, k_band = 0, n_band = 0;
+    for (int v = 0; v < VPT; ++v) {
+        int x, y, z;
+        M::cell(threadIdx.x, v, x, y, z);
+        x += q.x0; y += q.y0; z += q.z0;
+        if (!(x < q.x1 && y < q.y1 && z < q.z1)) continue;
+        int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+        float d = sdf64 ? static_cast<float>(fabs(sdf64[idx])) : fabsf(sdf32[idx]);
+        float px = (x + 0.5f) * h, py = (y + 0.5f) * h, pz = (z + 0.5f) * h;
+        unsigned kk = 0;
+        for (int64_t e = cand_off[gb]; e < cand_off[gb + 1]; ++e) {
+            float4 ti = tinfo[cand[e]];
+            float dx = px - ti.x, dy = py - ti.y, dz = pz - ti.z;
+            kk += sqrtf(dx * dx + dy * dy + dz * dz) - ti.w <= d;
+        }
+        kk = max(kk, 1u);
+        k_all += kk;
+        if (d <= band_cells * h) {
+            k_band += kk;
+            ++n_band;
+        }
+    }
+    long long a = warp_sum(static_cast<long long>(k_all));
+    long long b = warp_sum(static_cast<long long>(k_band));
+    long long c = warp_sum(static_cast<long long>(n_band));
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicAdd(&out[0], static_cast<unsigned long long>(a));
+        if (b) atomicAdd(&out[1], static_cast<unsigned long long>(b));
+        if (c) atomicAdd(&out[2], static_cast<unsigned long long>(c));
+    }
+}
+
 // LPT order of the bricks: key = ~count so an ascending sort puts the most
 // expensive bricks first.
 __global__ void k_work_keys(const int* __restrict__ cand_cnt, int64_t n, uint32_t* __restrict__ keys,
@@ -872,6 +923,20 @@ void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks
         k_brick_walk<false><<<grid, 128, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi,
                                                   bin_off, bin_list, large_list, bound, cand_cnt,
                                                   cand_off, cand, brick_emax, stats);
+    CMG_LAUNCH();
+}
+
+void launch_count_K(int brick, const MeshSeg* segs, int nseg, int64_t nbricks, const float4* tinfo,
+                    const int64_t* cand_off, const int* cand, const double* sdf64,
+                    const float* sdf32, float band_cells, unsigned long long* out,
+                    cudaStream_t st) {
+    if (nbricks == 0) return;
+    if (brick == 4)
+        k_count_K<4, 64><<<static_cast<unsigned>(nbricks), 64, 0, st>>>(
+            segs, nseg, nbricks, tinfo, cand_off, cand, sdf64, sdf32, band_cells, out);
+    else
+        k_count_K<8, 128><<<static_cast<unsigned>(nbricks), 128, 0, st>>>(
+            segs, nseg, nbricks, tinfo, cand_off, cand, sdf64, sdf32, band_cells, out);
     CMG_LAUNCH();
 }
 

@@ -102,6 +102,39 @@ int cmg_batch_size(const cmg_batch*);
 int64_t cmg_batch_cells(const cmg_batch*);
 void cmg_batch_destroy(cmg_batch*);
 
+/* ---- measurement ---------------------------------------------------------- */
+/* Phase times of a batch's last run (CUDA events on its stream), once enabled. */
+typedef struct cmg_batch_timing {
+    float occupancy_ms; /* triangle prep .. exact pass */
+    float sdf_prep_ms;  /* triangle bins, brick candidate lists, work order */
+    float eval_ms;      /* distance evaluation kernel */
+    float total_ms;
+} cmg_batch_timing;
+
+/* Cost-model counts of a batch's last run: sum over cells of K(v), the number of
+ * triangles whose bounding sphere reaches the cell's distance sphere (the minimal
+ * candidate set of a bounding-sphere-pruned exact search), the same over the
+ * FP64 band, and the occupancy filter's orient3d and plane_z evaluations. */
+typedef struct cmg_work_model {
+    double sum_k;
+    double sum_k_band;
+    double band_cells;
+    double orient_calls;
+    double crossings;
+} cmg_work_model;
+
+/* The cudaStream_t the batch runs on (for events recorded by the caller). */
+void* cmg_batch_stream(const cmg_batch*);
+cmg_status cmg_batch_set_timing(cmg_batch*, int on);
+cmg_status cmg_batch_get_timing(cmg_batch*, cmg_batch_timing* out, char* errbuf, size_t errbuf_len);
+cmg_status cmg_batch_work_model(cmg_batch*, cmg_work_model* out, char* errbuf, size_t errbuf_len);
+cmg_status cmg_batch_stats(cmg_batch*, cmg_voxel_stats* out, char* errbuf, size_t errbuf_len);
+/* Kernels this library has launched in this process. */
+long long cmg_gpu_launches(void);
+/* Measured FMA throughput of the current GPU in FLOP/s (FMA = 2 FLOPs):
+ * fp64 != 0 for DFMA, else FFMA. */
+cmg_status cmg_gpu_peak_flops(int fp64, double* flops, char* errbuf, size_t errbuf_len);
+
 /* Library build identification, e.g. "cmg-gb300 sm_103a". */
 const char* cmg_gpu_version(void);
 
