@@ -140,6 +140,8 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_batch_stats", I, [V, ctypes.POINTER(VoxelStats), S, Z])
     sig("cmg_gpu_launches", ctypes.c_longlong, [])
     sig("cmg_gpu_peak_flops", I, [I, c_double_p, S, Z])
+    sig("cmg_gpu_occupancy_static", I, [V, ctypes.c_int64, V, ctypes.c_int64, c_double_p, D,
+                                        c_int_p, I, V, V, S, Z])
 
 
 _LIB = None

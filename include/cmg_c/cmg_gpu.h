@@ -135,6 +135,27 @@ long long cmg_gpu_launches(void);
  * fp64 != 0 for DFMA, else FFMA. */
 cmg_status cmg_gpu_peak_flops(int fp64, double* flops, char* errbuf, size_t errbuf_len);
 
+/* ---- occupancy without allocation ----------------------------------------- */
+/* No counterpart in the reference. For callers that cannot call cudaMalloc (a host
+ * framework that owns device memory through its own pool, a loop that may not
+ * allocate after start-up): occupancy of one mesh on an explicit grid, with the
+ * inputs and the output in device buffers the caller owns (d_points: 3*npoints
+ * doubles, d_triangles: 3*ntriangles ints, d_occupancy: dims[0]*dims[1]*dims[2]
+ * bytes, idx = (k*ny + j)*nx + i) and all working memory taken from a fixed 32 MiB
+ * array in device memory that the library holds on every GPU it is loaded on.
+ * Allocates nothing. Inputs that need more working memory than the array holds
+ * are rejected with CMG_ERR_INVALID_INPUT and a message. The first call on a device
+ * resolves the array's address (make it before any stream capture); calls share
+ * the array, so calls that overlap on the GPU race and must be serialised.
+ * `stream` is a cudaStream_t (NULL for the default stream); the call returns
+ * after the work on it has finished. predicates: CMG_PRED_COMPAT or
+ * CMG_PRED_EXACT. The result equals cmg_plc_voxelize_ex's occupancy. */
+cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t npoints,
+                                    const int* d_triangles, int64_t ntriangles,
+                                    const double* corner, double spacing, const int* dims,
+                                    int predicates, unsigned char* d_occupancy, void* stream,
+                                    char* errbuf, size_t errbuf_len);
+
 /* Library build identification, e.g. "cmg-gb300 sm_103a". */
 const char* cmg_gpu_version(void);
 
