@@ -295,7 +295,8 @@ def run_ours(args):
                                  "band_cells": int(st["band_cells"]),
                                  "evaluations": int(st["evaluations"]),
                                  "fp64_evaluations": int(st["fp64_evaluations"]),
-                                 "candidates": int(st["candidates"])}
+                                 "candidates": int(st["candidates"]),
+                                 "subbrick_entries": int(st["filtered"])}
         # end to end through the C ABI with host buffers (upload, pipeline, download)
         e2e_t = []
         for i in range(args.warmup + args.steps):

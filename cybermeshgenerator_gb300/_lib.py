@@ -29,7 +29,7 @@ class VoxelOpts(ctypes.Structure):
                 ("predicates", ctypes.c_int), ("explicit_grid", ctypes.c_int),
                 ("corner", ctypes.c_double * 3), ("spacing", ctypes.c_double),
                 ("dims", ctypes.c_int * 3), ("band", ctypes.c_double), ("brick", ctypes.c_int),
-                ("autotune", ctypes.c_int)]
+                ("autotune", ctypes.c_int), ("grab", ctypes.c_int), ("stage", ctypes.c_int)]
 
 
 class VoxelStats(ctypes.Structure):
@@ -39,7 +39,8 @@ class VoxelStats(ctypes.Structure):
                 ("exact_calls", ctypes.c_int64), ("bucket_entries", ctypes.c_int64),
                 ("candidates", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("fp64_evaluations", ctypes.c_int64), ("band_cells", ctypes.c_int64),
-                ("brick", ctypes.c_int), ("max_error_bound", ctypes.c_double)]
+                ("filtered", ctypes.c_int64), ("brick", ctypes.c_int),
+                ("max_error_bound", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -177,6 +177,8 @@ cmg::gpu::VoxOpts to_vox(const cmg_voxel_opts& o, int outputs) {
     v.want_near = outputs & CMG_OUT_NEAREST;
     v.want_err = outputs & CMG_OUT_ERROR_BOUND;
     v.autotune = o.autotune != 0;
+    v.grab = o.grab;
+    v.stage = o.stage;
     return v;
 }
 
@@ -197,6 +199,7 @@ void fill_stats(cmg_voxels* v, const cmg::gpu::RunInfo& ri) {
     s.evaluations = static_cast<int64_t>(ri.stats.evaluations);
     s.fp64_evaluations = static_cast<int64_t>(ri.stats.fp64_evaluations);
     s.band_cells = static_cast<int64_t>(ri.stats.band_voxels);
+    s.filtered = static_cast<int64_t>(ri.stats.filtered);
     s.brick = ri.brick;
     double m = 0;
     for (float e : v->r.err) m = std::max(m, static_cast<double>(e));
@@ -347,6 +350,7 @@ void cmg_voxel_opts_init(cmg_voxel_opts* o) {
     o->precision = CMG_PREC_FP64;
     o->predicates = CMG_PRED_COMPAT;
     o->band = 1.0;
+    o->stage = -1;
 }
 
 cmg_status cmg_plc_voxelize(const cmg_plc* in, int resolution, int mode, int pad,
@@ -373,8 +377,8 @@ cmg_status cmg_plc_voxelize_ex(const cmg_plc* in, const cmg_voxel_opts* opts, cm
         set_err(errbuf, len, "resolution must be >= 1");
         return CMG_ERR_INVALID_INPUT;
     }
-    if (opts->brick != 0 && opts->brick != 4 && opts->brick != 8) {
-        set_err(errbuf, len, "brick must be 0, 4 or 8");
+    if (opts->brick != 0 && opts->brick != 4 && opts->brick != 8 && opts->brick != 16) {
+        set_err(errbuf, len, "brick must be 0, 4, 8 or 16");
         return CMG_ERR_UNSUPPORTED_OPTION;
     }
     return guarded(errbuf, len, [&] { *out = voxelize_one(*in, *opts); });

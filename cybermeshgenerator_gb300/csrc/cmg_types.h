@@ -45,6 +45,7 @@ struct Stats {
     unsigned long long error_flags;        // nonzero: a kernel hit a capacity limit
     unsigned long long orient_calls;       // occupancy filter: orient3d evaluations
     unsigned long long crossings;          // occupancy filter: plane_z evaluations
+    unsigned long long filtered;           // SDF: sub-brick list entries (sphere tests per cell)
 };
 
 enum : int { kPredCompat = 0, kPredExact = 1 };

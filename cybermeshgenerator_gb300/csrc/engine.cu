@@ -37,7 +37,9 @@ T* carve(Arena& a, size_t n) {
     return p;
 }
 
-int pick_brick(const VoxOpts& o) { return o.brick == 4 ? 4 : 8; }
+// 16: candidate lists per 16^3 brick, evaluation per 4^3 sub-brick (default);
+// 4 or 8: one list and one evaluation CTA per brick of that edge.
+int pick_brick(const VoxOpts& o) { return (o.brick == 4 || o.brick == 8) ? o.brick : 16; }
 
 }  // namespace
 
@@ -82,6 +84,8 @@ struct Batch::Impl {
     uint8_t* hv = nullptr;
     // sdf
     float4* tinfo = nullptr;
+    float4* tinfo_lo = nullptr;
+    void* trec = nullptr;
     float4* tlo = nullptr;
     float4* thi = nullptr;
     int64_t* tbin = nullptr;
@@ -143,7 +147,8 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
     }
     ntris_ = tb;
     npts_ = pb;
-    if (nbrick_ >= (int64_t(1) << 32)) throw std::invalid_argument("voxelize: grid too large");
+    nwork_ = brick == 16 ? 64 * nbrick_ : nbrick_;
+    if (nwork_ >= (int64_t(1) << 32)) throw std::invalid_argument("voxelize: grid too large");
     const int nseg = static_cast<int>(segs_.size());
     const bool sdf = opts_.want_sdf32 || opts_.want_sdf64 || opts_.want_near;
 
@@ -168,6 +173,8 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
         if (!opts_.want_occ) impl_->occ_internal = carve<uint8_t>(A, nvox_);
         if (sdf) {
             impl_->tinfo = carve<float4>(A, ntris_);
+            impl_->tinfo_lo = carve<float4>(A, ntris_);
+            impl_->trec = carve<char>(A, 144 * static_cast<size_t>(ntris_));
             impl_->tlo = carve<float4>(A, ntris_);
             impl_->thi = carve<float4>(A, ntris_);
             impl_->tbin = carve<int64_t>(A, ntris_);
@@ -182,9 +189,9 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
             impl_->cand_cnt = carve<int>(A, nbrick_);
             impl_->cand_off = carve<int64_t>(A, nbrick_ + 1);
             impl_->brick_emax = carve<float>(A, nbrick_);
-            impl_->work_keys = carve<uint32_t>(A, nbrick_);
-            impl_->work = carve<uint32_t>(A, nbrick_);
-            impl_->sort_tmp = carve<char>(A, radix_sort_tmp_bytes(nbrick_));
+            impl_->work_keys = carve<uint32_t>(A, nwork_);
+            impl_->work = carve<uint32_t>(A, nwork_);
+            impl_->sort_tmp = carve<char>(A, radix_sort_tmp_bytes(nwork_));
         }
         if (commit) return;
     };
@@ -232,12 +239,11 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
 
     const int sms = device_sms();
     impl_->grid_exact = 2 * sms;
-    int per_sm = 1;
-    if (sdf) {
-        // persistent evaluation grid: resident CTAs per SM for the chosen kernel
-        per_sm = brick == 4 ? 8 : 3;
-    }
-    impl_->grid_eval = per_sm * sms;
+    // persistent evaluation grid: resident CTAs per SM for the chosen kernel
+    if (opts_.grab <= 0) opts_.grab = 1;
+    if (opts_.stage < 0) opts_.stage = 0;
+    if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(opts_.precision, opts_.stage != 0) : sms;
+    else impl_->grid_eval = (brick == 4 ? 8 : 3) * sms;
 }
 
 Batch::~Batch() {
@@ -339,8 +345,8 @@ void Batch::run_impl(bool sizing) {
     CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
     CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
     CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * nseg, st));
-    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tlo, I.thi, I.tbin, I.bincnt,
-                        I.large_cnt, I.emax_bits, st);
+    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tlo, I.thi,
+                        I.tbin, I.bincnt, I.large_cnt, I.emax_bits, st);
     exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);
     exclusive_scan(I.large_cnt, I.large_off, nseg, I.scan_tmp, st);
     launch_seg_finish(dsegs_, nseg, I.large_off, I.emax_bits, st);
@@ -372,13 +378,20 @@ void Batch::run_impl(bool sizing) {
     launch_brick_walk(true, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
                       I.bin_list, I.large_list, I.bound, I.cand_cnt, I.cand_off, I.cand,
                       I.brick_emax, stats_, st);
-    launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
-    radix_sort_pairs(I.work_keys, I.work, nbrick_, 32, I.sort_tmp, st);
+    if (opts_.brick == 16) launch_sub_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
+    else launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
+    radix_sort_pairs(I.work_keys, I.work, nwork_, 32, I.sort_tmp, st);
     CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
     if (timed) CMG_CUDA(cudaEventRecord(ev_[2], st));
-    launch_sdf_eval(opts_.precision, opts_.brick, dsegs_, nseg, I.work, nbrick_, queue_, I.soup,
-                    I.tinfo, I.cand_off, I.cand, I.brick_emax, opts_.band, occ, sdf32_, sdf64_,
-                    near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
+    if (opts_.brick == 16)
+        launch_sdf_sub(opts_.precision, opts_.stage != 0, opts_.grab, dsegs_, nseg, I.work, nwork_,
+                       queue_, I.soup, I.tinfo,
+                       I.tinfo_lo, I.trec, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
+                       sdf32_, sdf64_, near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
+    else
+        launch_sdf_eval(opts_.precision, opts_.brick, dsegs_, nseg, I.work, nbrick_, queue_,
+                        I.soup, I.tinfo, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
+                        sdf32_, sdf64_, near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
     if (timed) CMG_CUDA(cudaEventRecord(ev_[3], st));
 }
 
@@ -476,11 +489,11 @@ int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cud
         if (it != cache.end()) return it->second;
     }
     float best_ms = 0.f;
-    int best = 8;
+    int best = 16;
     cudaEvent_t e0, e1;
     CMG_CUDA(cudaEventCreate(&e0));
     CMG_CUDA(cudaEventCreate(&e1));
-    for (int b : {4, 8}) {
+    for (int b : {16, 8}) {
         VoxOpts o = opts;
         o.brick = b;
         o.autotune = false;
@@ -493,7 +506,7 @@ int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cud
         CMG_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
         CMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (b == 4 || ms < best_ms) {
+        if (b == 16 || ms < best_ms) {
             best_ms = ms;
             best = b;
         }

@@ -25,7 +25,8 @@ namespace cmg::gpu {
 struct VoxOpts {
     int predicates = kPredCompat;  // kPredCompat (reference semantics) | kPredExact
     int precision = kPrecFP64;     // kPrecFP64 (plain, bit-exact) | kPrecMixed
-    int brick = 0;                 // 4 or 8 cells per brick edge; 0 = tuned/default
+    int brick = 0;                 // candidate brick edge: 16 (default; 4^3 sub-brick
+                                   // evaluation), 8 or 4 (one CTA per brick)
     float band = 1.0f;             // mixed: FP64 refinement band, in cells
     bool want_occ = true;
     bool want_sdf32 = false;
@@ -33,6 +34,9 @@ struct VoxOpts {
     bool want_near = false;        // nearest triangle id + Ericson region per cell
     bool want_err = false;         // mixed: stated per-cell FP32 error bound
     bool autotune = false;
+    int grab = 0;                  // sub-bricks per queue grab (1, 2, 4, 8); 0 = default
+    int stage = -1;                // mixed: stage candidate records in shared memory
+                                   // (1) or read them from L1/L2 (0); -1 = default
 };
 
 struct HostMesh {
@@ -135,7 +139,7 @@ private:
     VoxOpts opts_;
     cudaStream_t stream_;
     std::vector<MeshSeg> segs_;
-    int64_t npts_ = 0, ntris_ = 0, ncol_ = 0, nrow_ = 0, nvox_ = 0, nbrick_ = 0;
+    int64_t npts_ = 0, ntris_ = 0, ncol_ = 0, nrow_ = 0, nvox_ = 0, nbrick_ = 0, nwork_ = 0;
     int64_t pairs_cap_ = -1, cand_cap_ = -1;
     double* pts_ = nullptr;
     int* tris_ = nullptr;
@@ -155,8 +159,8 @@ private:
     void run_impl(bool sizing);
 };
 
-// Chooses the brick edge for a workload by timing both on the device (cached per
-// process by workload shape). Returns 4 or 8.
+// Chooses the brick edge for a workload by timing 16 and 8 on the device (cached
+// per process by workload shape).
 int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream);
 
 // Number of SMs of the current device.

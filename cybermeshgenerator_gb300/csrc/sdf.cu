@@ -30,6 +30,7 @@
 #include <climits>
 
 #include "cmg_device.cuh"
+#include "cmg_sdf.cuh"
 #include "cmg_seg.cuh"
 #include "cmg_types.h"
 #include "cmg_util.h"
@@ -39,68 +40,7 @@ namespace cmg::gpu {
 
 namespace {
 
-constexpr float kU32 = 5.9604645e-8f;  // 2^-24
-
-// ------------------------------------------------------------------ FP64 Ericson
-// Squared distance and region, reference operation order (voxelize.cpp:202-247).
-__device__ __forceinline__ double dot3r(double ax, double ay, double az, double bx, double by,
-                                        double bz) {
-    return dadd(dadd(dmul(ax, bx), dmul(ay, by)), dmul(az, bz));
-}
-__device__ __forceinline__ double d2r(const d3& p, double qx, double qy, double qz) {
-    double dx = dsub(p.x, qx), dy = dsub(p.y, qy), dz = dsub(p.z, qz);
-    return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-}
-
-__device__ __noinline__ double ericson(const d3& p, const d3& a, const d3& b, const d3& c,
-                                       int* region) {
-    double abx = dsub(b.x, a.x), aby = dsub(b.y, a.y), abz = dsub(b.z, a.z);
-    double acx = dsub(c.x, a.x), acy = dsub(c.y, a.y), acz = dsub(c.z, a.z);
-    double apx = dsub(p.x, a.x), apy = dsub(p.y, a.y), apz = dsub(p.z, a.z);
-    double d1 = dot3r(abx, aby, abz, apx, apy, apz), d2 = dot3r(acx, acy, acz, apx, apy, apz);
-    if (d1 <= 0 && d2 <= 0) { *region = 0; return d2r(p, a.x, a.y, a.z); }
-    double bpx = dsub(p.x, b.x), bpy = dsub(p.y, b.y), bpz = dsub(p.z, b.z);
-    double d3v = dot3r(abx, aby, abz, bpx, bpy, bpz), d4 = dot3r(acx, acy, acz, bpx, bpy, bpz);
-    if (d3v >= 0 && d4 <= d3v) { *region = 1; return d2r(p, b.x, b.y, b.z); }
-    double vc = dsub(dmul(d1, d4), dmul(d3v, d2));
-    if (vc <= 0 && d1 >= 0 && d3v <= 0) {
-        double v = ddiv(d1, dsub(d1, d3v));
-        *region = 2;
-        return d2r(p, dadd(a.x, dmul(v, abx)), dadd(a.y, dmul(v, aby)), dadd(a.z, dmul(v, abz)));
-    }
-    double cpx = dsub(p.x, c.x), cpy = dsub(p.y, c.y), cpz = dsub(p.z, c.z);
-    double d5 = dot3r(abx, aby, abz, cpx, cpy, cpz), d6 = dot3r(acx, acy, acz, cpx, cpy, cpz);
-    if (d6 >= 0 && d5 <= d6) { *region = 3; return d2r(p, c.x, c.y, c.z); }
-    double vb = dsub(dmul(d5, d2), dmul(d1, d6));
-    if (vb <= 0 && d2 >= 0 && d6 <= 0) {
-        double w = ddiv(d2, dsub(d2, d6));
-        *region = 4;
-        return d2r(p, dadd(a.x, dmul(w, acx)), dadd(a.y, dmul(w, acy)), dadd(a.z, dmul(w, acz)));
-    }
-    double va = dsub(dmul(d3v, d6), dmul(d5, d4));
-    double d43 = dsub(d4, d3v), d56 = dsub(d5, d6);
-    if (va <= 0 && d43 >= 0 && d56 >= 0) {
-        double w = ddiv(d43, dadd(d43, d56));
-        *region = 5;
-        return d2r(p, dadd(b.x, dmul(w, dsub(c.x, b.x))), dadd(b.y, dmul(w, dsub(c.y, b.y))),
-                   dadd(b.z, dmul(w, dsub(c.z, b.z))));
-    }
-    double denom = ddiv(1.0, dadd(dadd(va, vb), vc));
-    double v = dmul(vb, denom), w = dmul(vc, denom);
-    *region = 6;
-    return d2r(p, dadd(dadd(a.x, dmul(abx, v)), dmul(acx, w)),
-               dadd(dadd(a.y, dmul(aby, v)), dmul(acy, w)),
-               dadd(dadd(a.z, dmul(abz, v)), dmul(acz, w)));
-}
-
-__device__ __forceinline__ void load_soup(const double* __restrict__ soup, int64_t t, d3& a, d3& b,
-                                          d3& c) {
-    const double2* r = reinterpret_cast<const double2*>(soup + t * kSoupStride);
-    double2 v0 = __ldg(r), v1 = __ldg(r + 1), v2 = __ldg(r + 2), v3 = __ldg(r + 3), v4 = __ldg(r + 4);
-    a = {v0.x, v0.y, v1.x};
-    b = {v1.y, v2.x, v2.y};
-    c = {v3.x, v3.y, v4.x};
-}
+using namespace sdf;
 
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
 
@@ -109,6 +49,7 @@ __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru
 // nearest) and the radius e_t rounded up (plus the rounding of the centroid).
 __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64_t ntris,
                                const double* __restrict__ soup, float4* __restrict__ tinfo,
+                               float4* __restrict__ tinfo_lo, TriRec* __restrict__ trec,
                                float4* __restrict__ tlo, float4* __restrict__ thi,
                                int64_t* __restrict__ tbin, int* __restrict__ bincnt,
                                int* __restrict__ large_cnt, unsigned* __restrict__ emax_bits) {
@@ -131,10 +72,12 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         lo[1] = fmin(lo[1], V[k].y); hi[1] = fmax(hi[1], V[k].y);
         lo[2] = fmin(lo[2], V[k].z); hi[2] = fmax(hi[2], V[k].z);
     }
-    float4 ci;
-    ci.x = static_cast<float>(cx - K[0]);
-    ci.y = static_cast<float>(cy - K[1]);
-    ci.z = static_cast<float>(cz - K[2]);
+    float4 ci, cl;
+    split2(cx - K[0], ci.x, cl.x);
+    split2(cy - K[1], ci.y, cl.y);
+    split2(cz - K[2], ci.z, cl.z);
+    cl.w = 0.f;
+    tinfo_lo[t] = cl;
     // radius: sqrt rounded up, padded for the FP32 centroid (|err| <= u*|c - K|*sqrt3)
     double pad = 2.0 * kU32 * (fabs(cx - K[0]) + fabs(cy - K[1]) + fabs(cz - K[2])) + 1e-300;
     ci.w = round_up_f(sqrt(r2) * (1.0 + 1e-12) + pad);
@@ -143,11 +86,42 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
                          __double2float_rd(lo[2] - K[2]), 0.f);
     thi[t] = make_float4(__double2float_ru(hi[0] - K[0]), __double2float_ru(hi[1] - K[1]),
                          __double2float_ru(hi[2] - K[2]), 0.f);
-    // degenerate (zero-area) or larger than two bricks: always considered
+    // translation-invariant FP32 record (from FP64)
     double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
     double vx = c.x - a.x, vy = c.y - a.y, vz = c.z - a.z;
     double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
     bool degenerate = !(nx * nx + ny * ny + nz * nz > 0.0);
+    {
+        TriRec r;
+        const double E[3][3] = {{b.x - a.x, b.y - a.y, b.z - a.z},
+                                {c.x - b.x, c.y - b.y, c.z - b.z},
+                                {a.x - c.x, a.y - c.y, a.z - c.z}};
+        double nl = sqrt(nx * nx + ny * ny + nz * nz);
+        double n3[3] = {0.0, 0.0, 0.0};
+        if (nl > 0.0) { n3[0] = nx / nl; n3[1] = ny / nl; n3[2] = nz / nl; }
+        float* O[3] = {r.o0, r.o1, r.o2};
+        float* Ef[3] = {r.e0, r.e1, r.e2};
+        float* Mf[3] = {r.m0, r.m1, r.m2};
+        const double C[3] = {cx, cy, cz};
+        for (int k = 0; k < 3; ++k) {
+            const double Vk[3] = {V[k].x, V[k].y, V[k].z};
+            for (int q = 0; q < 3; ++q) {
+                O[k][q] = static_cast<float>(Vk[q] - C[q]);
+                Ef[k][q] = static_cast<float>(E[k][q]);
+            }
+            const double* e = E[k];
+            Mf[k][0] = static_cast<float>(n3[1] * e[2] - n3[2] * e[1]);
+            Mf[k][1] = static_cast<float>(n3[2] * e[0] - n3[0] * e[2]);
+            Mf[k][2] = static_cast<float>(n3[0] * e[1] - n3[1] * e[0]);
+            double ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+            r.inv[k] = ee > 0.0 ? static_cast<float>(1.0 / ee) : 0.f;
+        }
+        for (int q = 0; q < 3; ++q) r.nn[q] = static_cast<float>(n3[q]);
+        r.ok = nl > 0.0 ? 1.f : 0.f;
+        r.pad_[0] = r.pad_[1] = 0.f;
+        trec[t] = r;
+    }
+    // degenerate (zero-area) or larger than two bricks: always considered
     const double bw = static_cast<double>(s.brick) * s.g.h;
     bool large = degenerate || sqrt(r2) > 2.0 * bw;
     if (large) {
@@ -251,6 +225,22 @@ __device__ __forceinline__ void shell_offset(int r, int q, int& dx, int& dy, int
 
 __device__ __forceinline__ int shell_count(int r) { return r == 0 ? 1 : 24 * r * r + 2; }
 
+// Bin k of the Chebyshev shell r around the brick (if in the grid): its entry
+// range [b0, b1) in the bin CSR; `inside` is set when the bin lies in the grid.
+__device__ __forceinline__ void shell_bin(const MeshSeg& s, const BrickGeo& q,
+                                          const int64_t* __restrict__ bin_off, int r, int k, int n,
+                                          bool& inside, int64_t& b0, int64_t& b1) {
+    if (k >= n) return;
+    int dx, dy, dz;
+    shell_offset(r, k, dx, dy, dz);
+    const int x = q.bx + dx, y = q.by + dy, z = q.bz + dz;
+    if (x < 0 || y < 0 || z < 0 || x >= s.bnx || y >= s.bny || z >= s.bnz) return;
+    inside = true;
+    const int64_t bin = s.brick_begin + (static_cast<int64_t>(z) * s.bny + y) * s.bnx + x;
+    b0 = bin_off[bin];
+    b1 = bin_off[bin + 1];
+}
+
 // Upper bound on the distance from point c (corner-relative) to a large triangle:
 // the distance to its nearest edge point (segments), plus rounding margin.
 __device__ __forceinline__ float seg_dist(float px, float py, float pz, float ax, float ay, float az,
@@ -320,18 +310,22 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
             if (r > 0 && (r - 1) * bw > U) break;  // farther bins cannot lower U
             const int n = shell_count(r);
             bool inside = false;
-            for (int k = lane; k < n; k += 32) {
-                int dx, dy, dz;
-                shell_offset(r, k, dx, dy, dz);
-                int x = q.bx + dx, y = q.by + dy, z = q.bz + dz;
-                if (x < 0 || y < 0 || z < 0 || x >= s.bnx || y >= s.bny || z >= s.bnz) continue;
-                inside = true;
-                int64_t bin = s.brick_begin + (static_cast<int64_t>(z) * s.bny + y) * s.bnx + x;
-                for (int64_t e = bin_off[bin]; e < bin_off[bin + 1]; ++e) {
-                    float4 ti = tinfo[bin_list[e]];
-                    float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
-                    float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f + 4.f * kU32);
-                    U = fminf(U, d + ti.w + tol);
+            for (int k0 = 0; k0 < n; k0 += 32) {
+                int64_t b0 = 0, b1 = 0;
+                shell_bin(s, q, bin_off, r, k0 + lane, n, inside, b0, b1);
+                // the non-empty bins of this group, one at a time, all lanes over its list
+                unsigned m = __ballot_sync(0xffffffffu, b1 > b0);
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int64_t s0 = __shfl_sync(0xffffffffu, b0, src);
+                    const int64_t s1 = __shfl_sync(0xffffffffu, b1, src);
+                    for (int64_t e = s0 + lane; e < s1; e += 32) {
+                        float4 ti = tinfo[bin_list[e]];
+                        float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
+                        float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f + 4.f * kU32);
+                        U = fminf(U, d + ti.w + tol);
+                    }
                 }
             }
             if (r > 0 && !__any_sync(0xffffffffu, inside)) {
@@ -374,32 +368,29 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         const int n = shell_count(r);
         bool any_inside = false;
         for (int k0 = 0; k0 < n; k0 += 32) {
-            int k = k0 + lane;
-            int64_t bin = -1;
-            if (k < n) {
-                int dx, dy, dz;
-                shell_offset(r, k, dx, dy, dz);
-                int x = q.bx + dx, y = q.by + dy, z = q.bz + dz;
-                if (!(x < 0 || y < 0 || z < 0 || x >= s.bnx || y >= s.bny || z >= s.bnz))
-                    bin = s.brick_begin + (static_cast<int64_t>(z) * s.bny + y) * s.bnx + x;
-            }
-            any_inside |= bin >= 0;
-            int64_t e = bin >= 0 ? bin_off[bin] : 0, eend = bin >= 0 ? bin_off[bin + 1] : 0;
-            // all lanes loop until every lane has drained its bin (ballot-ordered emits)
-            while (__any_sync(0xffffffffu, e < eend)) {
-                bool take = false;
-                int t = 0;
-                float et = 0.f;
-                if (e < eend) {
-                    t = bin_list[e];
-                    float4 ti = tinfo[t];
-                    float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
-                    float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f - 4.f * kU32);
-                    take = d - ti.w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
-                    et = ti.w;
-                    ++e;
+            int64_t b0 = 0, b1 = 0;
+            shell_bin(s, q, bin_off, r, k0 + lane, n, any_inside, b0, b1);
+            unsigned m = __ballot_sync(0xffffffffu, b1 > b0);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const int64_t s0 = __shfl_sync(0xffffffffu, b0, src);
+                const int64_t s1 = __shfl_sync(0xffffffffu, b1, src);
+                for (int64_t e0 = s0; e0 < s1; e0 += 32) {  // uniform trip count: ballots inside
+                    const int64_t e = e0 + lane;
+                    bool take = false;
+                    int t = 0;
+                    float et = 0.f;
+                    if (e < s1) {
+                        t = bin_list[e];
+                        float4 ti = tinfo[t];
+                        float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
+                        float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f - 4.f * kU32);
+                        take = d - ti.w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
+                        et = ti.w;
+                    }
+                    emit(take, t, et);
                 }
-                emit(take, t, et);
             }
         }
         if (r > 0 && !__any_sync(0xffffffffu, any_inside)) break;
@@ -429,24 +420,6 @@ struct CellMap {
         z = zslab * VPT + v;
     }
 };
-
-struct Out {
-    const uint8_t* occ;
-    float* sdf32;
-    double* sdf64;
-    int* near_tri;
-    uint8_t* near_reg;
-    float* errbound;   // mixed: per-cell stated FP32 error bound (nullable)
-};
-
-__device__ __forceinline__ void write_cell(const Out& o, int64_t idx, double d, int tri, int reg) {
-    const bool in = o.occ[idx] != 0;
-    const double sd = in ? -d : d;
-    if (o.sdf64) o.sdf64[idx] = sd;
-    if (o.sdf32) o.sdf32[idx] = __double2float_rn(sd);
-    if (o.near_tri) o.near_tri[idx] = tri;
-    if (o.near_reg) o.near_reg[idx] = static_cast<uint8_t>(reg);
-}
 
 // Plain FP64: CTA per brick (persistent over a work list), THREADS threads.
 template <int B, int THREADS>
@@ -885,11 +858,13 @@ __global__ void k_work_keys(const int* __restrict__ cand_cnt, int64_t n, uint32_
 
 // ------------------------------------------------------------------ launchers
 void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
-                         float4* tinfo, float4* tlo, float4* thi, int64_t* tbin, int* bincnt,
-                         int* large_cnt, unsigned* emax_bits, cudaStream_t st) {
+                         float4* tinfo, float4* tinfo_lo, void* trec, float4* tlo, float4* thi,
+                         int64_t* tbin, int* bincnt, int* large_cnt, unsigned* emax_bits,
+                         cudaStream_t st) {
     if (ntris == 0) return;
     k_sdf_tri_prep<<<static_cast<unsigned>((ntris + 255) / 256), 256, 0, st>>>(
-        segs, nseg, ntris, soup, tinfo, tlo, thi, tbin, bincnt, large_cnt, emax_bits);
+        segs, nseg, ntris, soup, tinfo, tinfo_lo, static_cast<TriRec*>(trec), tlo, thi, tbin,
+        bincnt, large_cnt, emax_bits);
     CMG_LAUNCH();
 }
 
@@ -933,6 +908,9 @@ void launch_count_K(int brick, const MeshSeg* segs, int nseg, int64_t nbricks, c
     if (nbricks == 0) return;
     if (brick == 4)
         k_count_K<4, 64><<<static_cast<unsigned>(nbricks), 64, 0, st>>>(
+            segs, nseg, nbricks, tinfo, cand_off, cand, sdf64, sdf32, band_cells, out);
+    else if (brick == 16)
+        k_count_K<16, 256><<<static_cast<unsigned>(nbricks), 256, 0, st>>>(
             segs, nseg, nbricks, tinfo, cand_off, cand, sdf64, sdf32, band_cells, out);
     else
         k_count_K<8, 128><<<static_cast<unsigned>(nbricks), 128, 0, st>>>(

@@ -1,0 +1,462 @@
+// sdf_sub.cu — distance per cell, evaluated in 4^3 sub-bricks of the 16^3 candidate bricks.
+//
+// The brick candidate lists (k_brick_walk at brick edge 16) hold every triangle
+// that can be nearest to some cell of the brick. One 64-thread CTA per 4^3
+// sub-brick (a persistent kernel over an LPT-ordered queue of sub-bricks):
+//   1. probe: an upper bound U on the distance from the sub-brick centre c to the
+//      surface (FP32 point-triangle distance with its error bound, over the brick
+//      list, each thread skipping triangles whose bounding sphere is beyond its
+//      own bound so far);
+//   2. filter: the brick list is compacted in shared memory to the triangles whose
+//      bounding sphere can reach U + 2 r (r the sub-brick radius) — in rounds of at
+//      most kCap entries;
+//   3. cells, one per thread: a bounding-sphere test per listed triangle, and the
+//      distance only when some lane of the warp needs it; FP64 Ericson in the
+//      reference order (plain) or the FP32 record distance (mixed);
+//   4. mixed only: cells within `band` cells of the surface are re-evaluated in FP64
+//      over the triangles whose FP32 distance is within twice the stated bound of
+//      the FP32 best, which gives the FP64 minimum exactly there.
+// Centroids are stored as FP32 hi + lo pairs relative to the grid corner, so the
+// centroid-to-centre differences are formed in FP32 without losing the low bits
+// (the sub-brick recentring).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <climits>
+
+#include "cmg_device.cuh"
+#include "cmg_sdf.cuh"
+#include "cmg_seg.cuh"
+#include "cmg_types.h"
+#include "cmg_util.h"
+#include "engine_kernels.h"
+
+namespace cmg::gpu {
+
+namespace {
+
+using namespace sdf;
+
+constexpr int kSub = 4;          // sub-brick edge (cells)
+constexpr int kSubThreads = 64;  // one cell per thread
+// filtered candidates per round in shared memory (STAGE: their records as well)
+template <bool STAGE>
+struct Cap {
+    static constexpr int value = STAGE ? 256 : 512;
+};
+constexpr int kBatch = 4;  // candidates per thread per probe/filter step (loads in flight)
+
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only) and its wait.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+}
+
+struct SubGeo {
+    int x0, y0, z0, x1, y1, z1;
+    bool empty;
+};
+
+__device__ __forceinline__ SubGeo sub_geo(const MeshSeg& s, int64_t lb, int sub) {
+    SubGeo q;
+    const int bx = static_cast<int>(lb % s.bnx);
+    const int by = static_cast<int>((lb / s.bnx) % s.bny);
+    const int bz = static_cast<int>(lb / (static_cast<int64_t>(s.bnx) * s.bny));
+    const int per = s.brick / kSub;
+    const int sx = sub % per, sy = (sub / per) % per, sz = sub / (per * per);
+    q.x0 = bx * s.brick + sx * kSub;
+    q.y0 = by * s.brick + sy * kSub;
+    q.z0 = bz * s.brick + sz * kSub;
+    q.x1 = min(q.x0 + kSub, s.g.nx);
+    q.y1 = min(q.y0 + kSub, s.g.ny);
+    q.z1 = min(q.z0 + kSub, s.g.nz);
+    q.empty = q.x0 >= s.g.nx || q.y0 >= s.g.ny || q.z0 >= s.g.nz;
+    return q;
+}
+
+// PREC: kPrecMixed or kPrecFP64. STAGE (mixed only): copy the records of the
+// filtered candidates into shared memory (cp.async) instead of reading them
+// from L1/L2 at evaluation time. grab: consecutive sub-bricks taken from the queue
+// at once (a divisor of 64: they share one brick list).
+template <int PREC, bool STAGE>
+__global__ void __launch_bounds__(kSubThreads, 12)
+k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict__ work,
+          int64_t nwork, int grab_n, unsigned long long* __restrict__ queue,
+          const double* __restrict__ soup,
+          const float4* __restrict__ tinfo, const float4* __restrict__ tinfo_lo,
+          const TriRec* __restrict__ trec, const int64_t* __restrict__ cand_off,
+          const int* __restrict__ cand, const float* __restrict__ brick_emax, float band_cells,
+          Out o, Stats* __restrict__ st) {
+    constexpr int kCap = Cap<STAGE>::value;
+    __shared__ float4 s_c[kCap];  // centroid relative to the sub-brick centre, radius
+    __shared__ int s_t[kCap];
+    __shared__ TriRec s_rec[STAGE ? kCap : 1];
+    __shared__ int s_n;
+    __shared__ long long s_item;
+    __shared__ unsigned long long s_red[kSubThreads / 32];
+    __shared__ int s_band;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned long long evals = 0, evals64 = 0, bandc = 0;
+
+    for (;;) {
+        if (tid == 0) s_item = static_cast<long long>(atomicAdd(queue, 1ull));
+        __syncthreads();
+        const int64_t grab = s_item;
+        __syncthreads();
+        if (grab * grab_n >= nwork) break;
+      for (int gi = 0; gi < grab_n; ++gi) {
+        const int64_t item = grab * grab_n + gi;
+        if (item >= nwork) break;
+        if (tid == 0) s_band = 0;
+        const uint32_t w = work[item];
+        const int64_t gb = static_cast<int64_t>(w >> 6);
+        const int sub = static_cast<int>(w & 63u);
+        const MeshSeg& s = segs[find_seg<&MeshSeg::brick_begin>(segs, nseg, gb)];
+        const GridDesc g = s.g;
+        const SubGeo q = sub_geo(s, gb - s.brick_begin, sub);
+        if (q.empty) continue;
+        // sub-brick centre relative to the grid corner, as an FP32 hi + lo pair
+        const double ckx = 0.5 * (q.x0 + q.x1) * g.h, cky = 0.5 * (q.y0 + q.y1) * g.h,
+                     ckz = 0.5 * (q.z0 + q.z1) * g.h;
+        float chx, clx, chy, cly, chz, clz;
+        split2(ckx, chx, clx);
+        split2(cky, chy, cly);
+        split2(ckz, chz, clz);
+        const double hx = 0.5 * (q.x1 - q.x0 - 1) * g.h, hy = 0.5 * (q.y1 - q.y0 - 1) * g.h,
+                     hz = 0.5 * (q.z1 - q.z0 - 1) * g.h;
+        const float r4 = __double2float_ru(sqrt(hx * hx + hy * hy + hz * hz) * (1.0 + 1e-9));
+        // this thread's cell
+        const int x = q.x0 + (tid & 3), y = q.y0 + ((tid >> 2) & 3), z = q.z0 + (tid >> 4);
+        const bool valid = x < q.x1 && y < q.y1 && z < q.z1;
+        const float px = static_cast<float>((x + 0.5) * g.h - ckx);
+        const float py = static_cast<float>((y + 0.5) * g.h - cky);
+        const float pz = static_cast<float>((z + 0.5) * g.h - ckz);
+        const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
+
+        // ---- 1. probe: upper bound on the distance from the centre to the surface,
+        //         and the triangle that gives it (the seed of every cell below)
+        float tb = FLT_MAX;
+        int tseed = INT_MAX;
+        for (int64_t k0 = c0 + tid; k0 < c1; k0 += kBatch * kSubThreads) {
+            // loads of kBatch candidates in flight before any of them is used
+            int tt[kBatch];
+            float4 hh[kBatch], ll[kBatch];
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i) {
+                const int64_t k = k0 + i * kSubThreads;
+                tt[i] = k < c1 ? cand[k] : -1;
+            }
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i)
+                if (tt[i] >= 0) { hh[i] = tinfo[tt[i]]; ll[i] = tinfo_lo[tt[i]]; }
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i) {
+                if (tt[i] < 0) continue;
+                const int t = tt[i];
+                const float4 hi = hh[i], lo = ll[i];
+                const float rx = (hi.x - chx) + (lo.x - clx);
+                const float ry = (hi.y - chy) + (lo.y - cly);
+                const float rz = (hi.z - chz) + (lo.z - clz);
+                const float dc = sqrtf(rx * rx + ry * ry + rz * rz);
+                const float sb = (dc + hi.w) * (1.f + 8.f * kU32);  // bounding-sphere bound
+                if (sb < tb) { tb = sb; tseed = t; }
+                if (dc - hi.w < tb) {
+                    TriRec r;
+                    load_rec(trec, t, r);
+                    int reg;
+                    const float d = sqrtf(dist_rec(r, -rx, -ry, -rz, &reg));
+                    const float ub = d * (1.f + 32.f * kU32) + 32.f * kU32 * (dc + 2.f * hi.w);
+                    if (ub < tb || (ub == tb && t < tseed)) { tb = ub; tseed = t; }
+                }
+            }
+        }
+        // block argmin of (bound, triangle): bound bits first, then the id
+        unsigned long long key =
+            (static_cast<unsigned long long>(__float_as_uint(tb)) << 32) | static_cast<unsigned>(tseed);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+            key = k2 < key ? k2 : key;
+        }
+        if (lane == 0) s_red[warp] = key;
+        __syncthreads();
+        unsigned long long kmin = s_red[0];
+#pragma unroll
+        for (int i = 1; i < kSubThreads / 32; ++i) kmin = s_red[i] < kmin ? s_red[i] : kmin;
+        const float U = __uint_as_float(static_cast<unsigned>(kmin >> 32));
+        const int seed = static_cast<int>(static_cast<unsigned>(kmin & 0xffffffffull));
+        // a triangle can be nearest to a cell only if its sphere reaches U + 2 r
+        const float limf = (U + 2.f * r4) * (1.f + 32.f * kU32) + 32.f * kU32 * (U + r4);
+
+        // ---- 2+3. rounds: filter into shared memory, then evaluate the cells
+        float best = FLT_MAX, bestd = FLT_MAX;  // FP32 path
+        double best64 = DBL_MAX;                // FP64 path
+        int bt = INT_MAX, br = 0;
+        d3 P{0, 0, 0};
+        if (PREC == kPrecFP64)
+            P = {cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
+                 cell_center(g.corner[2], z, g.h)};
+        if (seed != INT_MAX && valid) {
+            // the centre's nearest triangle: a tight start for every cell's bound
+            const float4 hi = tinfo[seed], lo = tinfo_lo[seed];
+            const float dx = px - ((hi.x - chx) + (lo.x - clx));
+            const float dy = py - ((hi.y - chy) + (lo.y - cly));
+            const float dz = pz - ((hi.z - chz) + (lo.z - clz));
+            if (PREC == kPrecMixed) {
+                TriRec r;
+                load_rec(trec, seed, r);
+                int reg;
+                best = dist_rec(r, dx, dy, dz, &reg);
+                ++evals;
+                bt = seed;
+                br = reg;
+                bestd = sqrtf(best) * (1.f + 8.f * kU32);
+            } else {
+                d3 a, b, c;
+                load_soup(soup, seed, a, b, c);
+                int reg;
+                best64 = ericson(P, a, b, c, &reg);
+                ++evals;
+                bt = seed;
+                br = reg;
+                bestd = __double2float_ru(sqrt(best64)) * (1.f + 8.f * kU32);
+            }
+        }
+        int64_t cursor = c0;
+        while (cursor < c1) {
+            if (tid == 0) s_n = 0;
+            __syncthreads();
+            int n = 0;
+            while (cursor < c1 && n <= kCap - kBatch * kSubThreads) {
+                int tt[kBatch];
+                float4 hh[kBatch], ll[kBatch];
+#pragma unroll
+                for (int i = 0; i < kBatch; ++i) {
+                    const int64_t k = cursor + tid + i * kSubThreads;
+                    tt[i] = k < c1 ? cand[k] : -1;
+                }
+#pragma unroll
+                for (int i = 0; i < kBatch; ++i)
+                    if (tt[i] >= 0) { hh[i] = tinfo[tt[i]]; ll[i] = tinfo_lo[tt[i]]; }
+#pragma unroll
+                for (int i = 0; i < kBatch; ++i) {
+                    bool take = false;
+                    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const int t = tt[i];
+                    if (t >= 0) {
+                        e.x = (hh[i].x - chx) + (ll[i].x - clx);
+                        e.y = (hh[i].y - chy) + (ll[i].y - cly);
+                        e.z = (hh[i].z - chz) + (ll[i].z - clz);
+                        e.w = hh[i].w;
+                        take = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z) - e.w <= limf;
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, take);
+                    int base = 0;
+                    if (lane == 0 && m) base = atomicAdd(&s_n, __popc(m));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (take) {
+                        const int pos = base + __popc(m & ((1u << lane) - 1u));
+                        s_c[pos] = e;
+                        s_t[pos] = t;
+                        if (STAGE) {
+                            const float4* src = reinterpret_cast<const float4*>(trec + t);
+                            float4* dst = reinterpret_cast<float4*>(&s_rec[pos]);
+#pragma unroll
+                            for (int q2 = 0; q2 < 9; ++q2) cp_async16(dst + q2, src + q2);
+                        }
+                    }
+                }
+                cursor += kBatch * kSubThreads;
+                if (STAGE) cp_async_wait_all();
+                __syncthreads();
+                n = s_n;
+            }
+            if (tid == 0 && n) atomicAdd(&st->filtered, static_cast<unsigned long long>(n));
+            for (int j = 0; j < n; ++j) {
+                const float4 e = s_c[j];
+                const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                const float lim = (bestd + e.w) * (1.f + 16.f * kU32) + 16.f * kU32 * r4;
+                const bool need = valid && dx * dx + dy * dy + dz * dz <= lim * lim;
+                if (!__any_sync(0xffffffffu, need)) continue;
+                const int t = s_t[j];
+                if (PREC == kPrecMixed) {
+                    TriRec rr;
+                    if (!STAGE) load_rec(trec, t, rr);
+                    const TriRec& r = STAGE ? s_rec[j] : rr;
+                    if (valid) {
+                        int reg;
+                        const float d2 = dist_rec(r, dx, dy, dz, &reg);
+                        ++evals;
+                        if (d2 < best || (d2 == best && t < bt)) {
+                            best = d2;
+                            bt = t;
+                            br = reg;
+                            bestd = sqrtf(d2) * (1.f + 8.f * kU32);
+                        }
+                    }
+                } else {
+                    d3 a, b, c;
+                    load_soup(soup, t, a, b, c);
+                    if (valid) {
+                        int reg;
+                        const double d2 = ericson(P, a, b, c, &reg);
+                        ++evals;
+                        if (d2 < best64 || (d2 == best64 && t < bt)) {
+                            best64 = d2;
+                            bt = t;
+                            br = reg;
+                            bestd = __double2float_ru(sqrt(d2)) * (1.f + 8.f * kU32);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- 4. mixed: FP64 band
+        float eb = 0.f;
+        bool inband = false;
+        double best_band = DBL_MAX;
+        int bt64 = INT_MAX, br64 = 0;
+        if (PREC == kPrecMixed) {
+            const float d32 = sqrtf(best);
+            eb = 48.f * kU32 * (d32 + 2.f * brick_emax[gb] + 2.f * r4) + 1e-30f;
+            inband = valid && d32 <= band_cells * static_cast<float>(g.h) + eb;
+            if (__any_sync(0xffffffffu, inband) && lane == 0) s_band = 1;
+            __syncthreads();
+            if (s_band) {
+                const float reach = d32 + 2.f * eb;
+                const d3 Pc{cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
+                            cell_center(g.corner[2], z, g.h)};
+                for (int64_t base = c0; base < c1; base += kSubThreads) {
+                    const int64_t k = base + tid;
+                    if (k < c1) {
+                        const int t = cand[k];
+                        const float4 hi = tinfo[t], lo = tinfo_lo[t];
+                        s_c[tid] = make_float4((hi.x - chx) + (lo.x - clx), (hi.y - chy) + (lo.y - cly),
+                                               (hi.z - chz) + (lo.z - clz), hi.w);
+                        s_t[tid] = t;
+                    }
+                    __syncthreads();
+                    const int n = static_cast<int>(c1 - base < kSubThreads ? c1 - base : kSubThreads);
+                    for (int j = 0; j < n; ++j) {
+                        const float4 e = s_c[j];
+                        const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                        const float lim = (reach + e.w) * (1.f + 16.f * kU32) + 16.f * kU32 * r4;
+                        const bool need = inband && dx * dx + dy * dy + dz * dz <= lim * lim;
+                        if (!__any_sync(0xffffffffu, need)) continue;
+                        const int t = s_t[j];
+                        TriRec r;
+                        load_rec(trec, t, r);
+                        if (!need) continue;
+                        int reg;
+                        const float d = sqrtf(dist_rec(r, dx, dy, dz, &reg));
+                        if (d > reach * (1.f + 1e-6f)) continue;
+                        d3 a, b, c;
+                        load_soup(soup, t, a, b, c);
+                        int r64;
+                        const double e2 = ericson(Pc, a, b, c, &r64);
+                        ++evals64;
+                        if (e2 < best_band || (e2 == best_band && t < bt64)) {
+                            best_band = e2;
+                            bt64 = t;
+                            br64 = r64;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+        if (valid) {
+            const int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+            if (PREC == kPrecFP64) {
+                write_cell(o, idx, __dsqrt_rn(best64), bt, br);
+            } else if (inband) {
+                ++bandc;
+                write_cell(o, idx, __dsqrt_rn(best_band), bt64, br64);
+                if (o.errbound) o.errbound[idx] = 0.f;
+            } else {
+                write_cell(o, idx, static_cast<double>(sqrtf(best)), bt, br);
+                if (o.errbound) o.errbound[idx] = eb;
+            }
+        }
+        __syncthreads();
+      }
+    }
+    long long ev = warp_sum(static_cast<long long>(evals));
+    long long ev64 = warp_sum(static_cast<long long>(evals64));
+    long long bc = warp_sum(static_cast<long long>(bandc));
+    if (lane == 0) {
+        if (ev) atomicAdd(&st->evaluations, static_cast<unsigned long long>(ev));
+        const long long f64 = PREC == kPrecFP64 ? ev : ev64;
+        if (f64) atomicAdd(&st->fp64_evaluations, static_cast<unsigned long long>(f64));
+        if (bc) atomicAdd(&st->band_voxels, static_cast<unsigned long long>(bc));
+    }
+}
+
+// Work ids of the sub-bricks (brick * 64 + sub) in LPT order: key = ~brick count.
+__global__ void k_sub_work_keys(const int* __restrict__ cand_cnt, int64_t nbricks,
+                                uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (w >= nbricks * 64) return;
+    keys[w] = ~static_cast<uint32_t>(cand_cnt[w >> 6]);
+    vals[w] = static_cast<uint32_t>(w);
+}
+
+}  // namespace
+
+void launch_sub_work_keys(const int* cand_cnt, int64_t nbricks, uint32_t* keys, uint32_t* vals,
+                          cudaStream_t st) {
+    if (nbricks == 0) return;
+    const int64_t n = nbricks * 64;
+    k_sub_work_keys<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(cand_cnt, nbricks, keys,
+                                                                           vals);
+    CMG_LAUNCH();
+}
+
+int sdf_sub_grid(int precision, bool stage) {
+    int dev = 0, sms = 0, per = 0;
+    CMG_CUDA(cudaGetDevice(&dev));
+    CMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (precision == kPrecMixed && stage)
+        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecMixed, true>,
+                                                               kSubThreads, 0));
+    else if (precision == kPrecMixed)
+        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecMixed, false>,
+                                                               kSubThreads, 0));
+    else
+        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecFP64, false>,
+                                                               kSubThreads, 0));
+    return sms * (per > 0 ? per : 1);
+}
+
+void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, int nseg,
+                    const uint32_t* work, int64_t nwork, unsigned long long* queue, const double* soup,
+                    const float4* tinfo, const float4* tinfo_lo, const void* trec,
+                    const int64_t* cand_off, const int* cand, const float* brick_emax,
+                    float band_cells, const uint8_t* occ, float* sdf32, double* sdf64,
+                    int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats, int grid,
+                    cudaStream_t st) {
+    if (nwork == 0) return;
+    Out o{occ, sdf32, sdf64, near_tri, near_reg, errbound};
+    const TriRec* r = static_cast<const TriRec*>(trec);
+    if (grab != 1 && grab != 2 && grab != 4 && grab != 8) grab = 1;
+    if (precision == kPrecMixed && stage)
+        k_sdf_sub<kPrecMixed, true><<<grid, kSubThreads, 0, st>>>(
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            brick_emax, band_cells, o, stats);
+    else if (precision == kPrecMixed)
+        k_sdf_sub<kPrecMixed, false><<<grid, kSubThreads, 0, st>>>(
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            brick_emax, band_cells, o, stats);
+    else
+        k_sdf_sub<kPrecFP64, false><<<grid, kSubThreads, 0, st>>>(
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            brick_emax, band_cells, o, stats);
+    CMG_LAUNCH();
+}
+
+}  // namespace cmg::gpu

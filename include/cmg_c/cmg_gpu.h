@@ -46,8 +46,12 @@ typedef struct cmg_voxel_opts {
     double spacing;      /* cubic cell edge */
     int dims[3];         /* nx, ny, nz */
     double band;         /* mixed: FP64 refinement band around the surface, in cells */
-    int brick;           /* SDF brick edge: 0 = default, 4 or 8 */
+    int brick;           /* SDF candidate brick edge: 0 = default (16, evaluated by 4^3
+                            sub-bricks), 8 or 4 (one evaluation CTA per brick) */
     int autotune;        /* nonzero: time brick edges on this input and keep the faster */
+    int grab;            /* sub-bricks taken per work-queue grab: 0 = default, 1, 2, 4, 8 */
+    int stage;           /* mixed: 1 stage candidate records in shared memory, 0 read them
+                            through L1/L2, -1 = default */
 } cmg_voxel_opts;
 
 /* Counters of one voxelization. */
@@ -62,6 +66,7 @@ typedef struct cmg_voxel_stats {
     int64_t evaluations;       /* (cell, triangle) distance evaluations */
     int64_t fp64_evaluations;  /* of which in FP64 */
     int64_t band_cells;        /* mixed: cells refined in FP64 */
+    int64_t filtered;          /* SDF: sub-brick candidate entries (each tested by 64 cells) */
     int brick;                 /* brick edge used */
     double max_error_bound;    /* mixed: largest stated per-cell bound (0 for FP64) */
 } cmg_voxel_stats;

@@ -67,7 +67,7 @@ def test_nudge_statistics_match_oracle(cm, golden, orc):
 
 
 @pytest.mark.parametrize("name", [c for c in API_CASES if c != "boxtorus64_r62p1"])
-@pytest.mark.parametrize("brick", [4, 8])
+@pytest.mark.parametrize("brick", [4, 8, 16])
 def test_sdf_float_bit_exact(cm, golden, name, brick):
     g = golden(name)
     r = _run(cm, g, name, outputs=cm.OUT_SDF_F32, brick=brick)
@@ -87,7 +87,7 @@ def test_sdf64_matches_reference_distance(cm, golden, name):
 
 
 @pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "shsphere64_r30p1", "boxtorus64_facegrid"])
-@pytest.mark.parametrize("brick", [4, 8])
+@pytest.mark.parametrize("brick", [4, 8, 16])
 def test_mixed_precision_error(cm, golden, name, brick):
     g = golden(name)
     plain = _run(cm, g, name, outputs=cm.OUT_SDF_F64, brick=brick)
