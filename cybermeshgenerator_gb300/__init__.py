@@ -340,6 +340,56 @@ class Batch:
             self._h = None
 
 
+MEM_HOST, MEM_DEVICE = 0, 1
+
+
+def _stream_call(fn, npt, soa, mode, stream=None):
+    """soa: (3*npt, n) float64 NumPy array (host) or a list of device pointers with n."""
+    if isinstance(soa, np.ndarray):
+        soa = np.ascontiguousarray(soa, dtype=np.float64)
+        if soa.shape[0] != 3 * npt:
+            raise ValueError(f"expected {3 * npt} coordinate rows")
+        n = soa.shape[1]
+        rows = (ctypes.c_void_p * (3 * npt))(*[soa[k].ctypes.data for k in range(3 * npt)])
+        out = np.zeros(n, dtype=np.int8)
+        st = _L.PredStats()
+        err = ctypes.create_string_buffer(512)
+        _check(fn(rows, n, int(mode), MEM_HOST, out.ctypes.data_as(ctypes.c_void_p),
+                  ctypes.byref(st), None, err, 512), err)
+        return out, st.as_dict()
+    ptrs, n, out_ptr = soa
+    rows = (ctypes.c_void_p * (3 * npt))(*ptrs)
+    st = _L.PredStats()
+    err = ctypes.create_string_buffer(512)
+    _check(fn(rows, int(n), int(mode), MEM_DEVICE, ctypes.c_void_p(out_ptr), ctypes.byref(st),
+              ctypes.c_void_p(stream or 0), err, 512), err)
+    return None, st.as_dict()
+
+
+def orient3d_stream(soa, mode: int = PRED_COMPAT, stream=None):
+    """Signs of orient3d queries: soa is a (12, n) float64 array (a, b, c, d in SoA),
+    or (device pointers [12], n, device out pointer). Returns (signs int8, stats)."""
+    return _stream_call(_clib.cmg_orient3d_stream, 4, soa, mode, stream)
+
+
+def insphere_stream(soa, mode: int = PRED_COMPAT, stream=None):
+    """Signs of insphere queries: soa is a (15, n) float64 array (a..e in SoA)."""
+    return _stream_call(_clib.cmg_insphere_stream, 5, soa, mode, stream)
+
+
+def orient3d_signs(points, tets) -> np.ndarray:
+    """robust::orient3d_signs on the GPU: points (N, 3), tets (M, 4) indices."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    t = np.ascontiguousarray(tets, dtype=np.int32)
+    out = np.zeros(len(t), dtype=np.int32)
+    st = _clib.cmg_orient3d_signs(pts.ctypes.data_as(_L.c_double_p), len(pts),
+                                  t.ctypes.data_as(_L.c_int_p), len(t),
+                                  out.ctypes.data_as(_L.c_int_p))
+    if st != 0:
+        raise RuntimeError(f"cmg_orient3d_signs failed with status {st}")
+    return out
+
+
 def gpu_launches() -> int:
     """Kernels launched by the library in this process."""
     return int(_clib.cmg_gpu_launches())
@@ -365,6 +415,6 @@ def library_path() -> str:
     return _L.library_path()
 
 
-__all__ = ["PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
+__all__ = ["orient3d_stream", "insphere_stream", "orient3d_signs", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
            "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
            "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT"]

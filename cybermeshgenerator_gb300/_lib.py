@@ -63,6 +63,14 @@ class WorkModel(ctypes.Structure):
         return {k: float(getattr(self, k)) for k, _ in self._fields_}
 
 
+class PredStats(ctypes.Structure):
+    _fields_ = [("queries", ctypes.c_int64), ("fp64_queries", ctypes.c_int64),
+                ("exact_queries", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 def library_path() -> str:
     return os.environ.get("CMG_C_LIB") or IN_TREE
 
@@ -141,6 +149,9 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_batch_stats", I, [V, ctypes.POINTER(VoxelStats), S, Z])
     sig("cmg_gpu_launches", ctypes.c_longlong, [])
     sig("cmg_gpu_peak_flops", I, [I, c_double_p, S, Z])
+    for n in ("cmg_orient3d_stream", "cmg_insphere_stream"):
+        sig(n, I, [ctypes.POINTER(V), ctypes.c_int64, I, I, V, ctypes.POINTER(PredStats), V, S, Z])
+    sig("cmg_orient3d_signs", I, [c_double_p, I, c_int_p, I, c_int_p])
     sig("cmg_gpu_occupancy_static", I, [V, ctypes.c_int64, V, ctypes.c_int64, c_double_p, D,
                                         c_int_p, I, V, V, S, Z])
 

@@ -37,7 +37,7 @@ __device__ __forceinline__ void two_diff(double a, double b, double& x, double& 
 
 // h = e + f: merge by magnitude, then a Two-Sum sweep, zero-eliminated.
 // h holds elen + flen doubles and may not alias e or f.
-__device__ __noinline__ int sum(int elen, const double* e, int flen, const double* f,
+static __device__ __noinline__ int sum(int elen, const double* e, int flen, const double* f,
                                 double* h) {
     int i = 0, j = 0, hn = 0;
     double q;
@@ -62,7 +62,7 @@ __device__ __noinline__ int sum(int elen, const double* e, int flen, const doubl
 }
 
 // h = b * e, zero-eliminated; h holds 2 * elen doubles.
-__device__ __noinline__ int scale(int elen, const double* e, double b, double* h) {
+static __device__ __noinline__ int scale(int elen, const double* e, double b, double* h) {
     double q, hh;
     int hn = 0;
     two_prod(e[0], b, q, hh);
@@ -80,7 +80,7 @@ __device__ __noinline__ int scale(int elen, const double* e, double b, double* h
 }
 
 // Renormalise in place (Shewchuk's Compress): same value, fewer components.
-__device__ __noinline__ int compress(int m, double* e) {
+static __device__ __noinline__ int compress(int m, double* e) {
     if (m <= 1) return m;
     double q = e[m - 1];
     int bottom = m - 1;
@@ -122,7 +122,7 @@ __device__ __forceinline__ int minor2(double ux, double uy, double vx, double vy
 }
 
 // |pqr| (rows of x, y, z) = pz*m(q,r) - qz*m(p,r) + rz*m(p,q), exactly (<= 24).
-__device__ __noinline__ int det3(const d3& p, const d3& q, const d3& r, double* out) {
+static __device__ __noinline__ int det3(const d3& p, const d3& q, const d3& r, double* out) {
     double mqr[4], mpr[4], mpq[4], s1[8], s2[8], s3[8], t[16];
     int n1 = minor2(q.x, q.y, r.x, r.y, mqr);
     int n2 = minor2(p.x, p.y, r.x, r.y, mpr);
@@ -136,7 +136,7 @@ __device__ __noinline__ int det3(const d3& p, const d3& q, const d3& r, double* 
 
 // Exact orient3d(a,b,c,d) with homogeneous coordinates (no rounding in the
 // differences): |abc| - |abd| + |acd| - |bcd| (<= 96 components).
-__device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b, const d3& c,
+static __device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b, const d3& c,
                                                  const d3& d, double* out) {
     double t1[24], t2[24], t3[24], t4[24], u[48], v[48];
     int n1 = det3(a, b, c, t1);
@@ -151,7 +151,7 @@ __device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b, const
 }
 
 // Exact sign of orient3d(a, b, c, d).
-__device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c, const d3& d) {
+static __device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c, const d3& d) {
     double adx, ady, adz, bdx, bdy, bdz, cdx, cdy, cdz;
     double t0, t1, t2, t3, t4, t5, t6, t7, t8;
     two_diff(a.x, d.x, adx, t0);
@@ -177,7 +177,7 @@ __device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c,
 
 // acc += s * w * x (w a short expansion, x up to 96 components); acc holds cap
 // doubles, work holds cap + 192. Returns the new length or -1 on overflow.
-__device__ __noinline__ int accumulate(int nacc, double* acc, int nw, const double* w, double s,
+static __device__ __noinline__ int accumulate(int nacc, double* acc, int nw, const double* w, double s,
                                        int nx, const double* x, double* work, int cap) {
     double prod[192];
     for (int c = 0; c < nw; ++c) {
@@ -206,7 +206,7 @@ constexpr int kInsphereCap = 256;
 
 // Exact sign of insphere(a, b, c, d, e); sets *overflow when the accumulator
 // capacity is exceeded (the sign is then 0 and must not be trusted).
-__device__ __noinline__ int insphere_sign(const d3& a, const d3& b, const d3& c, const d3& d,
+static __device__ __noinline__ int insphere_sign(const d3& a, const d3& b, const d3& c, const d3& d,
                                           const d3& e, int* overflow) {
     double acc[kInsphereCap], work[kInsphereCap + 192];
     int nacc = 1;

@@ -1,0 +1,413 @@
+// predicates.cu — batched orient3d / insphere sign streams.
+//
+// Semantics per query (src/predicates/robust.cpp:36-50 as initialised by :28-34):
+//   COMPAT: sign of the rounded determinant in Shewchuk's operation order
+//           (predicates.cpp:2201-2222, 4067-4110) unless it is exactly zero, then
+//           the exact sign (the reference's orient3dadapt / insphereadapt result);
+//   EXACT:  the sign of the exact determinant.
+// Three passes, each over a compacted list of the queries the previous pass could
+// not decide, so that divergent work never holds back a full warp:
+//   k_pred_fp32   one thread per query, coordinates streamed from HBM (SoA,
+//                 coalesced), the determinant in FP32 with a rigorous bound that
+//                 covers the rounding of the inputs to FP32 and of every FP32
+//                 operation, plus the FP64 filter bound of the reference: a sign it
+//                 certifies is the exact sign and also the sign of the FP64 rounded
+//                 determinant, so it serves both modes;
+//   k_pred_fp64   the reference's rounded determinant (and, in EXACT mode, its
+//                 permanent bound);
+//   k_pred_exact  expansion arithmetic (cmg_exact.cuh).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/cmg_c/cmg_gpu.h"
+#include "cmg_device.cuh"
+#include "cmg_exact.cuh"
+#include "cmg_types.h"
+#include "cmg_util.h"
+#include "engine.h"
+
+namespace cmg::gpu {
+
+namespace {
+
+constexpr float kU = 5.9604645e-8f;  // 2^-24
+constexpr int kThreads = 256;
+
+struct Soa {
+    const double* c[15];
+};
+
+__device__ __forceinline__ float amax3(float a, float b, float c) {
+    return fmaxf(fabsf(a), fmaxf(fabsf(b), fabsf(c)));
+}
+
+// FP32 orient3d: certified sign (+1/-1) or 0 when the bound does not decide.
+// Differences of inputs rounded to FP32 are off by at most eta = 4 u A (A the
+// largest magnitude among the coordinates, |difference| <= 2A); the determinant
+// (three minor x coordinate terms, two sums) then errs by at most 512 u A^3 to
+// first order; 1024 u A^3 is used. The reference's FP64 bound o3derrboundA * permanent is at
+// most 7.8e-16 * 48 A^3 and is added, so a certified sign is the sign of the
+// FP64 rounded determinant as well.
+__device__ __forceinline__ int o3d_fp32(const double* v) {
+    float f[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) f[i] = __double2float_rn(v[i]);
+    float A = 0.f;
+#pragma unroll
+    for (int i = 0; i < 12; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
+    const float adx = f[0] - f[9], ady = f[1] - f[10], adz = f[2] - f[11];
+    const float bdx = f[3] - f[9], bdy = f[4] - f[10], bdz = f[5] - f[11];
+    const float cdx = f[6] - f[9], cdy = f[7] - f[10], cdz = f[8] - f[11];
+    const float det = adz * (bdx * cdy - cdx * bdy) + bdz * (cdx * ady - adx * cdy) +
+                      cdz * (adx * bdy - bdx * ady);
+    const float A3 = A * A * A * (1.f + 8.f * kU);
+    const float bound = 1024.f * kU * A3 + 4e-14f * A3 + 1e-36f;
+    if (!(A3 < 1e30f)) return 0;  // overflow / non-finite: no certificate
+    return det > bound ? 1 : (det < -bound ? -1 : 0);
+}
+
+// FP32 insphere, same scheme: the lifted 4x4 determinant (four lift x minor
+// products) errs by at most ~4.8e4 u A^5 to first order for inputs rounded to
+// FP32; 2^17 u A^5 is used, plus the reference's FP64 bound isperrboundA *
+// permanent <= 1.8e-15 * 2304 A^5.
+__device__ __forceinline__ int isp_fp32(const double* v) {
+    float f[15];
+#pragma unroll
+    for (int i = 0; i < 15; ++i) f[i] = __double2float_rn(v[i]);
+    float A = 0.f;
+#pragma unroll
+    for (int i = 0; i < 15; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
+    const float aex = f[0] - f[12], aey = f[1] - f[13], aez = f[2] - f[14];
+    const float bex = f[3] - f[12], bey = f[4] - f[13], bez = f[5] - f[14];
+    const float cex = f[6] - f[12], cey = f[7] - f[13], cez = f[8] - f[14];
+    const float dex = f[9] - f[12], dey = f[10] - f[13], dez = f[11] - f[14];
+    const float ab = aex * bey - bex * aey, bc = bex * cey - cex * bey;
+    const float cd = cex * dey - dex * cey, da = dex * aey - aex * dey;
+    const float ac = aex * cey - cex * aey, bd = bex * dey - dex * bey;
+    const float abc = aez * bc - bez * ac + cez * ab;
+    const float bcd = bez * cd - cez * bd + dez * bc;
+    const float cda = cez * da + dez * ac + aez * cd;
+    const float dab = dez * ab + aez * bd + bez * da;
+    const float al = aex * aex + aey * aey + aez * aez;
+    const float bl = bex * bex + bey * bey + bez * bez;
+    const float cl = cex * cex + cey * cey + cez * cez;
+    const float dl = dex * dex + dey * dey + dez * dez;
+    const float det = (dl * abc - cl * dab) + (bl * cda - al * bcd);
+    const float A2 = A * A;
+    const float A5 = A2 * A2 * A * (1.f + 16.f * kU);
+    const float bound = 131072.f * kU * A5 + 6e-12f * A5 + 1e-36f;
+    if (!(A5 < 1e30f)) return 0;
+    return det > bound ? 1 : (det < -bound ? -1 : 0);
+}
+
+template <int NPT>
+__device__ __forceinline__ void load_query(const Soa& s, int64_t i, double* v) {
+#pragma unroll
+    for (int k = 0; k < 3 * NPT; ++k) v[k] = __ldg(s.c[k] + i);
+}
+
+// Appends the lanes with `flag` to list (warp-aggregated).
+__device__ __forceinline__ void push(bool flag, int64_t i, int64_t* list,
+                                     unsigned long long* count) {
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(count, static_cast<unsigned long long>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    if (flag) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+template <int NPT>
+__global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t n, int8_t* __restrict__ out,
+                                                        int64_t* __restrict__ list,
+                                                        unsigned long long* __restrict__ count) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t n_round = (n + 31) & ~int64_t(31);  // whole warps in the loop
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
+         i += stride) {
+        int sg = 0;
+        const bool live = i < n;
+        if (live) {
+            double v[3 * NPT];
+            load_query<NPT>(s, i, v);
+            sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
+            out[i] = static_cast<int8_t>(sg);
+        }
+        push(live && sg == 0, i, list, count);
+    }
+}
+
+template <int NPT, int MODE>
+__global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __restrict__ in,
+                                                        const unsigned long long* __restrict__ nin,
+                                                        int8_t* __restrict__ out,
+                                                        int64_t* __restrict__ list,
+                                                        unsigned long long* __restrict__ count) {
+    const int64_t n = static_cast<int64_t>(*nin);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t n_round = (n + 31) & ~int64_t(31);
+    for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n_round;
+         k += stride) {
+        bool undecided = false;
+        int64_t i = 0;
+        if (k < n) {
+            i = in[k];
+            double v[3 * NPT];
+            load_query<NPT>(s, i, v);
+            const d3 a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]}, d{v[9], v[10], v[11]};
+            double perm = 0.0, det;
+            if (NPT == 4) {
+                det = o3d_fast(a, b, c, d, MODE == kPredExact ? &perm : nullptr);
+                perm *= kO3dErrA;
+            } else {
+                const d3 e{v[12], v[13], v[14]};
+                det = isp_fast(a, b, c, d, e, MODE == kPredExact ? &perm : nullptr);
+                perm *= kIspErrA;
+            }
+            const bool decided = MODE == kPredCompat ? det != 0.0 : (det > perm || -det > perm);
+            if (decided) out[i] = static_cast<int8_t>(sgn(det));
+            undecided = !decided;
+        }
+        push(undecided, i, list, count);
+    }
+}
+
+template <int NPT>
+__global__ void __launch_bounds__(128) k_pred_exact(Soa s, const int64_t* __restrict__ in,
+                                                    const unsigned long long* __restrict__ nin,
+                                                    int8_t* __restrict__ out,
+                                                    unsigned long long* __restrict__ overflow) {
+    const int64_t n = static_cast<int64_t>(*nin);
+    for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t i = in[k];
+        double v[3 * NPT];
+        load_query<NPT>(s, i, v);
+        const d3 a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]}, d{v[9], v[10], v[11]};
+        int sg;
+        if (NPT == 4) {
+            sg = exact::orient3d_sign(a, b, c, d);
+        } else {
+            int of = 0;
+            sg = exact::insphere_sign(a, b, c, d, {v[12], v[13], v[14]}, &of);
+            if (of) atomicAdd(overflow, 1ull);
+        }
+        out[i] = static_cast<int8_t>(sg);
+    }
+}
+
+// Gathers (xyz, tets) index-form queries into SoA for the stream kernels.
+__global__ void k_gather_tets(const double* __restrict__ xyz, const int* __restrict__ tets, int64_t n,
+                              double* __restrict__ soa) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int p = 0; p < 4; ++p) {
+        const int64_t v = tets[4 * i + p];
+        for (int a = 0; a < 3; ++a) soa[(3 * p + a) * n + i] = xyz[3 * v + a];
+    }
+}
+
+__global__ void k_widen(const int8_t* __restrict__ s, int64_t n, int* __restrict__ out) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = s[i];
+}
+
+// Device workspace for the stream (grows, kept per device).
+struct PredWork {
+    Arena arena;
+    std::mutex mu;
+};
+PredWork& pred_work() {
+    static PredWork w[64];
+    int dev = 0;
+    CMG_CUDA(cudaGetDevice(&dev));
+    return w[dev & 63];
+}
+
+struct Counters {
+    unsigned long long n32;  // left by the FP32 pass
+    unsigned long long n64;  // left by the FP64 pass
+    unsigned long long overflow;
+    unsigned long long pad;
+};
+
+}  // namespace
+
+// Runs the three passes on device-resident SoA coordinates.
+void pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
+                        int64_t* list_a, int64_t* list_b, void* counters, cudaStream_t st,
+                        int sms) {
+    Soa s{};
+    for (int k = 0; k < 3 * npt; ++k) s.c[k] = coords[k];
+    Counters* c = static_cast<Counters*>(counters);
+    CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
+    const int grid = 8 * sms;
+    if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, n, d_out, list_a, &c->n32);
+    else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, n, d_out, list_a, &c->n32);
+    CMG_LAUNCH();
+    if (npt == 4 && mode == kPredExact)
+        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+    else if (npt == 4)
+        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+    else if (mode == kPredExact)
+        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+    else
+        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+    CMG_LAUNCH();
+    if (npt == 4) k_pred_exact<4><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
+    else k_pred_exact<5><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
+    CMG_LAUNCH();
+}
+
+}  // namespace cmg::gpu
+
+namespace {
+
+void set_err(char* buf, size_t len, const std::string& msg) {
+    if (buf && len) {
+        std::strncpy(buf, msg.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+}
+
+cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode, int where,
+                      signed char* out, cmg_pred_stats* stats, void* stream, char* errbuf,
+                      size_t len) {
+    using namespace cmg::gpu;
+    if (!coords || !out || n < 0) return CMG_ERR_INVALID_INPUT;
+    if (mode != CMG_PRED_COMPAT && mode != CMG_PRED_EXACT) {
+        set_err(errbuf, len, "predicate mode must be CMG_PRED_COMPAT or CMG_PRED_EXACT");
+        return CMG_ERR_UNSUPPORTED_OPTION;
+    }
+    if (where != CMG_MEM_HOST && where != CMG_MEM_DEVICE) {
+        set_err(errbuf, len, "where must be CMG_MEM_HOST or CMG_MEM_DEVICE");
+        return CMG_ERR_INVALID_INPUT;
+    }
+    for (int k = 0; k < 3 * npt; ++k)
+        if (!coords[k] && n) return CMG_ERR_INVALID_INPUT;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return CMG_OK;
+    try {
+        PredWork& w = pred_work();
+        std::lock_guard<std::mutex> lk(w.mu);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int sms = device_sms();
+        const bool host = where == CMG_MEM_HOST;
+        auto plan = [&](Arena& a, const double** dc, int8_t** dout, int64_t** la, int64_t** lb,
+                        void** cnt) {
+            a.reset();
+            for (int k = 0; k < 3 * npt; ++k) dc[k] = host ? a.take<double>(n) : coords[k];
+            *dout = host ? a.take<int8_t>(n) : reinterpret_cast<int8_t*>(out);
+            *la = a.take<int64_t>(n);
+            *lb = a.take<int64_t>(n);
+            *cnt = a.take<Counters>(1);
+        };
+        const double* dc[15];
+        int8_t* dout;
+        int64_t *la, *lb;
+        void* cnt;
+        w.arena.clear_need();
+        plan(w.arena, dc, &dout, &la, &lb, &cnt);
+        if (w.arena.overflowed()) {
+            w.arena.reserve(w.arena.need());
+            plan(w.arena, dc, &dout, &la, &lb, &cnt);
+        }
+        if (host)
+            for (int k = 0; k < 3 * npt; ++k)
+                CMG_CUDA(cudaMemcpyAsync(const_cast<double*>(dc[k]), coords[k], sizeof(double) * n,
+                                         cudaMemcpyHostToDevice, st));
+        pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout, la,
+                           lb, cnt, st, sms);
+        Counters hc{};
+        CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        if (host) CMG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        if (stats) {
+            stats->queries = n;
+            stats->fp64_queries = static_cast<int64_t>(hc.n32);
+            stats->exact_queries = static_cast<int64_t>(hc.n64);
+        }
+        if (hc.overflow) {
+            set_err(errbuf, len, "insphere: exact expansion exceeded its capacity");
+            return CMG_ERR_INTERNAL;
+        }
+        return CMG_OK;
+    } catch (const std::exception& e) {
+        set_err(errbuf, len, e.what());
+        return CMG_ERR_INTERNAL;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+cmg_status cmg_orient3d_stream(const double* const* coords, int64_t n, int mode, int where,
+                               signed char* out, cmg_pred_stats* stats, void* stream, char* errbuf,
+                               size_t errbuf_len) {
+    return run_stream(4, coords, n, mode, where, out, stats, stream, errbuf, errbuf_len);
+}
+
+cmg_status cmg_insphere_stream(const double* const* coords, int64_t n, int mode, int where,
+                               signed char* out, cmg_pred_stats* stats, void* stream, char* errbuf,
+                               size_t errbuf_len) {
+    return run_stream(5, coords, n, mode, where, out, stats, stream, errbuf, errbuf_len);
+}
+
+cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int n, int* out_sign) {
+    using namespace cmg::gpu;
+    if (n <= 0) return CMG_OK;
+    if (!xyz || !tets || !out_sign || npts <= 0) return CMG_ERR_INVALID_INPUT;
+    for (int i = 0; i < 4 * n; ++i)
+        if (tets[i] < 0 || tets[i] >= npts) return CMG_ERR_INVALID_INPUT;
+    try {
+        PredWork& w = pred_work();
+        std::lock_guard<std::mutex> lk(w.mu);
+        cudaStream_t st = nullptr;
+        const int64_t N = n;
+        auto plan = [&](Arena& a, double** dx, int** dt, double** soa, int8_t** d8, int** dsg,
+                        int64_t** la, int64_t** lb, void** cnt) {
+            a.reset();
+            *dx = a.take<double>(3 * static_cast<size_t>(npts));
+            *dt = a.take<int>(4 * N);
+            *soa = a.take<double>(12 * N);
+            *d8 = a.take<int8_t>(N);
+            *dsg = a.take<int>(N);
+            *la = a.take<int64_t>(N);
+            *lb = a.take<int64_t>(N);
+            *cnt = a.take<Counters>(1);
+        };
+        double *dx, *soa;
+        int *dt, *dsg;
+        int8_t* d8;
+        int64_t *la, *lb;
+        void* cnt;
+        w.arena.clear_need();
+        plan(w.arena, &dx, &dt, &soa, &d8, &dsg, &la, &lb, &cnt);
+        if (w.arena.overflowed()) {
+            w.arena.reserve(w.arena.need());
+            plan(w.arena, &dx, &dt, &soa, &d8, &dsg, &la, &lb, &cnt);
+        }
+        CMG_CUDA(cudaMemcpyAsync(dx, xyz, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
+        CMG_CUDA(cudaMemcpyAsync(dt, tets, sizeof(int) * 4 * N, cudaMemcpyHostToDevice, st));
+        k_gather_tets<<<static_cast<unsigned>((N + 255) / 256), 256, 0, st>>>(dx, dt, N, soa);
+        CMG_LAUNCH();
+        const double* cols[12];
+        for (int k = 0; k < 12; ++k) cols[k] = soa + k * N;
+        pred_stream_device(4, cols, N, kPredCompat, d8, la, lb, cnt, st, device_sms());
+        k_widen<<<static_cast<unsigned>((N + 255) / 256), 256, 0, st>>>(d8, N, dsg);
+        CMG_LAUNCH();
+        CMG_CUDA(cudaMemcpyAsync(out_sign, dsg, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        return CMG_OK;
+    } catch (const std::exception&) {
+        return CMG_ERR_INTERNAL;
+    }
+}
+
+}  // extern "C"

@@ -140,6 +140,39 @@ long long cmg_gpu_launches(void);
  * fp64 != 0 for DFMA, else FFMA. */
 cmg_status cmg_gpu_peak_flops(int fp64, double* flops, char* errbuf, size_t errbuf_len);
 
+/* ---- predicate streams ------------------------------------------------------ */
+/* Where stream arrays live. */
+#define CMG_MEM_HOST 0
+#define CMG_MEM_DEVICE 1
+
+typedef struct cmg_pred_stats {
+    int64_t queries;
+    int64_t fp64_queries;  /* not certified by the FP32 filter */
+    int64_t exact_queries; /* resolved in exact arithmetic */
+} cmg_pred_stats;
+
+/* Signs (-1, 0, +1) of n orient3d(a,b,c,d) queries given as 12 SoA coordinate
+ * arrays (ax ay az bx by bz cx cy cz dx dy dz). mode: CMG_PRED_COMPAT (the
+ * reference's robust::orient3d as initialised: the rounded determinant's sign
+ * unless it is exactly zero, src/predicates/robust.cpp:36-42) or CMG_PRED_EXACT.
+ * where: CMG_MEM_HOST (arrays and out in host memory) or CMG_MEM_DEVICE (device
+ * memory; stream is the cudaStream_t to use, NULL for the default). The call
+ * returns when the signs are written. stats may be NULL. No counterpart in the
+ * reference beyond the scalar predicate it applies per query. */
+cmg_status cmg_orient3d_stream(const double* const* coords, int64_t n, int mode, int where,
+                               signed char* out, cmg_pred_stats* stats, void* stream,
+                               char* errbuf, size_t errbuf_len);
+/* Same for insphere(a,b,c,d,e) with 15 SoA arrays (src/predicates/robust.cpp:44-50). */
+cmg_status cmg_insphere_stream(const double* const* coords, int64_t n, int mode, int where,
+                               signed char* out, cmg_pred_stats* stats, void* stream,
+                               char* errbuf, size_t errbuf_len);
+/* Replaces cmg::backend::cuda::orient3d_signs (src/backend/cuda/orient3d.cu:54-82)
+ * together with the CPU escalation of robust::orient3d_signs
+ * (src/predicates/robust.cpp:68-105): host points xyz[3*npts], candidate
+ * tetrahedra tets[4*n] (indices into xyz), signs equal to the scalar
+ * robust::orient3d's for every candidate, computed entirely on the GPU. */
+cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int n, int* out_sign);
+
 /* ---- occupancy without allocation ----------------------------------------- */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc (a host
  * framework that owns device memory through its own pool, a loop that may not

@@ -1,0 +1,73 @@
+"""Batched orient3d / insphere signs on the GPU against the reference's own signs
+(tests/golden, made from the reference's predicates) and the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kind", ["orient3d", "insphere"])
+@pytest.mark.parametrize("mode", ["compat", "exact"])
+def test_stream_matches_reference_signs(cm, golden, kind, mode):
+    g = golden("predicates")
+    fn = cm.orient3d_stream if kind == "orient3d" else cm.insphere_stream
+    m = cm.PRED_COMPAT if mode == "compat" else cm.PRED_EXACT
+    got, st = fn(g[kind + "_soa"], m)
+    assert np.array_equal(got, g[kind + "_" + mode])
+    assert st["queries"] == g[kind + "_soa"].shape[1]
+
+
+@pytest.mark.parametrize("kind", ["orient3d", "insphere"])
+def test_stream_matches_oracle_large(cm, orc, kind):
+    import oracle as O
+    from cybermeshgenerator_gb300 import workloads as W
+    S = W.predicate_stream(200_000, kind, degenerate=0.1, near=0.1, seed=31)
+    fn = cm.orient3d_stream if kind == "orient3d" else cm.insphere_stream
+    for mode in (cm.PRED_COMPAT, cm.PRED_EXACT):
+        got, st = fn(S, mode)
+        want = orc.stream(kind, S, O.COMPAT if mode == cm.PRED_COMPAT else O.EXACT)
+        assert np.array_equal(got, want)
+        # the FP32 filter certifies the generic queries; ties reach the exact pass
+        assert st["fp64_queries"] < 0.5 * S.shape[1]
+        assert st["exact_queries"] >= int(0.09 * S.shape[1])
+
+
+def test_stream_device_memory(cm):
+    torch = pytest.importorskip("torch")
+    from cybermeshgenerator_gb300 import workloads as W
+    S = W.predicate_stream(50_000, "orient3d", degenerate=0.1, near=0.1, seed=32)
+    host, _ = cm.orient3d_stream(S, cm.PRED_EXACT)
+    d = torch.tensor(S, device="cuda")
+    out = torch.zeros(S.shape[1], dtype=torch.int8, device="cuda")
+    ptrs = [d[k].data_ptr() for k in range(12)]
+    cm.orient3d_stream((ptrs, S.shape[1], out.data_ptr()), cm.PRED_EXACT,
+                       stream=torch.cuda.current_stream().cuda_stream)
+    assert np.array_equal(out.cpu().numpy(), host)
+
+
+def _lcg_cloud(n, s):
+    # the point cloud of tests/test_backend.cpp:14-18 (LCG, 24-bit fractions)
+    pts = []
+    for _ in range(n):
+        p = []
+        for _ in range(3):
+            s = (s * 1664525 + 1013904223) & 0xFFFFFFFF
+            p.append((s >> 8) / float(1 << 24))
+        pts.append(p)
+    return np.array(pts), s
+
+
+def test_orient3d_signs_replaces_cuda_backend(cm, orc):
+    # tests/test_backend.cpp:37-54: 2000 points, 100k random candidate tetrahedra
+    import oracle as O
+    pts, _ = _lcg_cloud(2000, 9)
+    s = 123
+    tets = np.zeros((100_000, 4), dtype=np.int32)
+    for i in range(100_000):
+        for k in range(4):
+            s = (s * 1664525 + 1013904223) & 0xFFFFFFFF
+            tets[i, k] = (s >> 8) % 2000
+    got = cm.orient3d_signs(pts, tets)
+    soa = np.concatenate([pts[tets[:, k]].T for k in range(4)])
+    want = orc.stream("orient3d", soa, O.COMPAT)
+    assert np.array_equal(got, want.astype(np.int32))
