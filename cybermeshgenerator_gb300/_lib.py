@@ -154,6 +154,16 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_orient3d_signs", I, [c_double_p, I, c_int_p, I, c_int_p])
     sig("cmg_gpu_occupancy_static", I, [V, ctypes.c_int64, V, ctypes.c_int64, c_double_p, D,
                                         c_int_p, I, V, V, S, Z])
+    # differentiable signed distance
+    sig("cmg_sdf_plan_create", I, [c_double_p, ctypes.c_int64, c_int_p, ctypes.c_int64, V,
+                                   ctypes.POINTER(V), S, Z])
+    sig("cmg_sdf_plan_forward", I, [V, V, V, S, Z])
+    sig("cmg_sdf_plan_outputs", I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V),
+                                    ctypes.POINTER(V)])
+    sig("cmg_sdf_plan_cells", ctypes.c_int64, [V])
+    sig("cmg_sdf_plan_copy_outputs", I, [V, V, V, V, V, V, S, Z])
+    sig("cmg_sdf_plan_backward", I, [V, V, V, V, V, V, V, V, S, Z])
+    sig("cmg_sdf_plan_destroy", None, [V])
 
 
 _LIB = None

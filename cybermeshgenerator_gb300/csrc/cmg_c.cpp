@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -70,6 +71,21 @@ struct cmg_batch {
     std::vector<GridDesc> grids;
     int outputs = 0;
     bool ran = false;
+};
+
+struct cmg_sdf_plan {
+    std::unique_ptr<cmg::gpu::Batch> batch;
+    GridDesc g{};
+    int64_t npts = 0, ntris = 0, ncell = 0;
+    int64_t* voff = nullptr;  // per point: its (3 * triangle + corner) entries, ascending
+    int* vinc = nullptr;
+    void* tmp = nullptr;      // adjoint workspace
+    bool ran = false;
+    ~cmg_sdf_plan() {
+        if (voff) cudaFree(voff);
+        if (vinc) cudaFree(vinc);
+        if (tmp) cudaFree(tmp);
+    }
 };
 
 namespace {
@@ -563,6 +579,136 @@ cmg_status cmg_batch_stats(cmg_batch* b, cmg_voxel_stats* out, char* errbuf, siz
         *out = v.stats;
         out->cells = b->batch->total_cells();
     });
+}
+
+// ------------------------------------------------------------------ SDF plan (adjoint)
+cmg_status cmg_sdf_plan_create(const double* points, int64_t npoints, const int* triangles,
+                               int64_t ntriangles, const cmg_voxel_opts* opts, cmg_sdf_plan** out,
+                               char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!points || !triangles || !opts || !out || npoints < 1 || ntriangles < 1)
+        return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        if (!opts->explicit_grid)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "cmg_sdf_plan_create: an explicit grid is required"};
+        if (npoints > INT32_MAX || 3 * ntriangles > INT32_MAX)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "cmg_sdf_plan_create: mesh too large"};
+        for (int64_t i = 0; i < 3 * ntriangles; ++i)
+            if (triangles[i] < 0 || triangles[i] >= npoints)
+                throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: facet vertex index out of range"};
+        std::unique_ptr<cmg_sdf_plan> p(new cmg_sdf_plan);
+        GridDesc g{};
+        for (int a = 0; a < 3; ++a) g.corner[a] = opts->corner[a];
+        g.h = opts->spacing;
+        g.nx = opts->dims[0];
+        g.ny = opts->dims[1];
+        g.nz = opts->dims[2];
+        if (!(g.h > 0)) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: spacing must be > 0"};
+        check_grid_size(g);
+        p->g = g;
+        p->npts = npoints;
+        p->ntris = ntriangles;
+        p->ncell = static_cast<int64_t>(g.nx) * g.ny * g.nz;
+        if (p->ncell >= (int64_t(1) << 32))
+            throw CoreError{CMG_ERR_INVALID_INPUT, "cmg_sdf_plan_create: grid too large"};
+        cmg::gpu::VoxOpts vo =
+            to_vox(*opts, CMG_OUT_OCCUPANCY | CMG_OUT_SDF_F64 | CMG_OUT_NEAREST);
+        cmg::gpu::HostMesh m;
+        m.pts = points;
+        m.npts = npoints;
+        m.tris = triangles;
+        m.ntris = ntriangles;
+        m.g = g;
+        // the point -> (triangle, corner) incidence in a fixed order
+        std::vector<int64_t> voff(static_cast<size_t>(npoints + 1), 0);
+        for (int64_t i = 0; i < 3 * ntriangles; ++i) ++voff[static_cast<size_t>(triangles[i]) + 1];
+        for (int64_t v = 0; v < npoints; ++v) voff[v + 1] += voff[v];
+        std::vector<int64_t> cur(voff.begin(), voff.end() - 1);
+        std::vector<int> vinc(static_cast<size_t>(3 * ntriangles));
+        for (int64_t i = 0; i < 3 * ntriangles; ++i) vinc[cur[triangles[i]]++] = static_cast<int>(i);
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cudaStream_t st = gpu_stream();
+        if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick({m}, vo, st);
+        p->batch.reset(new cmg::gpu::Batch({m}, vo, st, /*transient=*/false));
+        CMG_CUDA(cudaMalloc(&p->voff, sizeof(int64_t) * voff.size()));
+        CMG_CUDA(cudaMalloc(&p->vinc, sizeof(int) * vinc.size()));
+        CMG_CUDA(cudaMalloc(&p->tmp, cmg::gpu::adjoint_tmp_bytes(p->ncell, ntriangles)));
+        CMG_CUDA(cudaMemcpy(p->voff, voff.data(), sizeof(int64_t) * voff.size(), cudaMemcpyHostToDevice));
+        CMG_CUDA(cudaMemcpy(p->vinc, vinc.data(), sizeof(int) * vinc.size(), cudaMemcpyHostToDevice));
+        *out = p.release();
+    });
+}
+
+cmg_status cmg_sdf_plan_forward(cmg_sdf_plan* p, const double* d_points, void* stream,
+                                char* errbuf, size_t len) {
+    if (!p) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
+        p->batch->set_stream(st);
+        if (d_points) p->batch->update_points_device(d_points);
+        p->batch->run();
+        p->ran = true;
+    });
+}
+
+cmg_status cmg_sdf_plan_outputs(const cmg_sdf_plan* p, const unsigned char** d_occupancy,
+                                const double** d_sdf, const int** d_nearest_triangle,
+                                const unsigned char** d_nearest_region) {
+    if (!p || !p->ran) return CMG_ERR_INVALID_INPUT;
+    if (d_occupancy) *d_occupancy = p->batch->d_occ();
+    if (d_sdf) *d_sdf = p->batch->d_sdf64();
+    if (d_nearest_triangle) *d_nearest_triangle = p->batch->d_near_tri();
+    if (d_nearest_region) *d_nearest_region = p->batch->d_near_reg();
+    return CMG_OK;
+}
+
+int64_t cmg_sdf_plan_cells(const cmg_sdf_plan* p) { return p ? p->ncell : 0; }
+
+cmg_status cmg_sdf_plan_copy_outputs(const cmg_sdf_plan* p, unsigned char* d_occupancy,
+                                     double* d_sdf, int* d_nearest_triangle,
+                                     unsigned char* d_nearest_region, void* stream, char* errbuf,
+                                     size_t len) {
+    if (!p || !p->ran) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
+        const size_t n = static_cast<size_t>(p->ncell);
+        const cmg::gpu::Batch& b = *p->batch;
+        if (d_occupancy)
+            CMG_CUDA(cudaMemcpyAsync(d_occupancy, b.d_occ(), n, cudaMemcpyDeviceToDevice, st));
+        if (d_sdf)
+            CMG_CUDA(cudaMemcpyAsync(d_sdf, b.d_sdf64(), 8 * n, cudaMemcpyDeviceToDevice, st));
+        if (d_nearest_triangle)
+            CMG_CUDA(cudaMemcpyAsync(d_nearest_triangle, b.d_near_tri(), 4 * n,
+                                     cudaMemcpyDeviceToDevice, st));
+        if (d_nearest_region)
+            CMG_CUDA(cudaMemcpyAsync(d_nearest_region, b.d_near_reg(), n, cudaMemcpyDeviceToDevice,
+                                     st));
+    });
+}
+
+cmg_status cmg_sdf_plan_backward(cmg_sdf_plan* p, const double* d_points,
+                                 const unsigned char* d_occupancy, const int* d_nearest_triangle,
+                                 const unsigned char* d_nearest_region, const double* d_grad_sdf,
+                                 double* d_grad_points, void* stream, char* errbuf, size_t len) {
+    if (!p || !d_occupancy || !d_nearest_triangle || !d_nearest_region || !d_grad_sdf ||
+        !d_grad_points)
+        return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
+        const double* pts = d_points ? d_points : p->batch->d_points();
+        cmg::gpu::adjoint_backward(p->g, p->ncell, pts, p->npts, p->batch->d_tris(), p->ntris,
+                                   d_nearest_triangle, d_nearest_region, d_occupancy, d_grad_sdf,
+                                   p->voff, p->vinc, d_grad_points, p->tmp, st);
+    });
+}
+
+void cmg_sdf_plan_destroy(cmg_sdf_plan* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(gpu_mutex());
+    delete p;
 }
 
 long long cmg_gpu_launches(void) { return cmg::gpu::launches(); }

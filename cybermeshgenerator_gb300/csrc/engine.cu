@@ -184,7 +184,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
             impl_->large_cnt = carve<int>(A, 2 * nseg);
             impl_->large_off = carve<int64_t>(A, nseg + 1);
             impl_->large_list = carve<int>(A, ntris_);
-            impl_->emax_bits = carve<unsigned>(A, nseg);
+            impl_->emax_bits = carve<unsigned>(A, 2 * nseg);  // emax, scale
             impl_->bound = carve<float>(A, nbrick_);
             impl_->cand_cnt = carve<int>(A, nbrick_);
             impl_->cand_off = carve<int64_t>(A, nbrick_ + 1);
@@ -262,18 +262,38 @@ void Batch::update_points(const std::vector<HostMesh>& meshes) {
     }
     CMG_CUDA(cudaMemcpyAsync(pts_, hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice, stream_));
     CMG_CUDA(cudaStreamSynchronize(stream_));
+    resize_ = true;
 }
 
 void Batch::update_points_device(const double* d_pts) {
     CMG_CUDA(cudaMemcpyAsync(pts_, d_pts, sizeof(double) * 3 * npts_, cudaMemcpyDeviceToDevice, stream_));
+    resize_ = true;
 }
 
-void Batch::run() { run_impl(pairs_cap_ < 0 || cand_cap_ < 0); }
+// A sizing pass: reads the list totals back, grows the list arenas if needed and
+// drops the captured graph when a grown arena moved the buffers it refers to.
+void Batch::sized_run() {
+    const size_t pc = impl_->pairs.capacity(), cc = impl_->cands.capacity();
+    run_impl(true);
+    resize_ = false;
+    if ((impl_->pairs.capacity() != pc || impl_->cands.capacity() != cc) && graph_) {
+        CMG_CUDA(cudaStreamSynchronize(stream_));
+        CMG_CUDA(cudaGraphExecDestroy(graph_));
+        graph_ = nullptr;
+        CMG_CUDA(cudaGraphDestroy(impl_->graph));
+        impl_->graph = nullptr;
+    }
+}
+
+void Batch::run() {
+    if (needs_sizing()) sized_run();
+    else run_impl(false);
+}
 
 void Batch::run_graph() {
-    if (pairs_cap_ < 0 || cand_cap_ < 0) {  // size first, outside the capture
-        run_impl(true);
-        CMG_CUDA(cudaStreamSynchronize(stream_));
+    if (needs_sizing()) {  // sizing synchronises, so it runs outside any capture
+        sized_run();
+        return;
     }
     if (!graph_) {
         CMG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
@@ -344,7 +364,7 @@ void Batch::run_impl(bool sizing) {
 
     CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
     CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
-    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * nseg, st));
+    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 2 * nseg, st));
     launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tlo, I.thi,
                         I.tbin, I.bincnt, I.large_cnt, I.emax_bits, st);
     exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);

@@ -93,17 +93,22 @@ public:
     Batch& operator=(const Batch&) = delete;
 
     // Re-uploads point coordinates (same topology and grids), e.g. between
-    // forward passes of an optimisation.
+    // forward passes of an optimisation. Moved points change the bucket and
+    // candidate list lengths, so the next run re-sizes the workspace.
     void update_points(const std::vector<HostMesh>& meshes);
     // Device-pointer form: the coordinates already live on the device
     // (concatenated, 3 doubles per point, triangle indices unchanged).
     void update_points_device(const double* d_pts);
 
-    // Enqueues the pipeline. The first call sizes the workspace (synchronising);
-    // later calls only enqueue.
+    // Enqueues the pipeline. The first call (and the first after an update of the
+    // points) sizes the workspace, synchronising twice; other calls only enqueue.
     void run();
-    // Captures run() into a CUDA graph once, then replays it.
+    // Replays the pipeline as a CUDA graph. A call that must size the workspace
+    // runs the pipeline eagerly instead (and drops a graph whose buffers moved);
+    // the graph is captured at the next call and replayed from then on.
     void run_graph();
+    // Stream for later runs (graph replays included).
+    void set_stream(cudaStream_t st) { stream_ = st; }
     void synchronize();
     void download(std::vector<HostResult>& out, RunInfo* info);
     RunInfo info();
@@ -141,6 +146,7 @@ private:
     std::vector<MeshSeg> segs_;
     int64_t npts_ = 0, ntris_ = 0, ncol_ = 0, nrow_ = 0, nvox_ = 0, nbrick_ = 0, nwork_ = 0;
     int64_t pairs_cap_ = -1, cand_cap_ = -1;
+    bool resize_ = false;  // points moved since the workspace was sized
     double* pts_ = nullptr;
     int* tris_ = nullptr;
     MeshSeg* dsegs_ = nullptr;
@@ -157,6 +163,8 @@ private:
     bool timing_ = false;
     cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     void run_impl(bool sizing);
+    bool needs_sizing() const { return pairs_cap_ < 0 || cand_cap_ < 0 || resize_; }
+    void sized_run();
 };
 
 // Chooses the brick edge for a workload by timing 16 and 8 on the device (cached

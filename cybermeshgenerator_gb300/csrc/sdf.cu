@@ -121,6 +121,17 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         r.pad_[0] = r.pad_[1] = 0.f;
         trec[t] = r;
     }
+    // the mesh's coordinate scale max |v - K| (rounded up), per segment, for the
+    // FP32 tolerances; k_seg_finish folds in the grid extent
+    {
+        double m = 0.0;
+        for (int k = 0; k < 3; ++k)
+            m = fmax(m, fmax(fabs(V[k].x - K[0]), fmax(fabs(V[k].y - K[1]), fabs(V[k].z - K[2]))));
+        const unsigned bits = __float_as_uint(round_up_f(m));
+        const unsigned grp = __match_any_sync(__activemask(), si);
+        const unsigned mx = __reduce_max_sync(grp, bits);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&emax_bits[nseg + si], mx);
+    }
     // degenerate (zero-area) or larger than two bricks: always considered
     const double bw = static_cast<double>(s.brick) * s.g.h;
     bool large = degenerate || sqrt(r2) > 2.0 * bw;
@@ -158,7 +169,9 @@ __global__ void k_bin_fill(int64_t ntris, const int64_t* __restrict__ tbin,
     }
 }
 
-// Writes each mesh's always-considered range and emax into its segment.
+// Writes each mesh's always-considered range, emax and coordinate scale (the
+// larger of max |v - K| over its points and the grid extent, with 1e-4 slack)
+// into its segment.
 __global__ void k_seg_finish(MeshSeg* segs, int nseg, const int64_t* __restrict__ large_off,
                              const unsigned* __restrict__ emax_bits) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -166,6 +179,10 @@ __global__ void k_seg_finish(MeshSeg* segs, int nseg, const int64_t* __restrict_
     segs[i].large_begin = large_off[i];
     segs[i].large_end = large_off[i + 1];
     segs[i].emax = __uint_as_float(emax_bits[i]);
+    const GridDesc& g = segs[i].g;
+    const double ext = g.h * static_cast<double>(max(g.nx, max(g.ny, g.nz)));
+    const double sc = fmax(static_cast<double>(__uint_as_float(emax_bits[nseg + i])), ext);
+    segs[i].scale = __double2float_ru(sc * 1.0001);
 }
 
 // ------------------------------------------------------------------ brick geometry

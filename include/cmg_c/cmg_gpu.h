@@ -140,6 +140,53 @@ long long cmg_gpu_launches(void);
  * fp64 != 0 for DFMA, else FFMA. */
 cmg_status cmg_gpu_peak_flops(int fp64, double* flops, char* errbuf, size_t errbuf_len);
 
+/* ---- differentiable signed distance (forward + adjoint) -------------------- */
+/* No counterpart in the reference (it has no SDF gradient). A plan holds one mesh
+ * of fixed topology on an explicit grid for repeated forwards with moving points
+ * and the adjoint dL/d(points) of the signed distance. */
+typedef struct cmg_sdf_plan cmg_sdf_plan;
+
+/* points: host, 3*npoints doubles (the first positions); triangles: host,
+ * 3*ntriangles indices (fixed). opts->explicit_grid must be set (corner, spacing,
+ * dims); precision, predicates, band and brick apply. Every forward produces
+ * occupancy, the FP64 signed distance and the nearest-feature checkpoint. */
+cmg_status cmg_sdf_plan_create(const double* points, int64_t npoints, const int* triangles,
+                               int64_t ntriangles, const cmg_voxel_opts* opts,
+                               cmg_sdf_plan** out, char* errbuf, size_t errbuf_len);
+/* Voxelizes at the device positions d_points (3*npoints doubles; NULL keeps the
+ * last ones), enqueued on `stream` (a cudaStream_t; NULL for the default stream).
+ * The call synchronises that stream twice (to size the candidate lists for the
+ * new positions) and returns with the evaluation enqueued. */
+cmg_status cmg_sdf_plan_forward(cmg_sdf_plan*, const double* d_points, void* stream,
+                                char* errbuf, size_t errbuf_len);
+/* Device views of the last forward's outputs, valid until the next forward:
+ * occupancy (uint8), signed distance (double), nearest triangle (int, -1 when
+ * none) and its Ericson region (uint8: 0 a, 1 b, 2 ab, 3 c, 4 ac, 5 bc, 6 face);
+ * cell idx = (k*ny + j)*nx + i. CMG_ERR_INVALID_INPUT before the first forward. */
+cmg_status cmg_sdf_plan_outputs(const cmg_sdf_plan*, const unsigned char** d_occupancy,
+                                const double** d_sdf, const int** d_nearest_triangle,
+                                const unsigned char** d_nearest_region);
+int64_t cmg_sdf_plan_cells(const cmg_sdf_plan*);
+/* Copies the last forward's outputs (the four arrays above) into device buffers
+ * the caller owns, enqueued on `stream`; a NULL destination is skipped. */
+cmg_status cmg_sdf_plan_copy_outputs(const cmg_sdf_plan*, unsigned char* d_occupancy,
+                                     double* d_sdf, int* d_nearest_triangle,
+                                     unsigned char* d_nearest_region, void* stream,
+                                     char* errbuf, size_t errbuf_len);
+/* Adjoint: d_grad_points (3*npoints doubles, overwritten) = dL/d(points) given
+ * d_grad_sdf = dL/d(signed distance) per cell, from a forward's checkpoint
+ * (occupancy, nearest triangle, region: device copies the caller kept) and the
+ * positions of that forward (d_points; NULL = the plan's last). Distances are
+ * recomputed in FP64; a cell on the surface (distance 0) contributes nothing.
+ * The reduction has a fixed order (no float atomics): results are bitwise
+ * reproducible. Enqueued on `stream`; allocates nothing. */
+cmg_status cmg_sdf_plan_backward(cmg_sdf_plan*, const double* d_points,
+                                 const unsigned char* d_occupancy, const int* d_nearest_triangle,
+                                 const unsigned char* d_nearest_region, const double* d_grad_sdf,
+                                 double* d_grad_points, void* stream, char* errbuf,
+                                 size_t errbuf_len);
+void cmg_sdf_plan_destroy(cmg_sdf_plan*);
+
 /* ---- predicate streams ------------------------------------------------------ */
 /* Where stream arrays live. */
 #define CMG_MEM_HOST 0

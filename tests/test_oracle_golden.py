@@ -102,3 +102,43 @@ def test_compat_differs_from_exact(golden):
     # the reference's as-initialised signs are not the exact ones on near cases
     g = golden("predicates")
     assert (g["orient3d_compat"] != g["orient3d_exact"]).sum() > 0
+
+
+def _fd_grad(orc, pts, tris, grid, occ, w, t, verts, h=1e-6):
+    """Central differences of L = sum w (sdf - t)^2 of the oracle's FP64 distance,
+    in difference form: L(+h) - L(-h) = sum w (s+ - s-)(s+ + s- - 2t), so that
+    only the cells that change carry rounding."""
+    sgn = np.where(occ != 0, -1.0, 1.0)
+    out = np.zeros((len(verts), 3))
+    for i, v in enumerate(verts):
+        for a in range(3):
+            s = []
+            for step in (h, -h):
+                p = pts.copy()
+                p[v, a] += step
+                d2, _, _ = orc.sdf_brute(p, tris, grid)
+                s.append(sgn * np.sqrt(d2))
+            out[i, a] = np.sum(w * (s[0] - s[1]) * (s[0] + s[1] - 2 * t)) / (2 * h)
+    return out
+
+
+def test_oracle_gradient_matches_central_differences(orc):
+    """The FP64 host analytic gradient (the adjoint's second check) against FP64
+    central differences, h = 1e-6, relative 1e-5."""
+    from cybermeshgenerator_gb300 import workloads as W
+    import oracle as O
+    pts, tris = W.jittered_icosphere(2, 0.02, seed=7)
+    g = orc.make_grid(pts, 14, 1)
+    occ, _ = orc.occupancy(pts, tris, g, O.COMPAT)
+    d2, tri, _ = orc.sdf_brute(pts, tris, g)
+    rng = np.random.default_rng(11)
+    w = rng.uniform(0.0, 1.0, g.ncell)
+    t = rng.normal(0.0, 0.1, g.ncell)
+    grad = orc.sdf_grad(pts, tris, g, occ, tri, w, t)
+    verts = rng.choice(len(pts), size=8, replace=False)
+    fd = _fd_grad(orc, pts, tris, g, occ, w, t, verts)
+    an = grad[verts]
+    assert np.linalg.norm(fd - an) <= 1e-5 * np.linalg.norm(an)
+    # vertices no cell's nearest triangle touches have zero gradient
+    used = np.unique(tris[tri[tri >= 0]].ravel())
+    assert np.all(grad[np.setdiff1d(np.arange(len(pts)), used)] == 0.0)
