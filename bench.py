@@ -10,6 +10,16 @@ surface) for every cell; a voxel query = one cell's occupancy bit + SDF value.
 The plain all-FP64 path (bit-identical to the reference) is timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload sdf|batch|scale|stream]
+
+The default workload (sdf) is the headline above. The others measure the rest of
+the path, each printing one line of the same form:
+  batch   512 meshes (icospheres / tori, resolutions 32-192) in one pipeline,
+          occupancy + mixed SDF, replayed as a CUDA graph, autotuned;
+  scale   2000 ellipsoids (2.56M triangles) at 512^3: forward (occupancy + mixed
+          SDF + nearest-feature checkpoint) and the adjoint per step;
+  stream  1e8 orient3d + 1e8 insphere sign queries (10 % exactly degenerate,
+          10 % within a few ulps), reference semantics.
 
 Under torchrun each rank runs its own replica (weak scaling; the path shares
 nothing between meshes), the timed region is bracketed by barriers and the
@@ -181,7 +191,7 @@ def traffic_from_profile():
     return None
 
 
-def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None):
+def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None, probe=2000):
     """The oracle (CPU restatement of the reference algorithm) on this host: full
     occupancy plus the ring-search SDF on a uniform sample of cells, scaled to
     the grid."""
@@ -195,20 +205,15 @@ def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None):
     orc.occupancy(pts, tris, g, threads=threads)
     t_occ = time.perf_counter() - t0
     rng = np.random.default_rng(7)
-    t0 = time.perf_counter()
-    orc.sdf_ring_sample(pts, tris, g, np.array([n // 2]), threads=threads)
-    t_build = time.perf_counter() - t0
-    # size the sample from a small probe so the run stays near `seconds`
-    probe = rng.choice(n, size=2000, replace=False)
-    t0 = time.perf_counter()
-    orc.sdf_ring_sample(pts, tris, g, probe, threads=threads)
-    per = max((time.perf_counter() - t0 - t_build) / len(probe), 1e-9)
-    m = int(min(n, max(2000, (seconds - t_occ - 2 * t_build) / per)))
+    # size the sample from a small probe so the run stays near `seconds`; the
+    # oracle times its bucket build and its queries separately
+    pv = rng.choice(n, size=min(n, probe), replace=False)
+    _, (t_build, t_q) = orc.sdf_ring_sample(pts, tris, g, pv, threads=threads, times=True)
+    per = max(t_q / len(pv), 1e-9)
+    m = int(min(n, max(probe, (seconds - t_occ - 2 * t_build) / per)))
     vox = rng.choice(n, size=m, replace=False)
-    t0 = time.perf_counter()
-    orc.sdf_ring_sample(pts, tris, g, vox, threads=threads)
-    t_s = time.perf_counter() - t0
-    t_full = t_occ + t_build + (t_s - t_build) * n / m
+    _, (t_build, t_q) = orc.sdf_ring_sample(pts, tris, g, vox, threads=threads, times=True)
+    t_full = t_occ + t_build + t_q / m * n
     return {"value": n / t_full, "unit": UNIT, "cores": int(threads), "kind": "port",
             "sample": f"occupancy on all {n} cells; ring-search SDF on {m} uniformly sampled cells "
                       f"+ the 3-D bucket build, scaled to {n} cells (extrapolated)"}
@@ -349,6 +354,412 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
+# --------------------------------------------------------------------------- other workloads
+def _base_line(metric, unit, value, world, args, total_ms, dtype, config, launches, clocks,
+               higher=True):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": higher, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic", "config": config, "gpu_launches": int(launches),
+            "clocks": clocks}
+
+
+def _events_time(torch, stream, fn, steps, warmup, flush=None):
+    """Device time of `steps` calls of fn() (CUDA events on `stream`)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    pairs = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            if flush is not None:
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            pairs.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in pairs]
+
+
+BATCH_METRIC = "voxel-queries/s, batch of 512 meshes (80-131k tris, 32^3-192^3): occupancy + mixed SDF"
+SCALE_METRIC = "voxel-queries/s, 512^3 grid/2.56M tris: occupancy + mixed SDF + adjoint"
+STREAM_METRIC = "predicate queries/s, 1e8 orient3d + 1e8 insphere (10% degenerate), reference semantics"
+
+
+def _batch_workload():
+    from cybermeshgenerator_gb300 import workloads as W
+    return W.mesh_batch(512)
+
+
+def run_batch(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    items = _batch_workload()
+    plcs = [cm.PLC.from_arrays(b.points, b.triangles) for b in items]
+    res, pads = [b.resolution for b in items], [b.pad for b in items]
+    outs = cm.OUT_OCCUPANCY | cm.OUT_SDF_F32
+    bt = cm.Batch(plcs, res, pads, outputs=outs, precision=cm.PREC_MIXED, autotune=True)
+    bt.run(graph=True).sync()  # sizing
+    bt.run(graph=True).sync()  # capture + replay
+    cells = bt.cells
+    stream = torch.cuda.ExternalStream(bt.stream)
+    l0 = cm.gpu_launches()
+    barrier(world)
+    with Clocks(local) as clk:
+        ms = _events_time(torch, stream, lambda: bt.run(graph=True), args.steps, args.warmup)
+    barrier(world)
+    # graph replays launch kernels the host counter does not see: count one eager pass
+    e0 = cm.gpu_launches()
+    bt.run().sync()
+    launches = cm.gpu_launches() - e0
+    total_ms = max_over_ranks(sum(ms), world)
+    value = cells * world * args.steps / (total_ms * 1e-3)
+    ntris = sum(len(b.triangles) for b in items)
+    st = bt.stats()
+    config = {"workload": f"batch of {len(items)} meshes (icosphere subdivision 1-5 / torus 16-256 "
+                          f"segments, scale 0.5-2, random rotation), {ntris} triangles, "
+                          f"resolutions 32-192 pad 1, {cells} cells: occupancy + mixed SDF",
+              "meshes": len(items), "triangles": int(ntris), "cells": int(cells),
+              "autotuned": {"brick": int(st["brick"]), "grab": int(st["grab"])},
+              "replay": "CUDA graph", "l2": "inputs and outputs larger than L2",
+              "parallelism": f"replicas x{world}"}
+    line = _base_line(BATCH_METRIC, UNIT, value, world, args, total_ms, "fp32+fp64", config,
+                      launches, clk.summary())
+    if rank == 0:
+        bt.set_timing(True)
+        bt.run().sync()
+        tm = bt.timing()
+        wm = bt.work_model()
+        p32 = cm.peak_flops(False)
+        w_sdf = wm["sum_k"] * PT_FLOPS
+        ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
+        line["roofline"] = {"bound": "fp32", "kernel": "k_sdf_mixed (distance evaluation)",
+                            "achieved": ach / 1e12, "peak": p32 / 1e12, "unit": "TFLOP/s",
+                            "frac": frac, "traffic": None, "eval_ms": tm["eval_ms"], "phase_ms": tm,
+                            "work": f"sum_v K(v) * {PT_FLOPS} = {w_sdf:.4g} flops per launch",
+                            "peak_source": "measured FFMA microbenchmark on this GPU"}
+        # end to end: one public batch call per step (plan + upload, pass, download)
+        e2e_t = []
+        for i in range(1 + min(args.steps, 3)):
+            t0 = time.perf_counter()
+            b2 = cm.Batch(plcs, res, pads, outputs=outs, precision=cm.PREC_MIXED, autotune=True)
+            b2.run().sync()
+            for k in range(len(items)):
+                b2.result(k)
+            del b2
+            if i:
+                e2e_t.append(time.perf_counter() - t0)
+        line["e2e"] = {"value": cells / (sum(e2e_t) / len(e2e_t)), "unit": UNIT,
+                       "h2d_bytes_per_step": int(sum(b.points.nbytes + b.triangles.nbytes for b in items)),
+                       "d2h_bytes_per_step": int(cells * 5),
+                       "call": "cmg_batch_create + cmg_batch_run + cmg_batch_get for every mesh"}
+        if not args.no_cpu:
+            line["cpu_baseline"] = _batch_cpu(items, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def _batch_cpu(items, seconds, threads=None):
+    """The oracle on every 64th mesh (occupancy + sampled ring SDF, extrapolated per
+    mesh), summed: voxel-queries/s of the whole batch at that rate."""
+    import oracle
+    orc = oracle.Oracle()
+    tot_cells, tot_t = 0, 0.0
+    sel = items[::64]
+    for b in sel:
+        g = orc.make_grid(b.points, b.resolution, b.pad)
+        r = cpu_baseline(b.points, b.triangles, (tuple(g.corner), g.spacing, g.dims),
+                         seconds=max(1.0, seconds / len(sel)), threads=threads)
+        tot_cells += g.ncell
+        tot_t += g.ncell / r["value"]
+    return {"value": tot_cells / tot_t, "unit": UNIT, "cores": int(threads or os.cpu_count() or 1),
+            "kind": "port", "sample": f"{len(sel)} of the {len(items)} meshes (every 64th): full "
+            "occupancy + ring-search SDF on sampled cells, extrapolated per mesh"}
+
+
+def _scale_workload():
+    from cybermeshgenerator_gb300 import workloads as W
+    return W.ellipsoid_field()
+
+
+def run_scale(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    import oracle
+    from cybermeshgenerator_gb300 import torch_sdf as TS
+    pts, tris = _scale_workload()
+    g = oracle.Oracle().make_grid(pts, 510, 1)
+    grid = TS.grid_of(list(g.corner), g.spacing, (g.nx, g.ny, g.nz))
+    plan = TS.SDFPlan(pts, tris, grid, precision=cm.PREC_MIXED)
+    v = torch.tensor(pts, device="cuda")
+    sdf, occ, tri, reg = plan.forward(v)  # sizing
+    rng = np.random.default_rng(53)
+    w = torch.tensor(rng.uniform(0.0, 1.0, g.ncell), device="cuda")
+    t = torch.tensor(rng.normal(0.0, 0.01, g.ncell), device="cuda")
+    state = {}
+
+    def step():
+        s_, o_, t_, r_ = plan.forward(None)
+        gs = 2.0 * w * (s_ - t)
+        state["grad"] = plan.backward(v, o_, t_, r_, gs)
+
+    stream = torch.cuda.current_stream()
+    l0 = cm.gpu_launches()
+    barrier(world)
+    with Clocks(local) as clk:
+        ms = _events_time(torch, stream, step, args.steps, args.warmup)
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // (args.steps + args.warmup)
+    total_ms = max_over_ranks(sum(ms), world)
+    cells = g.ncell
+    value = cells * world * args.steps / (total_ms * 1e-3)
+    config = {"workload": f"2000 ellipsoids (semi-axes U(0.01,0.04), icosphere subdivision 3), "
+                          f"{len(tris)} triangles, resolution 510 pad 1 ({g.nx}x{g.ny}x{g.nz} cells): "
+                          "occupancy + mixed SDF + nearest-feature checkpoint, then the adjoint of "
+                          "sum w (sdf - t)^2",
+              "triangles": int(len(tris)), "grid": [g.nx, g.ny, g.nz],
+              "l2": "inputs and outputs larger than L2", "parallelism": f"replicas x{world}"}
+    line = _base_line(SCALE_METRIC, UNIT, value, world, args, total_ms, "fp32+fp64", config,
+                      launches, clk.summary())
+    if rank == 0:
+        fwd = _events_time(torch, stream, lambda: plan.forward(None), 2, 1)
+        s_, o_, t_, r_ = plan.forward(None)
+        gs = 2.0 * w * (s_ - t)
+        bwd = _events_time(torch, stream, lambda: plan.backward(v, o_, t_, r_, gs), 3, 1)
+        # algorithmic bytes of one adjoint: the checkpoint (triangle 4 B, region 1 B,
+        # occupancy 1 B) and dL/dsdf (8 B) per cell, the points read and the gradient
+        # written (24 B each per point), the triangles (12 B each)
+        adj_bytes = cells * (4 + 1 + 1 + 8) + len(pts) * 48 + len(tris) * 12
+        hbm = _measured_hbm()
+        line["phases_ms"] = {"forward": sum(fwd) / len(fwd), "adjoint": sum(bwd) / len(bwd)}
+        line["roofline"] = {"bound": "hbm", "kernel": "adjoint (keys, sort, per-triangle sums)",
+                            "achieved": adj_bytes / (sum(bwd) / len(bwd) * 1e-3) / 1e9,
+                            "peak": hbm, "unit": "GB/s",
+                            "frac": adj_bytes / (sum(bwd) / len(bwd) * 1e-3) / 1e9 / hbm,
+                            "traffic": None,
+                            "work": f"{adj_bytes:.4g} algorithmic bytes per adjoint (checkpoint 6 B "
+                                    "+ dL/dsdf 8 B per cell, points and gradient 48 B per point, "
+                                    "triangles 12 B)",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+        # end to end: host vertices in, host gradient out, through the public torch API
+        e2e_t = []
+        host_pts = torch.tensor(pts).pin_memory()
+        for i in range(1 + min(args.steps, 3)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            vd = host_pts.to("cuda", non_blocking=True)
+            s_, o_, t_, r_ = plan.forward(vd)
+            gs = 2.0 * w * (s_ - t)
+            gr = plan.backward(vd, o_, t_, r_, gs).cpu()
+            if i:
+                e2e_t.append(time.perf_counter() - t0)
+        line["e2e"] = {"value": cells / (sum(e2e_t) / len(e2e_t)), "unit": UNIT,
+                       "h2d_bytes_per_step": int(pts.nbytes), "d2h_bytes_per_step": int(gr.numel() * 8),
+                       "call": "SDFPlan.forward + SDFPlan.backward (cmg_sdf_plan_*), host vertices in, "
+                               "host gradient out"}
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(pts, tris, (tuple(g.corner), g.spacing, g.dims),
+                                                seconds=args.cpu_seconds, probe=48)
+            line["cpu_baseline"]["sample"] += " (forward only: the reference has no adjoint)"
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def _measured_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+STREAM_N = 100_000_000
+STREAM_CHUNK = 10_000_000
+
+
+def _stream_soa(kind, n, seed):
+    """n queries built in chunks (bounded host memory for the generator)."""
+    from cybermeshgenerator_gb300 import workloads as W
+    rows = 12 if kind == "orient3d" else 15
+    out = np.empty((rows, n), dtype=np.float64)
+    for c0 in range(0, n, STREAM_CHUNK):
+        m = min(STREAM_CHUNK, n - c0)
+        out[:, c0:c0 + m] = W.predicate_stream(m, kind, degenerate=0.1, near=0.1,
+                                               seed=seed + c0 // STREAM_CHUNK)
+    return out
+
+
+def run_stream(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    n = STREAM_N
+    dev, outs, host = {}, {}, {}
+    for kind, seed in (("orient3d", 1000), ("insphere", 2000)):
+        host[kind] = _stream_soa(kind, n, seed)
+        dev[kind] = torch.from_numpy(host[kind]).to("cuda")
+        outs[kind] = torch.empty(n, dtype=torch.int8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sid = stream.cuda_stream
+    stats = {}
+
+    def step(mode=cm.PRED_COMPAT):
+        for kind, fn in (("orient3d", cm.orient3d_stream), ("insphere", cm.insphere_stream)):
+            d = dev[kind]
+            _, stats[kind] = fn(([d[k].data_ptr() for k in range(d.shape[0])], n,
+                                 outs[kind].data_ptr()), mode, stream=sid)
+
+    l0 = cm.gpu_launches()
+    barrier(world)
+    with Clocks(local) as clk:
+        ms = _events_time(torch, stream, step, args.steps, args.warmup)
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // (args.steps + args.warmup)
+    total_ms = max_over_ranks(sum(ms), world)
+    q = 2 * n
+    value = q * world * args.steps / (total_ms * 1e-3)
+    config = {"workload": f"{n} orient3d + {n} insphere queries, SoA float64 in HBM, 10% exactly "
+                          "coplanar/cospherical (small integers scaled by powers of two), 10% within "
+                          "a few ulps of that, the rest uniform in [0,1)^3; reference semantics "
+                          "(rounded determinant's sign unless exactly zero)",
+              "queries": q, "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
+    line = _base_line(STREAM_METRIC, "queries/s", value, world, args, total_ms, "fp32+fp64+exact",
+                      config, launches, clk.summary())
+    if rank == 0:
+        ex = _events_time(torch, stream, lambda: step(cm.PRED_EXACT), 2, 1)
+        line["exact_mode"] = {"value": q * len(ex) / (sum(ex) * 1e-3), "unit": "queries/s",
+                              "stats": {k: dict(v) for k, v in stats.items()}}
+        step()
+        torch.cuda.synchronize()
+        line["compat_stats"] = {k: dict(v) for k, v in stats.items()}
+        # parity on a sample against the oracle
+        import oracle
+        orc = oracle.Oracle()
+        rng = np.random.default_rng(3)
+        ok = True
+        for kind in ("orient3d", "insphere"):
+            idx = np.sort(rng.choice(n, size=200_000, replace=False))
+            want = orc.stream(kind, np.ascontiguousarray(host[kind][:, idx]), oracle.COMPAT)
+            ok = ok and bool(np.array_equal(outs[kind].cpu().numpy()[idx], want))
+        line["sample_parity"] = {"queries": 400_000, "equal": ok}
+        hbm = _measured_hbm()
+        byts = n * (96 + 1) + n * (120 + 1)
+        t_step = total_ms / args.steps / world * 1e-3
+        line["roofline"] = {"bound": "hbm", "kernel": "k_pred_fp32 (certification pass)",
+                            "achieved": byts / t_step / 1e9, "peak": hbm, "unit": "GB/s",
+                            "frac": byts / t_step / 1e9 / hbm, "traffic": None,
+                            "work": "97 B per orient3d + 121 B per insphere query (coordinates read "
+                                    "once, sign written once)",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+        # end to end: host arrays in, host signs out, through the public call
+        e2e_t = []
+        for i in range(2):
+            t0 = time.perf_counter()
+            cm.orient3d_stream(host["orient3d"], cm.PRED_COMPAT)
+            cm.insphere_stream(host["insphere"], cm.PRED_COMPAT)
+            if i:
+                e2e_t.append(time.perf_counter() - t0)
+        line["e2e"] = {"value": q / (sum(e2e_t) / len(e2e_t)), "unit": "queries/s",
+                       "h2d_bytes_per_step": int(n * (96 + 120)), "d2h_bytes_per_step": int(2 * n),
+                       "call": "cmg_orient3d_stream + cmg_insphere_stream, host arrays"}
+        if not args.no_cpu:
+            line["cpu_baseline"] = _stream_cpu(host, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def _stream_cpu(host, seconds, threads=None):
+    """The oracle's predicate stream (reference semantics) on all host threads, on
+    a contiguous sample of each kind sized to the time budget."""
+    import oracle
+    orc = oracle.Oracle()
+    threads = threads or os.cpu_count() or 1
+    tot_q, tot_t = 0, 0.0
+    for kind in ("orient3d", "insphere"):
+        m = 200_000
+        t0 = time.perf_counter()
+        orc.stream(kind, np.ascontiguousarray(host[kind][:, :m]), oracle.COMPAT, threads=threads)
+        per = (time.perf_counter() - t0) / m
+        m = int(min(host[kind].shape[1], max(m, seconds / 2 / per)))
+        t0 = time.perf_counter()
+        orc.stream(kind, np.ascontiguousarray(host[kind][:, :m]), oracle.COMPAT, threads=threads)
+        tot_t += time.perf_counter() - t0
+        tot_q += m
+    return {"value": tot_q / tot_t, "unit": "queries/s", "cores": int(threads), "kind": "port",
+            "sample": f"{tot_q} queries (the first of each kind), reference semantics"}
+
+
+def _ref_line(metric, unit, value, args, config, base, units_per_step):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": units_per_step / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic", "config": config, "cpu_baseline": base,
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def ref_batch(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    items = _batch_workload()
+    base = _batch_cpu(items, max(10.0, min(60.0, args.cpu_seconds * 2)))
+    orc = oracle.Oracle()
+    cells = sum(orc.make_grid(b.points, b.resolution, b.pad).ncell for b in items)
+    print(json.dumps(_ref_line(BATCH_METRIC, UNIT, base["value"], args,
+                               {"workload": "batch of 512 meshes (see the ours line)",
+                                "parallelism": "cpu threads"}, base, cells)), flush=True)
+
+
+def ref_scale(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    pts, tris = _scale_workload()
+    g = oracle.Oracle().make_grid(pts, 510, 1)
+    base = cpu_baseline(pts, tris, (tuple(g.corner), g.spacing, g.dims),
+                        seconds=max(20.0, args.cpu_seconds), probe=48)
+    print(json.dumps(_ref_line(SCALE_METRIC, UNIT, base["value"], args,
+                               {"workload": "2000 ellipsoids at 512^3 (forward only: the reference "
+                                            "has no adjoint)", "parallelism": "cpu threads"},
+                               base, g.ncell)), flush=True)
+
+
+def ref_stream(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    host = {k: _stream_soa(k, 4 * STREAM_CHUNK // 10, s) for k, s in (("orient3d", 1000),
+                                                                       ("insphere", 2000))}
+    base = _stream_cpu(host, args.cpu_seconds)
+    print(json.dumps(_ref_line(STREAM_METRIC, "queries/s", base["value"], args,
+                               {"workload": "the stream workload's first 4e6 queries of each kind",
+                                "parallelism": "cpu threads"}, base, 2 * STREAM_N)), flush=True)
+
 
 def main():
     ap = argparse.ArgumentParser()
@@ -359,13 +770,16 @@ def main():
     ap.add_argument("--brick", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="sdf", choices=["sdf", "batch", "scale", "stream"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
-        run_reference(args)
+        {"sdf": run_reference, "batch": ref_batch, "scale": ref_scale,
+         "stream": ref_stream}[args.workload](args)
     else:
-        run_ours(args)
+        {"sdf": run_ours, "batch": run_batch, "scale": run_scale,
+         "stream": run_stream}[args.workload](args)
 
 
 if __name__ == "__main__":

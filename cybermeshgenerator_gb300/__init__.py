@@ -88,8 +88,14 @@ class PLC:
         return self
 
     def add_facets(self, triangles) -> "PLC":
-        """Append every row of an (M, k) index array as a facet."""
-        for row in np.asarray(triangles, dtype=np.int32):
+        """Append every row of an (M, k) index array as a facet (one bulk call for
+        triangles)."""
+        a = np.ascontiguousarray(triangles, dtype=np.int32)
+        if a.ndim == 2 and a.shape[1] == 3:
+            _check(_clib.cmg_plc_add_triangles(self._handle, a.ctypes.data_as(_L.c_int_p),
+                                               len(a), 0), ctypes.create_string_buffer(1))
+            return self
+        for row in a:
             self.add_facet(row)
         return self
 

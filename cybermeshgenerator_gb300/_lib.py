@@ -39,7 +39,7 @@ class VoxelStats(ctypes.Structure):
                 ("exact_calls", ctypes.c_int64), ("bucket_entries", ctypes.c_int64),
                 ("candidates", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("fp64_evaluations", ctypes.c_int64), ("band_cells", ctypes.c_int64),
-                ("filtered", ctypes.c_int64), ("brick", ctypes.c_int),
+                ("filtered", ctypes.c_int64), ("brick", ctypes.c_int), ("grab", ctypes.c_int),
                 ("max_error_bound", ctypes.c_double)]
 
     def as_dict(self):
@@ -91,6 +91,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_mesh_destroy", None, [V])
     sig("cmg_plc_set_points", I, [V, c_double_p, Z])
     sig("cmg_plc_add_facet", I, [V, c_int_p, Z, I])
+    sig("cmg_plc_add_triangles", I, [V, c_int_p, Z, I])
     sig("cmg_plc_add_hole", I, [V, D, D, D])
     sig("cmg_plc_add_region", I, [V, D, D, D, D, D])
     sig("cmg_options_set_plc", I, [V, I])

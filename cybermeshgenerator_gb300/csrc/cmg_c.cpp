@@ -39,7 +39,8 @@ struct Region {
 
 struct cmg_plc {
     std::vector<double> points;            // 3 per point
-    std::vector<std::vector<int>> facets;  // one polygon per facet
+    std::vector<int> fidx;                 // facet polygons, concatenated
+    std::vector<size_t> foff{0};           // facet f is fidx[foff[f] .. foff[f+1])
     std::vector<int> markers;
     std::vector<double> holes;
     std::vector<Region> regions;
@@ -121,12 +122,16 @@ cudaStream_t gpu_stream() {
 // (src/voxelize/voxelize.cpp:29-38).
 std::vector<int> fan(const cmg_plc& p) {
     std::vector<int> t;
-    for (const auto& f : p.facets)
-        for (size_t i = 2; i < f.size(); ++i) {
-            t.push_back(f[0]);
-            t.push_back(f[i - 1]);
-            t.push_back(f[i]);
+    t.reserve(3 * (p.fidx.size() - 2 * (p.foff.size() - 1)));
+    for (size_t f = 0; f + 1 < p.foff.size(); ++f) {
+        const int* v = p.fidx.data() + p.foff[f];
+        const size_t n = p.foff[f + 1] - p.foff[f];
+        for (size_t i = 2; i < n; ++i) {
+            t.push_back(v[0]);
+            t.push_back(v[i - 1]);
+            t.push_back(v[i]);
         }
+    }
     return t;
 }
 
@@ -217,6 +222,7 @@ void fill_stats(cmg_voxels* v, const cmg::gpu::RunInfo& ri) {
     s.band_cells = static_cast<int64_t>(ri.stats.band_voxels);
     s.filtered = static_cast<int64_t>(ri.stats.filtered);
     s.brick = ri.brick;
+    s.grab = ri.grab;
     double m = 0;
     for (float e : v->r.err) m = std::max(m, static_cast<double>(e));
     s.max_error_bound = m;
@@ -259,7 +265,7 @@ cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
     m.g = g;
     std::lock_guard<std::mutex> lk(gpu_mutex());
     cudaStream_t st = gpu_stream();
-    if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick({m}, vo, st);
+    if (vo.autotune && vo.brick == 0) cmg::gpu::autotune({m}, vo, st);
     std::unique_ptr<cmg_voxels> v(new cmg_voxels);
     set_geometry(v.get(), g);
     cmg::gpu::Batch b({m}, vo, st, /*transient=*/true);
@@ -316,8 +322,23 @@ cmg_status cmg_plc_add_facet(cmg_plc* plc, const int* idx, size_t count, int mar
     if (!plc || (!idx && count)) return CMG_ERR_INVALID_INPUT;
     if (count < 3) return CMG_ERR_INVALID_INPUT;
     try {
-        plc->facets.emplace_back(idx, idx + count);
+        plc->fidx.insert(plc->fidx.end(), idx, idx + count);
+        plc->foff.push_back(plc->fidx.size());
         plc->markers.push_back(marker);
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
+cmg_status cmg_plc_add_triangles(cmg_plc* plc, const int* idx, size_t count, int marker) {
+    if (!plc || (!idx && count)) return CMG_ERR_INVALID_INPUT;
+    try {
+        plc->fidx.insert(plc->fidx.end(), idx, idx + 3 * count);
+        const size_t base = plc->foff.back();
+        plc->foff.reserve(plc->foff.size() + count);
+        for (size_t f = 1; f <= count; ++f) plc->foff.push_back(base + 3 * f);
+        plc->markers.insert(plc->markers.end(), count, marker);
     } catch (...) {
         return CMG_ERR_INTERNAL;
     }
@@ -489,7 +510,7 @@ cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, 
         cmg::gpu::VoxOpts vo = to_vox(*opts, b->outputs);
         std::lock_guard<std::mutex> lk(gpu_mutex());
         cudaStream_t st = gpu_stream();
-        if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick(meshes, vo, st);
+        if (vo.autotune && vo.brick == 0) cmg::gpu::autotune(meshes, vo, st);
         b->batch.reset(new cmg::gpu::Batch(meshes, vo, st, /*transient=*/false));
         *out = b.release();
     });
@@ -628,7 +649,7 @@ cmg_status cmg_sdf_plan_create(const double* points, int64_t npoints, const int*
         for (int64_t i = 0; i < 3 * ntriangles; ++i) vinc[cur[triangles[i]]++] = static_cast<int>(i);
         std::lock_guard<std::mutex> lk(gpu_mutex());
         cudaStream_t st = gpu_stream();
-        if (vo.autotune && vo.brick == 0) vo.brick = cmg::gpu::autotune_brick({m}, vo, st);
+        if (vo.autotune && vo.brick == 0) cmg::gpu::autotune({m}, vo, st);
         p->batch.reset(new cmg::gpu::Batch({m}, vo, st, /*transient=*/false));
         CMG_CUDA(cudaMalloc(&p->voff, sizeof(int64_t) * voff.size()));
         CMG_CUDA(cudaMalloc(&p->vinc, sizeof(int) * vinc.size()));

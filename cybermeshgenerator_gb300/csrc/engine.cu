@@ -463,6 +463,7 @@ RunInfo Batch::info() {
     CMG_CUDA(cudaMemcpyAsync(&r.stats, stats_, sizeof(Stats), cudaMemcpyDeviceToHost, stream_));
     CMG_CUDA(cudaStreamSynchronize(stream_));
     r.brick = opts_.brick;
+    r.grab = opts_.brick == 16 ? opts_.grab : 0;
     r.cells = nvox_;
     r.pairs = pairs_cap_;
     r.candidates = cand_cap_;
@@ -493,29 +494,42 @@ void Batch::download(std::vector<HostResult>& out, RunInfo* info) {
 }
 
 // ------------------------------------------------------------------ autotuner
-int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream) {
+void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t stream) {
     static std::mutex mu;
-    static std::map<std::tuple<int, int, int, int>, int> cache;
+    static std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> cache;
     int64_t tris = 0, cells = 0;
     for (const HostMesh& m : meshes) {
         tris += m.ntris;
         cells += static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
     }
+    const bool sdf = opts.want_sdf32 || opts.want_sdf64 || opts.want_near;
+    if (!sdf) return;  // the occupancy kernels have no tunables
     auto lg = [](int64_t v) { return v > 0 ? static_cast<int>(std::log2(static_cast<double>(v)) * 2) : 0; };
-    auto key = std::make_tuple(opts.precision, lg(tris), lg(cells), static_cast<int>(meshes.size() > 1));
+    auto key = std::make_tuple(opts.precision, lg(tris), lg(cells),
+                               static_cast<int>(std::min<size_t>(meshes.size(), 4)),
+                               static_cast<int>(opts.want_sdf64));
     {
         std::lock_guard<std::mutex> g(mu);
         auto it = cache.find(key);
-        if (it != cache.end()) return it->second;
+        if (it != cache.end()) {
+            opts.brick = it->second.first;
+            opts.grab = it->second.second;
+            return;
+        }
     }
+    // candidates: 16^3 candidate bricks evaluated by 4^3 sub-bricks taken 1 or 2 per
+    // queue grab, or 8^3 bricks with one evaluation CTA each
+    const std::pair<int, int> cand[] = {{16, 1}, {16, 2}, {8, 1}};
     float best_ms = 0.f;
-    int best = 16;
+    std::pair<int, int> best = cand[0];
     cudaEvent_t e0, e1;
     CMG_CUDA(cudaEventCreate(&e0));
     CMG_CUDA(cudaEventCreate(&e1));
-    for (int b : {16, 8}) {
+    bool first = true;
+    for (const auto& c : cand) {
         VoxOpts o = opts;
-        o.brick = b;
+        o.brick = c.first;
+        o.grab = c.second;
         o.autotune = false;
         Batch bt(meshes, o, stream);
         bt.run();  // sizing run (warms up as well)
@@ -526,16 +540,18 @@ int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cud
         CMG_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
         CMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (b == 16 || ms < best_ms) {
+        if (first || ms < best_ms) {
             best_ms = ms;
-            best = b;
+            best = c;
+            first = false;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> g(mu);
     cache[key] = best;
-    return best;
+    opts.brick = best.first;
+    opts.grab = best.second;
 }
 
 }  // namespace cmg::gpu

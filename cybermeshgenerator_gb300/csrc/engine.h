@@ -76,6 +76,7 @@ struct WorkModel {
 struct RunInfo {
     Stats stats{};
     int brick = 0;
+    int grab = 0;
     int64_t cells = 0;
     int64_t pairs = 0;       // (triangle, column) bucket entries
     int64_t candidates = 0;  // (brick, triangle) candidate entries
@@ -167,9 +168,11 @@ private:
     void sized_run();
 };
 
-// Chooses the brick edge for a workload by timing 16 and 8 on the device (cached
-// per process by workload shape).
-int autotune_brick(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStream_t stream);
+// Sets opts.brick and opts.grab for a workload by timing the candidates (16^3
+// bricks with 1 or 2 sub-bricks per queue grab, 8^3 bricks) on the device; the
+// choice is cached per process by workload shape (precision, log2 of triangle and
+// cell counts, number of meshes).
+void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t stream);
 
 // Number of SMs of the current device.
 int device_sms();

@@ -88,15 +88,22 @@ class SDFPlan:
             raise ValueError(f"vertices must have shape ({self.npoints}, 3)")
         return vertices.detach().to(torch.float64).contiguous()
 
-    def forward(self, vertices: torch.Tensor) -> Tuple[torch.Tensor, ...]:
+    def forward(self, vertices: Optional[torch.Tensor]) -> Tuple[torch.Tensor, ...]:
         """(sdf float64, occupancy uint8, nearest triangle int32, region uint8), each
-        a flat tensor of the grid's cells (idx = (k*ny + j)*nx + i)."""
-        p = self._points(vertices)
-        dev = p.device
+        a flat tensor of the grid's cells (idx = (k*ny + j)*nx + i). ``vertices=None``
+        reuses the last positions (no re-sizing, nothing synchronised)."""
+        if vertices is None:
+            if getattr(self, "_device", None) is None:
+                raise ValueError("the first forward needs vertices")
+            p, dev, ptr = None, self._device, 0
+        else:
+            p = self._points(vertices)
+            dev, ptr = p.device, p.data_ptr()
+            self._device = dev
         err = _err()
         with torch.cuda.device(dev):
             st = _stream()
-            _check(_clib.cmg_sdf_plan_forward(self._h, p.data_ptr(), st, err, 512), err)
+            _check(_clib.cmg_sdf_plan_forward(self._h, ptr, st, err, 512), err)
             n = self.cells
             sdf = torch.empty(n, dtype=torch.float64, device=dev)
             occ = torch.empty(n, dtype=torch.uint8, device=dev)

@@ -410,7 +410,13 @@ def predicate_stream(n: int, kind: str = "orient3d", degenerate: float = 0.1,
             pts = [a, b, c, d]
         else:
             lat = _sphere_lattice_points(27625)  # 1152 integer points on the sphere
-            sel = np.stack([rng.choice(len(lat), size=5, replace=False) for _ in range(m)])
+            sel = rng.integers(0, len(lat), size=(m, 5))
+            while True:  # five distinct points per query: redraw rows with a repeat
+                srt = np.sort(sel, axis=1)
+                dup = (srt[:, 1:] == srt[:, :-1]).any(axis=1)
+                if not dup.any():
+                    break
+                sel[dup] = rng.integers(0, len(lat), size=(int(dup.sum()), 5))
             off = rng.integers(-32, 33, size=(3, m)).astype(np.float64)
             pts = [lat[sel[:, i]].T + off for i in range(5)]
         perm = rng.permutation(npt)
@@ -421,14 +427,14 @@ def predicate_stream(n: int, kind: str = "orient3d", degenerate: float = 0.1,
             k = rng.integers(0, npt, size=nn)
             ax = rng.integers(0, 3, size=nn)
             ulps = rng.integers(1, 4, size=nn) * rng.choice([-1, 1], size=nn)
-            for q in range(nn):
-                col = nea[q]
-                v = P[k[q]][ax[q], col]
-                if v == 0.0:  # stay clear of subnormals (no expansion arithmetic there)
-                    v = float(ulps[q]) * 2.0 ** -60
-                    P[k[q]][ax[q], col] = v
-                    continue
-                for _ in range(abs(int(ulps[q]))):
-                    v = np.nextafter(v, np.inf if ulps[q] > 0 else -np.inf)
-                P[k[q]][ax[q], col] = v
+            v = P[k, ax, nea]
+            zero = v == 0.0
+            toward = np.where(ulps > 0, np.inf, -np.inf)
+            for step in range(1, 4):
+                sel_ = ~zero & (np.abs(ulps) >= step)
+                v[sel_] = np.nextafter(v[sel_], toward[sel_])
+            # a zero coordinate becomes +-k*2^-60, clear of subnormals (no expansion
+            # arithmetic there)
+            v[zero] = ulps[zero].astype(np.float64) * 2.0 ** -60
+            P[k, ax, nea] = v
     return np.ascontiguousarray(P.reshape(npt * 3, n))

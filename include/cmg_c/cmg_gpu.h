@@ -48,7 +48,8 @@ typedef struct cmg_voxel_opts {
     double band;         /* mixed: FP64 refinement band around the surface, in cells */
     int brick;           /* SDF candidate brick edge: 0 = default (16, evaluated by 4^3
                             sub-bricks), 8 or 4 (one evaluation CTA per brick) */
-    int autotune;        /* nonzero: time brick edges on this input and keep the faster */
+    int autotune;        /* nonzero (with brick 0): time the brick edges and queue grab
+                            sizes on this input and keep the fastest */
     int grab;            /* sub-bricks taken per work-queue grab: 0 = default, 1, 2, 4, 8 */
     int stage;           /* mixed: 1 stage candidate records in shared memory, 0 read them
                             through L1/L2, -1 = default */
@@ -68,11 +69,17 @@ typedef struct cmg_voxel_stats {
     int64_t band_cells;        /* mixed: cells refined in FP64 */
     int64_t filtered;          /* SDF: sub-brick candidate entries (each tested by 64 cells) */
     int brick;                 /* brick edge used */
+    int grab;                  /* sub-bricks per work-queue grab used (16^3 bricks) */
     double max_error_bound;    /* mixed: largest stated per-cell bound (0 for FP64) */
 } cmg_voxel_stats;
 
 /* Defaults: resolution 64, pad 1, occupancy, FP64, compat predicates, band 1. */
 void cmg_voxel_opts_init(cmg_voxel_opts* opts);
+
+/* Appends `count` triangular facets (idx: 3*count vertex indices), each as
+ * cmg_plc_add_facet(plc, idx + 3*i, 3, marker) would, in one call. No
+ * counterpart in the reference; for meshes of millions of triangles. */
+cmg_status cmg_plc_add_triangles(cmg_plc*, const int* idx, size_t count, int marker);
 
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */

@@ -155,15 +155,19 @@ class Oracle:
                             _ptr(s32, _fp), ctypes.c_int(self.threads(threads)))
         return s64, s32
 
-    def sdf_ring_sample(self, pts, tris, g: Grid, vox, threads=None):
+    def sdf_ring_sample(self, pts, tris, g: Grid, vox, threads=None, times=False):
+        """Ring-search squared distances at the listed voxels; with times=True also
+        (bucket build seconds, query seconds)."""
         pts, tris = _f64(pts), _i32(tris)
         vox = np.ascontiguousarray(vox, dtype=np.int64)
         d2 = np.zeros(len(vox), dtype=np.float64)
+        tm = np.zeros(2, dtype=np.float64)
         self.L.orc_sdf_ring_sample(_ptr(pts, _dp), _ptr(tris, _ip),
                                    ctypes.c_int64(len(tris)), ctypes.byref(g),
                                    _ptr(vox, _i64p), ctypes.c_int64(len(vox)),
-                                   _ptr(d2, _dp), ctypes.c_int(self.threads(threads)))
-        return d2
+                                   _ptr(d2, _dp), ctypes.c_int(self.threads(threads)),
+                                   _ptr(tm, _dp))
+        return (d2, (float(tm[0]), float(tm[1]))) if times else d2
 
     def sdf_brute(self, pts, tris, g: Grid, vox=None, threads=None):
         """Brute-force nearest (d2, triangle, region) at the listed voxels (all if None)."""

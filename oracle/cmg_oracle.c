@@ -4,12 +4,14 @@
  * -ffp-contract=off and without -ffast-math: every floating-point expression here
  * must round exactly as the reference's x86-64 (SSE2, no FMA) build rounds it.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include "cmg_oracle.h"
 
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -753,13 +755,23 @@ static double* tri_points(const double* pts, const int* tris, int64_t ntris) {
     return tp;
 }
 
+static double now_seconds(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* times (nullable): [0] the bucket build, [1] the queries, in seconds. */
 static void ring_run(const double* pts, const int* tris, int64_t ntris,
                      const orc_grid* g, const int64_t* vox, int64_t nq, double* d2out,
-                     const uint8_t* occ, double* sdf64, float* sdf32, int nthreads) {
+                     const uint8_t* occ, double* sdf64, float* sdf32, int nthreads,
+                     double* times) {
     (void)nthreads;
+    double t0 = now_seconds();
     xyz_buckets B;
     build_xyz(pts, tris, ntris, g, &B);
     double* tp = tri_points(pts, tris, ntris);
+    double t1 = now_seconds();
 #ifdef _OPENMP
 #pragma omp parallel num_threads(nthreads)
 #endif
@@ -768,7 +780,7 @@ static void ring_run(const double* pts, const int* tris, int64_t ntris,
         for (int64_t t = 0; t < ntris; ++t) seen[t] = -1;
         ring_ctx c = {g, &B, tp, seen, 0, DBL_MAX, NULL, 0};
 #ifdef _OPENMP
-#pragma omp for schedule(dynamic, 64)
+#pragma omp for schedule(dynamic, 4)
 #endif
         for (int64_t q = 0; q < nq; ++q) {
             int64_t idx = vox ? vox[q] : q;
@@ -788,6 +800,10 @@ static void ring_run(const double* pts, const int* tris, int64_t ntris,
         }
         free(seen);
     }
+    if (times) {
+        times[0] = t1 - t0;
+        times[1] = now_seconds() - t1;
+    }
     free(tp);
     free(B.off);
     free(B.list);
@@ -797,13 +813,13 @@ void orc_sdf_ring(const double* pts, const int* tris, int64_t ntris,
                   const orc_grid* g, const uint8_t* occ, double* sdf64, float* sdf32,
                   int nthreads) {
     int64_t n = (int64_t)g->nx * g->ny * g->nz;
-    ring_run(pts, tris, ntris, g, NULL, n, NULL, occ, sdf64, sdf32, nthreads);
+    ring_run(pts, tris, ntris, g, NULL, n, NULL, occ, sdf64, sdf32, nthreads, NULL);
 }
 
 void orc_sdf_ring_sample(const double* pts, const int* tris, int64_t ntris,
                          const orc_grid* g, const int64_t* vox, int64_t nq,
-                         double* d2, int nthreads) {
-    ring_run(pts, tris, ntris, g, vox, nq, d2, NULL, NULL, NULL, nthreads);
+                         double* d2, int nthreads, double* times) {
+    ring_run(pts, tris, ntris, g, vox, nq, d2, NULL, NULL, NULL, nthreads, times);
 }
 
 void orc_dist2_points(const double* pts, const int* tris, int64_t ntris,

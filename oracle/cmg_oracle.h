@@ -103,10 +103,11 @@ void orc_sdf_ring(const double* pts, const int* tris, int64_t ntris,
                   const orc_grid* g, const uint8_t* occ, double* sdf64, float* sdf32,
                   int nthreads);
 /* Ring search restricted to the listed voxels (flat indices); unsigned distance
- * squared out. Used to time a bounded sample. Includes the bucket build. */
+ * squared out. Used to time a bounded sample: times (nullable) receives the
+ * seconds of the bucket build [0] and of the queries [1]. */
 void orc_sdf_ring_sample(const double* pts, const int* tris, int64_t ntris,
                          const orc_grid* g, const int64_t* vox, int64_t nq,
-                         double* d2, int nthreads);
+                         double* d2, int nthreads, double* times);
 /* Brute force over every triangle for the listed voxels: nearest squared distance,
  * the first triangle attaining it (ascending id) and its Ericson region. */
 void orc_sdf_brute(const double* pts, const int* tris, int64_t ntris,

@@ -2,7 +2,7 @@
 
 Run where the reference sources are available (it builds oracle/_ref from them):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]   # all cases, or only those named
 
 Every fixture stores its input mesh as raw float64/int32 bits (so hosts whose
 libm differs still see identical inputs) and the reference's outputs:
@@ -92,44 +92,58 @@ def pred_case(ref, name, n, seed):
 def main():
     O.build(ref=True)
     ref = O.Reference()
-    manifest = {}
+    only = set(sys.argv[1:])
+    path = os.path.join(HERE, "MANIFEST.json")
+    manifest = json.load(open(path)) if only and os.path.exists(path) else {}
+
+    def want(name):
+        return not only or name in only
 
     pts, tris = W.jittered_icosphere(3, 0.02, seed=1)
-    api_case(ref, "icosphere_s3_r58p3", pts, tris, 58, 3, nsample=2048)
+    if want("icosphere_s3_r58p3"):
+        api_case(ref, "icosphere_s3_r58p3", pts, tris, 58, 3, nsample=2048)
     manifest["icosphere_s3_r58p3"] = "icosphere subdivision 3, radial jitter 2% (seed 1); resolution 58, pad 3 (64^3)"
 
     pts, tris = W.subdivided_cube(4)
-    api_case(ref, "cube4_r16p1", pts, tris, 16, 1)
+    if want("cube4_r16p1"):
+        api_case(ref, "cube4_r16p1", pts, tris, 16, 1)
     manifest["cube4_r16p1"] = "reference test fixture subdivided_cube(4); resolution 16, pad 1 (exact 16^3 block)"
 
     pts, tris = W.uv_sphere(1.0, 16, 16)
-    api_case(ref, "uvsphere16_r20p1", pts, tris, 20, 1)
+    if want("uvsphere16_r20p1"):
+        api_case(ref, "uvsphere16_r20p1", pts, tris, 20, 1)
     manifest["uvsphere16_r20p1"] = "reference test fixture sphere_plc(1,16,16); resolution 20, pad 1"
 
     pts, tris = W.brick(3.0, 1.0, 2.0)
-    api_case(ref, "brick312_r20p1", pts, tris, 20, 1)
+    if want("brick312_r20p1"):
+        api_case(ref, "brick312_r20p1", pts, tris, 20, 1)
     manifest["brick312_r20p1"] = "box [0,3]x[0,1]x[0,2]; resolution 20, pad 1 (axis order)"
 
     pts, tris = W.sh_sphere(nlon=64, nlat=32, seed=3)
-    api_case(ref, "shsphere64_r30p1", pts, tris, 30, 1)
+    if want("shsphere64_r30p1"):
+        api_case(ref, "shsphere64_r30p1", pts, tris, 30, 1)
     manifest["shsphere64_r30p1"] = "SH star surface on a 64x32-band UV sphere (seed 3); resolution 30, pad 1"
 
     pts, tris = W.box_and_torus(64, 32)
     h = 2.0 ** -5
-    grid_case(ref, "boxtorus64_facegrid", pts, tris, [-16.5 * h, -16.5 * h, -10.5 * h], h, (64, 64, 64))
+    if want("boxtorus64_facegrid"):
+        grid_case(ref, "boxtorus64_facegrid", pts, tris, [-16.5 * h, -16.5 * h, -10.5 * h], h, (64, 64, 64))
     manifest["boxtorus64_facegrid"] = ("unit box + torus(R .35, r .12, 64x32) on an explicit 64^3 grid, h=2^-5, "
                                        "cell centres exactly on the box faces (forces grazes)")
-    api_case(ref, "boxtorus64_r62p1", pts, tris, 62, 1, full_sdf=False)
+    if want("boxtorus64_r62p1"):
+        api_case(ref, "boxtorus64_r62p1", pts, tris, 62, 1, full_sdf=False)
     manifest["boxtorus64_r62p1"] = "same mesh through the API, resolution 62, pad 1"
 
     pts, tris = W.subdivided_cube(3)
-    grid_case(ref, "cube3_facegrid", pts, tris, [-4.5 / 12, -4.5 / 12, -4.5 / 12], 1.0 / 12, (20, 20, 20))
+    if want("cube3_facegrid"):
+        grid_case(ref, "cube3_facegrid", pts, tris, [-4.5 / 12, -4.5 / 12, -4.5 / 12], 1.0 / 12, (20, 20, 20))
     manifest["cube3_facegrid"] = "subdivided_cube(3) on a 20^3 grid, h=1/12, centres on faces and shared edges"
 
-    pred_case(ref, "predicates", 4096, seed=21)
+    if want("predicates"):
+        pred_case(ref, "predicates", 4096, seed=21)
     manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
 
-    with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
+    with open(path, "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
 

@@ -131,3 +131,19 @@ def test_getters_tolerate_null(lib):
     assert nx.value == 0 and lib.cmg_voxels_spacing(None) == 0.0
     assert not lib.cmg_voxels_occupancy(None) and not lib.cmg_voxels_distance(None)
     assert lib.cmg_version() == b"0.5.0"
+
+
+def test_bulk_triangles_equal_single_facets(lib):
+    """cmg_plc_add_triangles appends the same facets as one cmg_plc_add_facet call
+    per triangle (same fan triangulation readback), after any earlier polygon."""
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import workloads as W
+    pts, tris = W.icosphere(2)
+    quad = [0, 1, 2, 3]
+    a = cm.PLC().add_points(pts).add_facet(quad)
+    for t in tris:
+        a.add_facet(t)
+    b = cm.PLC().add_points(pts).add_facet(quad).add_facets(tris)
+    assert len(a.triangles) == len(b.triangles) == len(tris) + 2
+    assert np.array_equal(a.triangles, b.triangles)
+    assert np.array_equal(b.triangles[2:], tris)
