@@ -180,7 +180,7 @@ def fraction_of_peak(work_flops, ms, peak):
 
 def traffic_from_profile():
     """DRAM bytes per launch of the evaluation kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_sdf_mixed_shsphere256.md")
+    path = os.path.join(ROOT, "profiles", "k_sdf_sub_mixed_shsphere256.md")
     try:
         with open(path) as f:
             for line in f:
@@ -283,14 +283,14 @@ def run_ours(args):
         ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
         ach64, frac64 = fraction_of_peak(w_sdf, tp["eval_ms"], p64)
         line["roofline"] = {
-            "bound": "fp32", "kernel": "k_sdf_mixed (distance evaluation)",
+            "bound": "fp32", "kernel": "k_sdf_sub<mixed> (distance evaluation)",
             "achieved": ach / 1e12, "peak": p32 / 1e12, "unit": "TFLOP/s", "frac": frac,
             "traffic": traffic_from_profile(),
             "work": f"sum_v K(v) * {PT_FLOPS} = {w_sdf:.4g} flops per launch; K(v) = triangles whose "
                     f"bounding sphere reaches the cell's distance sphere",
             "peak_source": "measured FFMA microbenchmark on this GPU (no FP32 entry in MEASURED_PEAKS.json)",
             "eval_ms": tm["eval_ms"], "phase_ms": tm,
-            "fp64_kernel": {"kernel": "k_sdf_fp64", "achieved": ach64 / 1e12, "peak": p64 / 1e12,
+            "fp64_kernel": {"kernel": "k_sdf_sub<fp64>", "achieved": ach64 / 1e12, "peak": p64 / 1e12,
                             "frac": frac64, "eval_ms": tp["eval_ms"], "phase_ms": tp,
                             "peak_source": "measured DFMA microbenchmark (FMA = 2 flops)"}}
         line["mixed_vs_fp64"] = {"fp64_value": p_value, "speedup": value / world / p_value,
@@ -442,7 +442,7 @@ def run_batch(args):
         p32 = cm.peak_flops(False)
         w_sdf = wm["sum_k"] * PT_FLOPS
         ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
-        line["roofline"] = {"bound": "fp32", "kernel": "k_sdf_mixed (distance evaluation)",
+        line["roofline"] = {"bound": "fp32", "kernel": "k_sdf_sub<mixed> (distance evaluation)",
                             "achieved": ach / 1e12, "peak": p32 / 1e12, "unit": "TFLOP/s",
                             "frac": frac, "traffic": None, "eval_ms": tm["eval_ms"], "phase_ms": tm,
                             "work": f"sum_v K(v) * {PT_FLOPS} = {w_sdf:.4g} flops per launch",
