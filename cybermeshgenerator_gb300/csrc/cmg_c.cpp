@@ -720,7 +720,8 @@ cmg_status cmg_sdf_plan_backward(cmg_sdf_plan* p, const double* d_points,
         std::lock_guard<std::mutex> lk(gpu_mutex());
         cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
         const double* pts = d_points ? d_points : p->batch->d_points();
-        cmg::gpu::adjoint_backward(p->g, p->ncell, pts, p->npts, p->batch->d_tris(), p->ntris,
+        cmg::gpu::adjoint_backward(p->batch->opts().precision, p->g, p->ncell, pts, p->npts,
+                                   p->batch->d_tris(), p->ntris,
                                    d_nearest_triangle, d_nearest_region, d_occupancy, d_grad_sdf,
                                    p->voff, p->vinc, d_grad_points, p->tmp, st);
     });

@@ -66,14 +66,17 @@ void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, in
                     cudaStream_t st);
 
 // adjoint.cu: dL/d(points) of the signed distance from the nearest-feature
-// checkpoint. voff (npts+1) / vinc: per point, its (3 * triangle + corner) entries in
-// ascending order. grad (3*npts doubles) is overwritten; tmp holds
-// adjoint_tmp_bytes(ncell, ntris).
+// checkpoint, per-cell terms in FP64 (kPrecFP64) or FP32 on triangle-recentred
+// coordinates (kPrecMixed), sums in FP64 in a fixed order. voff (npts+1) / vinc: per
+// point, its (3 * triangle + corner) entries in ascending order. grad (3*npts
+// doubles) is overwritten; tmp holds adjoint_tmp_bytes(ncell, ntris). Synchronises
+// the stream once (the number of runs sizes the sort).
 size_t adjoint_tmp_bytes(int64_t ncell, int64_t ntris);
-void adjoint_backward(const GridDesc& g, int64_t ncell, const double* pts, int64_t npts,
-                      const int* tris, int64_t ntris, const int* near_tri, const uint8_t* near_reg,
-                      const uint8_t* occ, const double* grad_sdf, const int64_t* voff,
-                      const int* vinc, double* grad, void* tmp, cudaStream_t st);
+void adjoint_backward(int precision, const GridDesc& g, int64_t ncell, const double* pts,
+                      int64_t npts, const int* tris, int64_t ntris, const int* near_tri,
+                      const uint8_t* near_reg, const uint8_t* occ, const double* grad_sdf,
+                      const int64_t* voff, const int* vinc, double* grad, void* tmp,
+                      cudaStream_t st);
 
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);

@@ -79,7 +79,7 @@ def _central_differences(plan, pts, verts, w, t, h):
     return full, kept, masks
 
 
-def test_adjoint_vs_central_differences(c3):
+def test_adjoint_vs_central_differences(c3, c3_mixed):
     """FP64 central differences (h = 1e-6) of the plain FP64 distance (bit-identical
     to the reference's) on 64 random vertices x 3 coordinates, relative 1e-5.
 
@@ -101,12 +101,17 @@ def test_adjoint_vs_central_differences(c3):
 
     full, kept, masks = _central_differences(plan, pts, verts, w, t, 1e-6)
     an_kept = np.zeros_like(kept)
+    an_kept32 = np.zeros_like(kept)  # the FP32 adjoint, same checkpoint
     for i, vv in enumerate(verts):
         for a in range(3):
             g = gs.clone()
             g[torch.from_numpy(masks[i][a]).to("cuda")] = 0.0
             an_kept[i, a] = plan.backward(v, occ, tri, reg, g)[vv, a].item()
+            an_kept32[i, a] = c3_mixed.backward(v, occ, tri, reg, g)[vv, a].item()
     rel_kept = np.linalg.norm(kept - an_kept) / np.linalg.norm(an_kept)
+    rel_kept32 = np.linalg.norm(kept - an_kept32) / np.linalg.norm(an_kept32)
+    print(f"h=1e-6, FP32 adjoint: relative error {rel_kept32:.2e}")
+    assert rel_kept32 <= 1e-5, rel_kept32
     rel_full = np.linalg.norm(full - grad[verts]) / np.linalg.norm(grad[verts])
     print(f"h=1e-6: relative error {rel_kept:.2e} without the "
           f"{sum(int(m.sum()) for r in masks for m in r)} switching cells, "
@@ -154,17 +159,33 @@ def test_autograd_function(c3):
     _forward(plan, pts)
 
 
-def test_mixed_precision_forward_gradient(c3, cm):
-    """The checkpoint of a mixed-precision forward gives nearly the same gradient."""
+@pytest.fixture(scope="module")
+def c3_mixed(c3, cm):
     from cybermeshgenerator_gb300 import torch_sdf as TS
     pm = TS.SDFPlan(c3["pts"], c3["tris"], c3["grid"], precision=cm.PREC_MIXED)
+    yield pm
+    pm.close()
+
+
+def test_mixed_precision_forward_gradient(c3, c3_mixed):
+    """A mixed-precision plan: its forward within 1e-6 of the bbox diagonal, its
+    FP32 adjoint within 1e-5 of the FP64 adjoint on the same checkpoint, and its own
+    checkpoint giving nearly the same gradient."""
+    pm = c3_mixed
     gm, (sm, _, _, _) = _grad(pm, c3["pts"], c3["w"], c3["t"])
-    g64, (s64, _, _, _) = _grad(c3["plan"], c3["pts"], c3["w"], c3["t"])
+    g64, (s64, occ, tri, reg) = _grad(c3["plan"], c3["pts"], c3["w"], c3["t"])
     diag = float(np.linalg.norm(c3["pts"].max(0) - c3["pts"].min(0)))
     assert (sm - s64).abs().max().item() <= 1e-6 * diag
-    a, b = gm.cpu().numpy(), g64.cpu().numpy()
+    v = torch.tensor(c3["pts"], device="cuda")
+    gs = 2.0 * torch.tensor(c3["w"], device="cuda") * (s64 - torch.tensor(c3["t"], device="cuda"))
+    g32 = pm.backward(v, occ, tri, reg, gs).cpu().numpy()
+    b = g64.cpu().numpy()
+    rel = np.linalg.norm(g32 - b) / np.linalg.norm(b)
+    print(f"FP32 adjoint vs FP64 adjoint, same checkpoint: {rel:.2e}")
+    assert rel <= 1e-5
+    assert torch.equal(pm.backward(v, occ, tri, reg, gs), pm.backward(v, occ, tri, reg, gs))
+    a = gm.cpu().numpy()
     assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b)
-    pm.close()
 
 
 def test_plan_moves_points_and_resizes(c3, cm, orc):
