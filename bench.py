@@ -232,7 +232,7 @@ def run_ours(args):
     plc = cm.PLC.from_arrays(pts, tris)
     outs = cm.OUT_OCCUPANCY | cm.OUT_SDF_F32
     mixed = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_MIXED, band=1.0,
-                     brick=args.brick)
+                     brick=args.brick, stage=args.stage)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     mixed.run().sync()  # sizing pass
     cells = mixed.cells
@@ -307,7 +307,8 @@ def run_ours(args):
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             r = cm.voxelize_ex(plc, resolution=RESOLUTION, pad=PAD, outputs=outs,
-                               precision=cm.PREC_MIXED, band=1.0, brick=args.brick)
+                               precision=cm.PREC_MIXED, band=1.0, brick=args.brick,
+                               stage=args.stage)
             if i >= args.warmup:
                 e2e_t.append(time.perf_counter() - t0)
         line["e2e"] = {"value": cells / (sum(e2e_t) / len(e2e_t)), "unit": UNIT,
@@ -387,6 +388,7 @@ def _events_time(torch, stream, fn, steps, warmup, flush=None):
 BATCH_METRIC = "voxel-queries/s, batch of 512 meshes (80-131k tris, 32^3-192^3): occupancy + mixed SDF"
 SCALE_METRIC = "voxel-queries/s, 512^3 grid/2.56M tris: occupancy + mixed SDF + adjoint"
 STREAM_METRIC = "predicate queries/s, 1e8 orient3d + 1e8 insphere (10% degenerate), reference semantics"
+STREAM_NEAR = 0.1  # the harder mix reported beside: another 10 % within a few ulps of a tie
 
 
 def _batch_workload():
@@ -592,14 +594,15 @@ STREAM_N = 100_000_000
 STREAM_CHUNK = 10_000_000
 
 
-def _stream_soa(kind, n, seed):
-    """n queries built in chunks (bounded host memory for the generator)."""
+def _stream_soa(kind, n, seed, near=0.0):
+    """n queries built in chunks (bounded host memory for the generator): 10 %
+    exactly degenerate, `near` within a few ulps of a tie, the rest uniform."""
     from cybermeshgenerator_gb300 import workloads as W
     rows = 12 if kind == "orient3d" else 15
     out = np.empty((rows, n), dtype=np.float64)
     for c0 in range(0, n, STREAM_CHUNK):
         m = min(STREAM_CHUNK, n - c0)
-        out[:, c0:c0 + m] = W.predicate_stream(m, kind, degenerate=0.1, near=0.1,
+        out[:, c0:c0 + m] = W.predicate_stream(m, kind, degenerate=0.1, near=near,
                                                seed=seed + c0 // STREAM_CHUNK)
     return out
 
@@ -639,9 +642,9 @@ def run_stream(args):
     q = 2 * n
     value = q * world * args.steps / (total_ms * 1e-3)
     config = {"workload": f"{n} orient3d + {n} insphere queries, SoA float64 in HBM, 10% exactly "
-                          "coplanar/cospherical (small integers scaled by powers of two), 10% within "
-                          "a few ulps of that, the rest uniform in [0,1)^3; reference semantics "
-                          "(rounded determinant's sign unless exactly zero)",
+                          "coplanar/cospherical (small integers scaled by powers of two), the rest "
+                          "uniform in [0,1)^3; reference semantics (rounded determinant's sign "
+                          "unless exactly zero)",
               "queries": q, "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
     line = _base_line(STREAM_METRIC, "queries/s", value, world, args, total_ms, "fp32+fp64+exact",
                       config, launches, clk.summary())
@@ -662,6 +665,24 @@ def run_stream(args):
             want = orc.stream(kind, np.ascontiguousarray(host[kind][:, idx]), oracle.COMPAT)
             ok = ok and bool(np.array_equal(outs[kind].cpu().numpy()[idx], want))
         line["sample_parity"] = {"queries": 400_000, "equal": ok}
+        # the harder mix: the same plus 10 % of queries within a few ulps of a tie
+        # (the first 2e7 of each kind, replaced in place and restored afterwards)
+        m = 2 * STREAM_CHUNK
+        hard_stats, hard_ms = {}, 0.0
+        for kind, fn, seed in (("orient3d", cm.orient3d_stream, 3000),
+                               ("insphere", cm.insphere_stream, 4000)):
+            hs = torch.from_numpy(_stream_soa(kind, m, seed, near=STREAM_NEAR)).to("cuda")
+            keep = dev[kind][:, :m].clone()
+            dev[kind][:, :m] = hs
+            d = dev[kind]
+            call = lambda: fn(([d[k].data_ptr() for k in range(d.shape[0])], m,
+                               outs[kind].data_ptr()), cm.PRED_COMPAT, stream=sid)
+            t = _events_time(torch, stream, call, 2, 1)
+            hard_ms += sum(t) / len(t)
+            hard_stats[kind] = dict(call()[1])
+            dev[kind][:, :m] = keep
+        line["near_ties_mix"] = {"value": 2 * m / (hard_ms * 1e-3), "unit": "queries/s",
+                                 "queries": 2 * m, "near": STREAM_NEAR, "stats": hard_stats}
         hbm = _measured_hbm()
         byts = n * (96 + 1) + n * (120 + 1)
         t_step = total_ms / args.steps / world * 1e-3
@@ -768,6 +789,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--brick", type=int, default=0)
+    ap.add_argument("--stage", type=int, default=-1,
+                    help="mixed record access: 0 L1/L2, 1 staged in shared memory, -1 default")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="sdf", choices=["sdf", "batch", "scale", "stream"])

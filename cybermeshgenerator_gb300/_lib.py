@@ -65,7 +65,7 @@ class WorkModel(ctypes.Structure):
 
 class PredStats(ctypes.Structure):
     _fields_ = [("queries", ctypes.c_int64), ("fp64_queries", ctypes.c_int64),
-                ("exact_queries", ctypes.c_int64)]
+                ("exact_queries", ctypes.c_int64), ("expansion_queries", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -35,6 +35,74 @@ __device__ __forceinline__ void two_diff(double a, double b, double& x, double& 
     two_sum(a, -b, x, y);
 }
 
+// ---- exactness certificates
+// An FP64 evaluation whose every operation was exact gives the exact determinant.
+// Each step checks its own rounding: a subtraction or sum through its Two-Sum tail,
+// a product through its FMA residual (a nonzero product below 2^-960, or one that
+// underflowed to zero, is not trusted: its residual may not be representable).
+// Overflow produces a non-finite tail and fails the check.
+__device__ __forceinline__ double xsub(double a, double b, bool& ok) {
+    double x, y;
+    two_diff(a, b, x, y);
+    ok = ok && y == 0.0;
+    return x;
+}
+__device__ __forceinline__ double xadd(double a, double b, bool& ok) {
+    double x, y;
+    two_sum(a, b, x, y);
+    ok = ok && y == 0.0;
+    return x;
+}
+__device__ __forceinline__ double xmul(double a, double b, bool& ok) {
+    const double p = __dmul_rn(a, b);
+    const bool tiny = p != 0.0 ? fabs(p) < 0x1p-960 : (a != 0.0 && b != 0.0);
+    ok = ok && !tiny && __fma_rn(a, b, -p) == 0.0;
+    return p;
+}
+
+// orient3d(a, b, c, d) evaluated with exactness tracking; true when *det is exact.
+static __device__ __noinline__ bool orient3d_certified(const d3& a, const d3& b, const d3& c,
+                                                       const d3& d, double* det) {
+    bool ok = true;
+    const double adx = xsub(a.x, d.x, ok), ady = xsub(a.y, d.y, ok), adz = xsub(a.z, d.z, ok);
+    const double bdx = xsub(b.x, d.x, ok), bdy = xsub(b.y, d.y, ok), bdz = xsub(b.z, d.z, ok);
+    const double cdx = xsub(c.x, d.x, ok), cdy = xsub(c.y, d.y, ok), cdz = xsub(c.z, d.z, ok);
+    const double m1 = xsub(xmul(bdx, cdy, ok), xmul(cdx, bdy, ok), ok);
+    const double m2 = xsub(xmul(cdx, ady, ok), xmul(adx, cdy, ok), ok);
+    const double m3 = xsub(xmul(adx, bdy, ok), xmul(bdx, ady, ok), ok);
+    *det = xadd(xadd(xmul(adz, m1, ok), xmul(bdz, m2, ok), ok), xmul(cdz, m3, ok), ok);
+    return ok;
+}
+
+// insphere(a, b, c, d, e) (the lifted 4x4 form, e as origin) with exactness
+// tracking; true when *det is exact.
+static __device__ __noinline__ bool insphere_certified(const d3& a, const d3& b, const d3& c,
+                                                       const d3& d, const d3& e, double* det) {
+    bool ok = true;
+    const double aex = xsub(a.x, e.x, ok), aey = xsub(a.y, e.y, ok), aez = xsub(a.z, e.z, ok);
+    const double bex = xsub(b.x, e.x, ok), bey = xsub(b.y, e.y, ok), bez = xsub(b.z, e.z, ok);
+    const double cex = xsub(c.x, e.x, ok), cey = xsub(c.y, e.y, ok), cez = xsub(c.z, e.z, ok);
+    const double dex = xsub(d.x, e.x, ok), dey = xsub(d.y, e.y, ok), dez = xsub(d.z, e.z, ok);
+    if (!ok) return false;
+    const double ab = xsub(xmul(aex, bey, ok), xmul(bex, aey, ok), ok);
+    const double bc = xsub(xmul(bex, cey, ok), xmul(cex, bey, ok), ok);
+    const double cd = xsub(xmul(cex, dey, ok), xmul(dex, cey, ok), ok);
+    const double da = xsub(xmul(dex, aey, ok), xmul(aex, dey, ok), ok);
+    const double ac = xsub(xmul(aex, cey, ok), xmul(cex, aey, ok), ok);
+    const double bd = xsub(xmul(bex, dey, ok), xmul(dex, bey, ok), ok);
+    const double abc = xadd(xsub(xmul(aez, bc, ok), xmul(bez, ac, ok), ok), xmul(cez, ab, ok), ok);
+    const double bcd = xadd(xsub(xmul(bez, cd, ok), xmul(cez, bd, ok), ok), xmul(dez, bc, ok), ok);
+    const double cda = xadd(xadd(xmul(cez, da, ok), xmul(dez, ac, ok), ok), xmul(aez, cd, ok), ok);
+    const double dab = xadd(xadd(xmul(dez, ab, ok), xmul(aez, bd, ok), ok), xmul(bez, da, ok), ok);
+    const double al = xadd(xadd(xmul(aex, aex, ok), xmul(aey, aey, ok), ok), xmul(aez, aez, ok), ok);
+    const double bl = xadd(xadd(xmul(bex, bex, ok), xmul(bey, bey, ok), ok), xmul(bez, bez, ok), ok);
+    const double cl = xadd(xadd(xmul(cex, cex, ok), xmul(cey, cey, ok), ok), xmul(cez, cez, ok), ok);
+    const double dl = xadd(xadd(xmul(dex, dex, ok), xmul(dey, dey, ok), ok), xmul(dez, dez, ok), ok);
+    *det = xadd(xsub(xmul(dl, abc, ok), xmul(cl, dab, ok), ok),
+                xsub(xmul(bl, cda, ok), xmul(al, bcd, ok), ok), ok);
+    return ok;
+}
+
 // h = e + f: merge by magnitude, then a Two-Sum sweep, zero-eliminated.
 // h holds elen + flen doubles and may not alias e or f.
 static __device__ __noinline__ int sum(int elen, const double* e, int flen, const double* f,
@@ -152,6 +220,10 @@ static __device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b
 
 // Exact sign of orient3d(a, b, c, d).
 static __device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c, const d3& d) {
+    {
+        double det;
+        if (orient3d_certified(a, b, c, d, &det)) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+    }
     double adx, ady, adz, bdx, bdy, bdz, cdx, cdy, cdz;
     double t0, t1, t2, t3, t4, t5, t6, t7, t8;
     two_diff(a.x, d.x, adx, t0);
@@ -208,6 +280,10 @@ constexpr int kInsphereCap = 256;
 // capacity is exceeded (the sign is then 0 and must not be trusted).
 static __device__ __noinline__ int insphere_sign(const d3& a, const d3& b, const d3& c, const d3& d,
                                           const d3& e, int* overflow) {
+    {
+        double det;
+        if (insphere_certified(a, b, c, d, e, &det)) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+    }
     double acc[kInsphereCap], work[kInsphereCap + 192];
     int nacc = 1;
     acc[0] = 0.0;

@@ -14,7 +14,9 @@
 //                 certifies is the exact sign and also the sign of the FP64 rounded
 //                 determinant, so it serves both modes;
 //   k_pred_fp64   the reference's rounded determinant (and, in EXACT mode, its
-//                 permanent bound);
+//                 permanent bound); when that does not decide, an evaluation with
+//                 exactness tracking (cmg_exact.cuh): if no operation rounded, its
+//                 value is the exact determinant;
 //   k_pred_exact  expansion arithmetic (cmg_exact.cuh).
 #include <cuda_runtime.h>
 
@@ -147,13 +149,14 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
                                                         const unsigned long long* __restrict__ nin,
                                                         int8_t* __restrict__ out,
                                                         int64_t* __restrict__ list,
-                                                        unsigned long long* __restrict__ count) {
+                                                        unsigned long long* __restrict__ count,
+                                                        unsigned long long* __restrict__ ncert) {
     const int64_t n = static_cast<int64_t>(*nin);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     const int64_t n_round = (n + 31) & ~int64_t(31);
     for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n_round;
          k += stride) {
-        bool undecided = false;
+        bool undecided = false, certified = false;
         int64_t i = 0;
         if (k < n) {
             i = in[k];
@@ -169,10 +172,24 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
                 det = isp_fast(a, b, c, d, e, MODE == kPredExact ? &perm : nullptr);
                 perm *= kIspErrA;
             }
-            const bool decided = MODE == kPredCompat ? det != 0.0 : (det > perm || -det > perm);
-            if (decided) out[i] = static_cast<int8_t>(sgn(det));
+            bool decided = MODE == kPredCompat ? det != 0.0 : (det > perm || -det > perm);
+            if (decided) {
+                out[i] = static_cast<int8_t>(sgn(det));
+            } else {
+                // an evaluation in which no operation rounded is the exact determinant
+                double ex;
+                const bool cert = NPT == 4 ? exact::orient3d_certified(a, b, c, d, &ex)
+                                           : exact::insphere_certified(a, b, c, d,
+                                                                       {v[12], v[13], v[14]}, &ex);
+                if (cert) {
+                    out[i] = static_cast<int8_t>(sgn(ex));
+                    decided = certified = true;
+                }
+            }
             undecided = !decided;
         }
+        const unsigned cm = __ballot_sync(0xffffffffu, certified);
+        if (cm && (threadIdx.x & 31) == 0) atomicAdd(ncert, static_cast<unsigned long long>(__popc(cm)));
         push(undecided, i, list, count);
     }
 }
@@ -233,7 +250,7 @@ struct Counters {
     unsigned long long n32;  // left by the FP32 pass
     unsigned long long n64;  // left by the FP64 pass
     unsigned long long overflow;
-    unsigned long long pad;
+    unsigned long long certified;  // decided in the FP64 pass by an exact evaluation
 };
 
 }  // namespace
@@ -251,13 +268,17 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
     else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, n, d_out, list_a, &c->n32);
     CMG_LAUNCH();
     if (npt == 4 && mode == kPredExact)
-        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
     else if (npt == 4)
-        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
     else if (mode == kPredExact)
-        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
     else
-        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64);
+        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
     CMG_LAUNCH();
     if (npt == 4) k_pred_exact<4><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
     else k_pred_exact<5><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
@@ -330,7 +351,8 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
         if (stats) {
             stats->queries = n;
             stats->fp64_queries = static_cast<int64_t>(hc.n32);
-            stats->exact_queries = static_cast<int64_t>(hc.n64);
+            stats->exact_queries = static_cast<int64_t>(hc.n64 + hc.certified);
+            stats->expansion_queries = static_cast<int64_t>(hc.n64);
         }
         if (hc.overflow) {
             set_err(errbuf, len, "insphere: exact expansion exceeded its capacity");

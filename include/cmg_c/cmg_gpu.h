@@ -201,8 +201,10 @@ void cmg_sdf_plan_destroy(cmg_sdf_plan*);
 
 typedef struct cmg_pred_stats {
     int64_t queries;
-    int64_t fp64_queries;  /* not certified by the FP32 filter */
-    int64_t exact_queries; /* resolved in exact arithmetic */
+    int64_t fp64_queries;      /* not certified by the FP32 filter */
+    int64_t exact_queries;     /* resolved in exact arithmetic (an FP64 evaluation in
+                                  which no operation rounded, or expansions) */
+    int64_t expansion_queries; /* of which needed expansion arithmetic */
 } cmg_pred_stats;
 
 /* Signs (-1, 0, +1) of n orient3d(a,b,c,d) queries given as 12 SoA coordinate

@@ -118,3 +118,16 @@ def test_nearest_triangle_checkpoint(cm, golden, orc):
         t = r.nearest_triangle[v]
         d, rg = orc.point_tri_dist2(p, *pts[T[t]])
         assert d == d2[v] and rg == r.nearest_region[v]
+
+
+@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "shsphere64_r30p1", "boxtorus64_facegrid"])
+def test_mixed_record_access_modes_identical(cm, golden, name):
+    """Reading records from L1/L2 or staging them in shared memory evaluates the
+    same candidates in the same order: identical outputs."""
+    g = golden(name)
+    outs = cm.OUT_SDF_F64 | cm.OUT_NEAREST
+    r = [_run(cm, g, name, outputs=outs, precision=cm.PREC_MIXED, stage=m) for m in (0, 1)]
+    for x in r[1:]:
+        assert np.array_equal(x.sdf64.view(np.uint64), r[0].sdf64.view(np.uint64))
+        assert np.array_equal(x.nearest_triangle, r[0].nearest_triangle)
+        assert np.array_equal(x.nearest_region, r[0].nearest_region)
