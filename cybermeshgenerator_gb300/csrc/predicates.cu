@@ -72,21 +72,11 @@ __device__ __forceinline__ int o3d_fp32(const double* v) {
     return det > bound ? 1 : (det < -bound ? -1 : 0);
 }
 
-// FP32 insphere, same scheme: the lifted 4x4 determinant (four lift x minor
-// products) errs by at most ~4.8e4 u A^5 to first order for inputs rounded to
-// FP32; 2^17 u A^5 is used, plus the reference's FP64 bound isperrboundA *
-// permanent <= 1.8e-15 * 2304 A^5.
-__device__ __forceinline__ int isp_fp32(const double* v) {
-    float f[15];
-#pragma unroll
-    for (int i = 0; i < 15; ++i) f[i] = __double2float_rn(v[i]);
-    float A = 0.f;
-#pragma unroll
-    for (int i = 0; i < 15; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
-    const float aex = f[0] - f[12], aey = f[1] - f[13], aez = f[2] - f[14];
-    const float bex = f[3] - f[12], bey = f[4] - f[13], bez = f[5] - f[14];
-    const float cex = f[6] - f[12], cey = f[7] - f[13], cez = f[8] - f[14];
-    const float dex = f[9] - f[12], dey = f[10] - f[13], dez = f[11] - f[14];
+// The lifted insphere determinant (e as origin) of 12 differences, and the same
+// expression over absolute values (every monomial counted with its magnitude).
+__device__ __forceinline__ float isp_lifted(const float* x) {
+    const float aex = x[0], aey = x[1], aez = x[2], bex = x[3], bey = x[4], bez = x[5];
+    const float cex = x[6], cey = x[7], cez = x[8], dex = x[9], dey = x[10], dez = x[11];
     const float ab = aex * bey - bex * aey, bc = bex * cey - cex * bey;
     const float cd = cex * dey - dex * cey, da = dex * aey - aex * dey;
     const float ac = aex * cey - cex * aey, bd = bex * dey - dex * bey;
@@ -98,11 +88,60 @@ __device__ __forceinline__ int isp_fp32(const double* v) {
     const float bl = bex * bex + bey * bey + bez * bez;
     const float cl = cex * cex + cey * cey + cez * cez;
     const float dl = dex * dex + dey * dey + dez * dez;
-    const float det = (dl * abc - cl * dab) + (bl * cda - al * bcd);
-    const float A2 = A * A;
-    const float A5 = A2 * A2 * A * (1.f + 16.f * kU);
-    const float bound = 131072.f * kU * A5 + 6e-12f * A5 + 1e-36f;
-    if (!(A5 < 1e30f)) return 0;
+    return (dl * abc - cl * dab) + (bl * cda - al * bcd);
+}
+__device__ __forceinline__ float isp_absolute(const float* x) {  // x >= 0
+    const float aex = x[0], aey = x[1], aez = x[2], bex = x[3], bey = x[4], bez = x[5];
+    const float cex = x[6], cey = x[7], cez = x[8], dex = x[9], dey = x[10], dez = x[11];
+    const float ab = aex * bey + bex * aey, bc = bex * cey + cex * bey;
+    const float cd = cex * dey + dex * cey, da = dex * aey + aex * dey;
+    const float ac = aex * cey + cex * aey, bd = bex * dey + dex * bey;
+    const float abc = aez * bc + bez * ac + cez * ab;
+    const float bcd = bez * cd + cez * bd + dez * bc;
+    const float cda = cez * da + dez * ac + aez * cd;
+    const float dab = dez * ab + aez * bd + bez * da;
+    const float al = aex * aex + aey * aey + aez * aez;
+    const float bl = bex * bex + bey * bey + bez * bez;
+    const float cl = cex * cex + cey * cey + cez * cez;
+    const float dl = dex * dex + dey * dey + dez * dez;
+    return (dl * abc + cl * dab) + (bl * cda + al * bcd);
+}
+
+// FP32 insphere with a permanent-style bound. Inputs rounded to FP32 (|f - v| <= u|v|)
+// and differences D = fl(f_a - f_e) satisfy |D - d| <= 1.01 u |D| + 2.01 u A
+// (A = max |f|). The lifted determinant is a sum of degree-5 monomials, so
+//   |det(D) - det(d)| <= P(|D| + |D - d|) - P(|D|) <= P2 - P1,
+// P the absolute-value polynomial, P1 = P(|D|), P2 = P(|D| (1 + 1.01 u) + 2.01 u A)
+// (entries inflated once more by 4 u for their own rounding); the FP32 evaluation
+// of det(D) (at most eight roundings deep) errs by at most 8.1 u P(|D|); P1 and P2
+// are themselves computed in FP32 (relative error <= 9 u each). Bound:
+//   (P2 - P1) + 20 u (P1 + P2) + 1e-36,
+// which also covers the reference's FP64 bound isperrboundA * permanent (~16e-16
+// relative): a certified sign is exact and is the sign of the FP64 rounded
+// determinant. The additive term covers FP32 underflow (< 1e-43 over the whole
+// evaluation); no certificate on overflow or when A < 1e-30.
+__device__ __forceinline__ int isp_fp32(const double* v) {
+    float f[15];
+#pragma unroll
+    for (int i = 0; i < 15; ++i) f[i] = __double2float_rn(v[i]);
+    float A = 0.f;
+#pragma unroll
+    for (int i = 0; i < 15; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
+    float D[12], X[12], Y[12];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) D[3 * k + q] = f[3 * k + q] - f[12 + q];
+    const float eta = 2.01f * kU * A * (1.f + 4.f * kU);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        X[i] = fabsf(D[i]);
+        Y[i] = (X[i] * (1.f + 1.01f * kU) + eta) * (1.f + 4.f * kU);
+    }
+    const float det = isp_lifted(D);
+    const float p1 = isp_absolute(X), p2 = isp_absolute(Y);
+    if (!(p2 < 1e30f) || !(A >= 1e-30f)) return 0;  // overflow, non-finite or tiny
+    const float bound = (p2 - p1) + 20.f * kU * (p1 + p2) + 1e-36f;
     return det > bound ? 1 : (det < -bound ? -1 : 0);
 }
 
