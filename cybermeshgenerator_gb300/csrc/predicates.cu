@@ -47,17 +47,34 @@ __device__ __forceinline__ float amax3(float a, float b, float c) {
     return fmaxf(fabsf(a), fmaxf(fabsf(b), fabsf(c)));
 }
 
+// FP64 -> FP32 by truncating the significand, on the integer pipe (the hardware
+// conversion is far slower on this part): |f - x| < 2^-23 |x|. Zero maps to zero;
+// values outside the FP32 normal range, subnormals, infinities and NaN set ok = false.
+__device__ __forceinline__ float trunc32(double x, bool& ok) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+    const int e = static_cast<int>((hi >> 20) & 0x7ffu) - 1023 + 127;
+    const bool zero = (b << 1) == 0ull;
+    ok = ok && (zero || (e >= 1 && e <= 254));
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned bits = (hi & 0x80000000u) | (zero ? 0u : ((static_cast<unsigned>(e) << 23) | m));
+    return __uint_as_float(bits);
+}
+
 // FP32 orient3d: certified sign (+1/-1) or 0 when the bound does not decide.
-// Differences of inputs rounded to FP32 are off by at most eta = 4 u A (A the
-// largest magnitude among the coordinates, |difference| <= 2A); the determinant
-// (three minor x coordinate terms, two sums) then errs by at most 512 u A^3 to
-// first order; 1024 u A^3 is used. The reference's FP64 bound o3derrboundA * permanent is at
-// most 7.8e-16 * 48 A^3 and is added, so a certified sign is the sign of the
-// FP64 rounded determinant as well.
+// Inputs truncated to FP32 are off by less than 2 u |v|, so the FP32 differences
+// (|difference| <= 2A, A the largest magnitude) are off by at most eta = 6 u A; the
+// determinant (six products of three differences, at most five roundings deep) then
+// errs by at most 72 eta A^2 + 5 u 48 A^3 = 672 u A^3 to first order; 1024 u A^3 is
+// used. The reference's FP64 bound o3derrboundA * permanent is at most
+// 7.8e-16 * 48 A^3 and is added, so a certified sign is the sign of the FP64 rounded
+// determinant as well.
 __device__ __forceinline__ int o3d_fp32(const double* v) {
     float f[12];
+    bool ok = true;
 #pragma unroll
-    for (int i = 0; i < 12; ++i) f[i] = __double2float_rn(v[i]);
+    for (int i = 0; i < 12; ++i) f[i] = trunc32(v[i], ok);
+    if (!ok) return 0;
     float A = 0.f;
 #pragma unroll
     for (int i = 0; i < 12; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
@@ -107,11 +124,11 @@ __device__ __forceinline__ float isp_absolute(const float* x) {  // x >= 0
     return (dl * abc + cl * dab) + (bl * cda + al * bcd);
 }
 
-// FP32 insphere with a permanent-style bound. Inputs rounded to FP32 (|f - v| <= u|v|)
-// and differences D = fl(f_a - f_e) satisfy |D - d| <= 1.01 u |D| + 2.01 u A
-// (A = max |f|). The lifted determinant is a sum of degree-5 monomials, so
+// FP32 insphere with a permanent-style bound. Inputs truncated to FP32
+// (|f - v| < 2 u |v|) and differences D = fl(f_a - f_e) satisfy
+// |D - d| <= 1.01 u |D| + 4.02 u A (A = max |f|). The lifted determinant is a sum of degree-5 monomials, so
 //   |det(D) - det(d)| <= P(|D| + |D - d|) - P(|D|) <= P2 - P1,
-// P the absolute-value polynomial, P1 = P(|D|), P2 = P(|D| (1 + 1.01 u) + 2.01 u A)
+// P the absolute-value polynomial, P1 = P(|D|), P2 = P(|D| (1 + 1.01 u) + 4.02 u A)
 // (entries inflated once more by 4 u for their own rounding); the FP32 evaluation
 // of det(D) (at most eight roundings deep) errs by at most 8.1 u P(|D|); P1 and P2
 // are themselves computed in FP32 (relative error <= 9 u each). Bound:
@@ -122,8 +139,10 @@ __device__ __forceinline__ float isp_absolute(const float* x) {  // x >= 0
 // evaluation); no certificate on overflow or when A < 1e-30.
 __device__ __forceinline__ int isp_fp32(const double* v) {
     float f[15];
+    bool ok = true;
 #pragma unroll
-    for (int i = 0; i < 15; ++i) f[i] = __double2float_rn(v[i]);
+    for (int i = 0; i < 15; ++i) f[i] = trunc32(v[i], ok);
+    if (!ok) return 0;
     float A = 0.f;
 #pragma unroll
     for (int i = 0; i < 15; i += 3) A = fmaxf(A, amax3(f[i], f[i + 1], f[i + 2]));
@@ -132,7 +151,7 @@ __device__ __forceinline__ int isp_fp32(const double* v) {
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int q = 0; q < 3; ++q) D[3 * k + q] = f[3 * k + q] - f[12 + q];
-    const float eta = 2.01f * kU * A * (1.f + 4.f * kU);
+    const float eta = 4.02f * kU * A * (1.f + 4.f * kU);
 #pragma unroll
     for (int i = 0; i < 12; ++i) {
         X[i] = fabsf(D[i]);
