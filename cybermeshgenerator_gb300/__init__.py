@@ -231,7 +231,31 @@ def make_opts(resolution: int = 64, pad: int = 1, outputs: int = OUT_OCCUPANCY,
     return o
 
 
-def _result_from_handle(h) -> VoxelResult:
+class _Owner:
+    """Owns a cmg_voxels handle; destroys it when no array views its buffers."""
+
+    def __init__(self, h) -> None:
+        self.h = h
+
+    def __del__(self) -> None:
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            _clib.cmg_voxels_destroy(h)
+
+
+class _View:
+    """Array interface over one buffer of an owned handle (keeps the owner alive)."""
+
+    def __init__(self, owner: _Owner, ptr: int, n: int, dtype) -> None:
+        self._owner = owner
+        self.__array_interface__ = {"shape": (n,), "typestr": np.dtype(dtype).str,
+                                    "data": (ptr, False), "version": 3}
+
+
+def _result_from_handle(h, owner: Optional[_Owner] = None) -> VoxelResult:
+    """The grid behind handle h. With an owner, the arrays view the handle's
+    buffers (no copy) and the handle lives as long as they do; without, they are
+    copies."""
     dims, origin, spacing = _geometry(h)
     cx, cy, cz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     _clib.cmg_voxels_corner(h, ctypes.byref(cx), ctypes.byref(cy), ctypes.byref(cz))
@@ -239,7 +263,11 @@ def _result_from_handle(h) -> VoxelResult:
 
     def grab(fn, dtype):
         p = fn(h)
-        return np.ctypeslib.as_array(p, (n,)).astype(dtype).copy() if p else None
+        if not p:
+            return None
+        if owner is not None:
+            return np.asarray(_View(owner, ctypes.cast(p, ctypes.c_void_p).value, n, dtype))
+        return np.ctypeslib.as_array(p, (n,)).astype(dtype, copy=True)
 
     st = _L.VoxelStats()
     _clib.cmg_voxels_stats(h, ctypes.byref(st))
@@ -262,10 +290,7 @@ def voxelize_ex(plc: PLC, **kw) -> VoxelResult:
     out = ctypes.c_void_p()
     err = ctypes.create_string_buffer(512)
     _check(_clib.cmg_plc_voxelize_ex(plc._handle, ctypes.byref(o), ctypes.byref(out), err, 512), err)
-    try:
-        return _result_from_handle(out.value)
-    finally:
-        _clib.cmg_voxels_destroy(out.value)
+    return _result_from_handle(out.value, _Owner(out.value))
 
 
 class Batch:
@@ -307,10 +332,7 @@ class Batch:
         out = ctypes.c_void_p()
         err = ctypes.create_string_buffer(512)
         _check(_clib.cmg_batch_get(self._h, int(i), ctypes.byref(out), err, 512), err)
-        try:
-            return _result_from_handle(out.value)
-        finally:
-            _clib.cmg_voxels_destroy(out.value)
+        return _result_from_handle(out.value, _Owner(out.value))
 
     @property
     def stream(self) -> int:

@@ -540,13 +540,10 @@ cmg_status cmg_batch_get(cmg_batch* b, int i, cmg_voxels** out, char* errbuf, si
     }
     return guarded(errbuf, len, [&] {
         std::lock_guard<std::mutex> lk(gpu_mutex());
-        std::vector<cmg::gpu::HostResult> res;
-        cmg::gpu::RunInfo ri;
-        b->batch->download(res, &ri);
         std::unique_ptr<cmg_voxels> v(new cmg_voxels);
         set_geometry(v.get(), b->grids[static_cast<size_t>(i)]);
-        v->r = std::move(res[static_cast<size_t>(i)]);
-        fill_stats(v.get(), ri);
+        b->batch->download_one(i, v->r);
+        fill_stats(v.get(), b->batch->info());
         v->stats.cells = static_cast<int64_t>(v->nx) * v->ny * v->nz;
         *out = v.release();
     });

@@ -470,26 +470,27 @@ RunInfo Batch::info() {
     return r;
 }
 
+void Batch::download_one(int m, HostResult& r) {
+    const MeshSeg& s = segs_[static_cast<size_t>(m)];
+    const int64_t n = static_cast<int64_t>(s.g.nx) * s.g.ny * s.g.nz;
+    auto get = [&](auto* dev, auto& vec) {
+        if (!dev) return;
+        vec.resize(static_cast<size_t>(n));
+        CMG_CUDA(cudaMemcpyAsync(vec.data(), dev + s.vox_begin, sizeof(vec[0]) * n,
+                                 cudaMemcpyDeviceToHost, stream_));
+    };
+    get(occ_, r.occ);
+    get(sdf32_, r.sdf32);
+    get(sdf64_, r.sdf64);
+    get(near_tri_, r.near_tri);
+    get(near_reg_, r.near_reg);
+    get(err_, r.err);
+    CMG_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void Batch::download(std::vector<HostResult>& out, RunInfo* info) {
     out.resize(segs_.size());
-    for (size_t m = 0; m < segs_.size(); ++m) {
-        const MeshSeg& s = segs_[m];
-        const int64_t n = static_cast<int64_t>(s.g.nx) * s.g.ny * s.g.nz;
-        HostResult& r = out[m];
-        auto get = [&](auto* dev, auto& vec) {
-            if (!dev) return;
-            vec.resize(static_cast<size_t>(n));
-            CMG_CUDA(cudaMemcpyAsync(vec.data(), dev + s.vox_begin, sizeof(vec[0]) * n,
-                                     cudaMemcpyDeviceToHost, stream_));
-        };
-        get(occ_, r.occ);
-        get(sdf32_, r.sdf32);
-        get(sdf64_, r.sdf64);
-        get(near_tri_, r.near_tri);
-        get(near_reg_, r.near_reg);
-        get(err_, r.err);
-    }
-    CMG_CUDA(cudaStreamSynchronize(stream_));
+    for (size_t m = 0; m < segs_.size(); ++m) download_one(static_cast<int>(m), out[m]);
     if (info) *info = this->info();
 }
 

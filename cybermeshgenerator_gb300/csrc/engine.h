@@ -47,13 +47,35 @@ struct HostMesh {
     GridDesc g{};
 };
 
+// Host array filled by a device copy: allocated without value-initialisation.
+template <typename T>
+class HostBuf {
+public:
+    void resize(size_t n) {
+        p_.reset(n ? new T[n] : nullptr);
+        n_ = n;
+    }
+    T* data() { return p_.get(); }
+    const T* data() const { return p_.get(); }
+    size_t size() const { return n_; }
+    bool empty() const { return n_ == 0; }
+    T& operator[](size_t i) { return p_[i]; }
+    const T& operator[](size_t i) const { return p_[i]; }
+    const T* begin() const { return p_.get(); }
+    const T* end() const { return p_.get() + n_; }
+
+private:
+    std::unique_ptr<T[]> p_;
+    size_t n_ = 0;
+};
+
 struct HostResult {
-    std::vector<uint8_t> occ;
-    std::vector<float> sdf32;
-    std::vector<double> sdf64;
-    std::vector<int> near_tri;
-    std::vector<uint8_t> near_reg;
-    std::vector<float> err;
+    HostBuf<uint8_t> occ;
+    HostBuf<float> sdf32;
+    HostBuf<double> sdf64;
+    HostBuf<int> near_tri;
+    HostBuf<uint8_t> near_reg;
+    HostBuf<float> err;
 };
 
 // Phase times of the last run(), from CUDA events on the batch's stream.
@@ -112,6 +134,8 @@ public:
     void set_stream(cudaStream_t st) { stream_ = st; }
     void synchronize();
     void download(std::vector<HostResult>& out, RunInfo* info);
+    // Mesh i's outputs only.
+    void download_one(int i, HostResult& out);
     RunInfo info();
     // Records CUDA events around the phases of each run() (not in graph replays).
     void set_timing(bool on) { timing_ = on; }
