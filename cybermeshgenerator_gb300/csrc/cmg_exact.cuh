@@ -103,6 +103,95 @@ static __device__ __noinline__ bool insphere_certified(const d3& a, const d3& b,
     return ok;
 }
 
+// ---- integer certificates
+// When every coordinate of a query is an integer multiple of one power of two 2^L
+// and |v| / 2^L < 2^B, the scaled coordinates are exact integers (int64) and the
+// determinant of their differences, evaluated in 128-bit integers, is exact; scaling
+// by 2^-L > 0 keeps its sign. B is chosen per predicate so that no intermediate can
+// overflow. Decomposition is on the integer pipe (the FP64 pipe is narrow here).
+__device__ __forceinline__ bool scale_to_ints(const double* v, int n, int B, long long* out) {
+    int lmin = 0x7fffffff, emax = -0x7fffffff;
+    for (int i = 0; i < n; ++i) {
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v[i]));
+        if ((b << 1) == 0ull) continue;  // +-0
+        const int ef = static_cast<int>((b >> 52) & 0x7ffull);
+        if (ef == 0 || ef == 0x7ff) return false;  // subnormal, infinite or NaN
+        const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+        const int e = ef - 1023;
+        const int lb = e - 52 + (__ffsll(static_cast<long long>(m)) - 1);
+        lmin = min(lmin, lb);
+        emax = max(emax, e);
+    }
+    if (lmin == 0x7fffffff) {  // all zero
+        for (int i = 0; i < n; ++i) out[i] = 0;
+        return true;
+    }
+    if (emax - lmin + 1 > B) return false;
+    for (int i = 0; i < n; ++i) {
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v[i]));
+        if ((b << 1) == 0ull) {
+            out[i] = 0;
+            continue;
+        }
+        const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+        const int tz = __ffsll(static_cast<long long>(m)) - 1;
+        const int lb = static_cast<int>((b >> 52) & 0x7ffull) - 1023 - 52 + tz;
+        const long long x = static_cast<long long>((m >> tz) << (lb - lmin));
+        out[i] = (b >> 63) ? -x : x;
+    }
+    return true;
+}
+
+// orient3d on integers: differences < 2^41, 2x2 minors < 2^83, terms < 2^124,
+// the sum of three < 2^126.
+__device__ __forceinline__ bool orient3d_int(const d3& a, const d3& b, const d3& c, const d3& d,
+                                             int* sign) {
+    const double v[12] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z};
+    long long X[12];
+    if (!scale_to_ints(v, 12, 40, X)) return false;
+    const long long adx = X[0] - X[9], ady = X[1] - X[10], adz = X[2] - X[11];
+    const long long bdx = X[3] - X[9], bdy = X[4] - X[10], bdz = X[5] - X[11];
+    const long long cdx = X[6] - X[9], cdy = X[7] - X[10], cdz = X[8] - X[11];
+    const __int128 m1 = static_cast<__int128>(bdx) * cdy - static_cast<__int128>(cdx) * bdy;
+    const __int128 m2 = static_cast<__int128>(cdx) * ady - static_cast<__int128>(adx) * cdy;
+    const __int128 m3 = static_cast<__int128>(adx) * bdy - static_cast<__int128>(bdx) * ady;
+    const __int128 det = adz * m1 + bdz * m2 + cdz * m3;
+    *sign = det > 0 ? 1 : (det < 0 ? -1 : 0);
+    return true;
+}
+
+// insphere (lifted 4x4, e as origin) on integers: differences < 2^23, 2x2 minors
+// < 2^47, 3x3 minors < 2^72, lifts < 2^48, terms < 2^120, the sum of four < 2^122.
+__device__ __forceinline__ bool insphere_int(const d3& a, const d3& b, const d3& c, const d3& d,
+                                             const d3& e, int* sign) {
+    const double v[15] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z,
+                          d.x, d.y, d.z, e.x, e.y, e.z};
+    long long X[15];
+    if (!scale_to_ints(v, 15, 22, X)) return false;
+    const long long aex = X[0] - X[12], aey = X[1] - X[13], aez = X[2] - X[14];
+    const long long bex = X[3] - X[12], bey = X[4] - X[13], bez = X[5] - X[14];
+    const long long cex = X[6] - X[12], cey = X[7] - X[13], cez = X[8] - X[14];
+    const long long dex = X[9] - X[12], dey = X[10] - X[13], dez = X[11] - X[14];
+    const long long ab = aex * bey - bex * aey, bc = bex * cey - cex * bey;
+    const long long cd = cex * dey - dex * cey, da = dex * aey - aex * dey;
+    const long long ac = aex * cey - cex * aey, bd = bex * dey - dex * bey;
+    const __int128 abc = static_cast<__int128>(aez) * bc - static_cast<__int128>(bez) * ac +
+                         static_cast<__int128>(cez) * ab;
+    const __int128 bcd = static_cast<__int128>(bez) * cd - static_cast<__int128>(cez) * bd +
+                         static_cast<__int128>(dez) * bc;
+    const __int128 cda = static_cast<__int128>(cez) * da + static_cast<__int128>(dez) * ac +
+                         static_cast<__int128>(aez) * cd;
+    const __int128 dab = static_cast<__int128>(dez) * ab + static_cast<__int128>(aez) * bd +
+                         static_cast<__int128>(bez) * da;
+    const long long al = aex * aex + aey * aey + aez * aez;
+    const long long bl = bex * bex + bey * bey + bez * bez;
+    const long long cl = cex * cex + cey * cey + cez * cez;
+    const long long dl = dex * dex + dey * dey + dez * dez;
+    const __int128 det = (dl * abc - cl * dab) + (bl * cda - al * bcd);
+    *sign = det > 0 ? 1 : (det < 0 ? -1 : 0);
+    return true;
+}
+
 // h = e + f: merge by magnitude, then a Two-Sum sweep, zero-eliminated.
 // h holds elen + flen doubles and may not alias e or f.
 static __device__ __noinline__ int sum(int elen, const double* e, int flen, const double* f,
@@ -221,6 +310,8 @@ static __device__ __noinline__ int orient3d_homogeneous(const d3& a, const d3& b
 // Exact sign of orient3d(a, b, c, d).
 static __device__ __noinline__ int orient3d_sign(const d3& a, const d3& b, const d3& c, const d3& d) {
     {
+        int sg;
+        if (orient3d_int(a, b, c, d, &sg)) return sg;
         double det;
         if (orient3d_certified(a, b, c, d, &det)) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
     }
@@ -281,6 +372,8 @@ constexpr int kInsphereCap = 256;
 static __device__ __noinline__ int insphere_sign(const d3& a, const d3& b, const d3& c, const d3& d,
                                           const d3& e, int* overflow) {
     {
+        int sg;
+        if (insphere_int(a, b, c, d, e, &sg)) return sg;
         double det;
         if (insphere_certified(a, b, c, d, e, &det)) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
     }

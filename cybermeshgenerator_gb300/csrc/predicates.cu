@@ -234,14 +234,24 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
             if (decided) {
                 out[i] = static_cast<int8_t>(sgn(det));
             } else {
-                // an evaluation in which no operation rounded is the exact determinant
-                double ex;
-                const bool cert = NPT == 4 ? exact::orient3d_certified(a, b, c, d, &ex)
-                                           : exact::insphere_certified(a, b, c, d,
-                                                                       {v[12], v[13], v[14]}, &ex);
-                if (cert) {
-                    out[i] = static_cast<int8_t>(sgn(ex));
+                // integer coordinates after a common power-of-two scaling give the
+                // exact determinant on the integer pipe; else an FP64 evaluation in
+                // which no operation rounded is the exact determinant
+                const d3 e{NPT == 5 ? v[12] : 0.0, NPT == 5 ? v[13] : 0.0, NPT == 5 ? v[14] : 0.0};
+                int isg;
+                const bool icert = NPT == 4 ? exact::orient3d_int(a, b, c, d, &isg)
+                                            : exact::insphere_int(a, b, c, d, e, &isg);
+                if (icert) {
+                    out[i] = static_cast<int8_t>(isg);
                     decided = certified = true;
+                } else {
+                    double ex;
+                    const bool cert = NPT == 4 ? exact::orient3d_certified(a, b, c, d, &ex)
+                                               : exact::insphere_certified(a, b, c, d, e, &ex);
+                    if (cert) {
+                        out[i] = static_cast<int8_t>(sgn(ex));
+                        decided = certified = true;
+                    }
                 }
             }
             undecided = !decided;
