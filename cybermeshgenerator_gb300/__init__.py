@@ -120,6 +120,26 @@ class PLC:
             self._handle = None
 
 
+def read_plc(path: str) -> PLC:
+    """Read a PLC boundary from a surface file, as the reference's ``read_plc``
+    (bindings/python/src/cybermesh/__init__.py:395-397): .stl is read here (records
+    decoded and vertices merged on the GPU); the reference's other formats are outside
+    this library (RuntimeError)."""
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    _check(_clib.cmg_read_plc(str(path).encode(), ctypes.byref(out), err, 512), err)
+    return PLC(out.value)
+
+
+def plc_from_stl(data: bytes) -> PLC:
+    """A PLC from an in-memory STL image (binary or ASCII), as read_plc reads a file."""
+    buf = bytes(data)
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    _check(_clib.cmg_plc_from_stl(buf, len(buf), ctypes.byref(out), err, 512), err)
+    return PLC(out.value)
+
+
 @dataclass
 class VoxelGrid:
     """A regular grid from :func:`voxelize`: ``grid`` is (nx, ny, nz), uint8

@@ -92,6 +92,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_plc_set_points", I, [V, c_double_p, Z])
     sig("cmg_plc_add_facet", I, [V, c_int_p, Z, I])
     sig("cmg_plc_add_triangles", I, [V, c_int_p, Z, I])
+    sig("cmg_plc_from_stl", I, [V, Z, ctypes.POINTER(V), S, Z])
     sig("cmg_plc_add_hole", I, [V, D, D, D])
     sig("cmg_plc_add_region", I, [V, D, D, D, D, D])
     sig("cmg_options_set_plc", I, [V, I])

@@ -14,10 +14,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <climits>
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <fstream>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -797,11 +799,62 @@ const int* cmg_mesh_tets(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_faces(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_tet_markers(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_face_markers(const cmg_mesh*) { return nullptr; }
+// The file extension, lower case (src/io/dispatch.cpp:19-26).
+std::string lower_ext(const std::string& path) {
+    const auto dot = path.rfind('.');
+    if (dot == std::string::npos) return {};
+    std::string e = path.substr(dot + 1);
+    for (char& c : e) c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
+    return e;
+}
+
+cmg_plc* plc_from_stl(const char* bytes, size_t n) {
+    std::vector<double> pts;
+    std::vector<int> tris;
+    {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cmg::gpu::stl_read(bytes, n, pts, tris, gpu_stream());
+    }
+    std::unique_ptr<cmg_plc> p(new cmg_plc{});
+    p->points = std::move(pts);
+    const size_t nt = tris.size() / 3;
+    p->fidx = std::move(tris);
+    p->foff.resize(nt + 1);
+    for (size_t f = 0; f <= nt; ++f) p->foff[f] = 3 * f;
+    p->markers.assign(nt, 0);
+    return p.release();
+}
+
+cmg_status cmg_plc_from_stl(const void* data, size_t n, cmg_plc** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if ((!data && n) || !out) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] { *out = plc_from_stl(static_cast<const char*>(data), n); });
+}
+
+// read_plc (src/io/dispatch.cpp:64-74): .stl through the GPU reader; the other formats
+// the reference reads are outside this library; anything else is unsupported.
 cmg_status cmg_read_plc(const char* path, cmg_plc** out, char* errbuf, size_t len) {
     if (out) *out = nullptr;
     if (!path || !out) return CMG_ERR_INVALID_INPUT;
-    set_err(errbuf, len, kNotHere);
-    return CMG_ERR_NOT_IMPLEMENTED;
+    const std::string p(path), e = lower_ext(p);
+    if (e == "poly" || e == "smesh" || e == "off" || e == "ply" || e == "obj") {
+        set_err(errbuf, len, kNotHere);
+        return CMG_ERR_NOT_IMPLEMENTED;
+    }
+    if (e != "stl") {
+        set_err(errbuf, len, "unsupported file format for " + p);
+        return CMG_ERR_INVALID_INPUT;
+    }
+    return guarded(errbuf, len, [&] {
+        std::ifstream in(p, std::ios::binary | std::ios::ate);
+        if (!in) throw CoreError{CMG_ERR_INVALID_INPUT, "cannot open file for reading: " + p};
+        const std::streamoff sz = in.tellg();
+        if (sz < 0) throw CoreError{CMG_ERR_INVALID_INPUT, "cannot open file for reading: " + p};
+        std::vector<char> buf(static_cast<size_t>(sz));
+        in.seekg(0);
+        if (sz > 0) in.read(buf.data(), sz);
+        *out = plc_from_stl(buf.data(), buf.size());
+    });
 }
 cmg_status cmg_read_points(const char* path, cmg_plc** out, char* errbuf, size_t len) {
     if (out) *out = nullptr;

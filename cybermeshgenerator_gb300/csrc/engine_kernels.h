@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "cmg_types.h"
 
@@ -77,6 +78,12 @@ void adjoint_backward(int precision, const GridDesc& g, int64_t ncell, const dou
                       const uint8_t* near_reg, const uint8_t* occ, const double* grad_sdf,
                       const int64_t* voff, const int* vinc, double* grad, void* tmp,
                       cudaStream_t st);
+
+// stl.cu: an STL image (host bytes) -> merged points (3 doubles each, first-occurrence
+// order) and triangles (3 indices each), as the reference's read_stl; throws
+// std::invalid_argument with its messages.
+void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vector<int>& tris,
+              cudaStream_t st);
 
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);

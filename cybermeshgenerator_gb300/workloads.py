@@ -438,3 +438,40 @@ def predicate_stream(n: int, kind: str = "orient3d", degenerate: float = 0.1,
             v[zero] = ulps[zero].astype(np.float64) * 2.0 ** -60
             P[k, ax, nea] = v
     return np.ascontiguousarray(P.reshape(npt * 3, n))
+
+
+# --------------------------------------------------------------------------- #
+# STL images
+# --------------------------------------------------------------------------- #
+
+def stl_binary(points, triangles, header: bytes = b"cybermeshgenerator stl") -> bytes:
+    """Binary STL image: 80-byte header, u32 count, 50-byte records (zero normal,
+    three float32 vertices, zero attribute)."""
+    p = np.asarray(points, dtype=np.float32)
+    t = np.asarray(triangles, dtype=np.int64)
+    rec = np.zeros(len(t), dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]))
+    rec["v"] = p[t]
+    return header[:80].ljust(80, b"\0") + np.uint32(len(t)).tobytes() + rec.tobytes()
+
+
+def stl_ascii(points, triangles, fmt: str = "{:.9g}", crlf: bool = False,
+              comments: bool = False, commas: bool = False, upper: bool = False) -> bytes:
+    """ASCII STL image in the reference writer's layout, with optional variations
+    its reader accepts (comments, CRLF line ends, comma separators, upper case)."""
+    p = np.asarray(points, dtype=np.float64)
+    nl = "\r\n" if crlf else "\n"
+    sep = ", " if commas else " "
+    kw = "VERTEX" if upper else "vertex"
+    out = ["solid cmg"]
+    for i, t in enumerate(np.asarray(triangles)):
+        out.append("  facet normal 0 0 0" + (f"  # facet {i}" if comments else ""))
+        out.append("    outer loop")
+        for k in t:
+            out.append("      " + kw + " " + sep.join(fmt.format(float(c)) for c in p[k]))
+        out.append("    endloop")
+        out.append("  endfacet")
+        if comments and i % 7 == 0:
+            out.append("# a comment line")
+            out.append("   ")
+    out.append("endsolid cmg")
+    return (nl.join(out) + nl).encode()

@@ -97,6 +97,10 @@ const int* cmg_mesh_tets(const cmg_mesh*);
 const int* cmg_mesh_faces(const cmg_mesh*);
 const int* cmg_mesh_tet_markers(const cmg_mesh*);
 const int* cmg_mesh_face_markers(const cmg_mesh*);
+/* GB300 library: a .stl path is read on the GPU (the reference's read_stl semantics,
+ * see cmg_plc_from_stl in cmg_gpu.h); .poly/.smesh/.off/.ply/.obj answer
+ * CMG_ERR_NOT_IMPLEMENTED; any other extension is CMG_ERR_INVALID_INPUT
+ * ("unsupported file format for <path>"), as in the reference. */
 cmg_status cmg_read_plc(const char* path, cmg_plc** out, char* errbuf, size_t len);
 cmg_status cmg_read_points(const char* path, cmg_plc** out, char* errbuf, size_t len);
 cmg_status cmg_read_mesh(const char* path, cmg_mesh** out, char* errbuf, size_t len);

@@ -81,6 +81,14 @@ void cmg_voxel_opts_init(cmg_voxel_opts* opts);
  * counterpart in the reference; for meshes of millions of triangles. */
 cmg_status cmg_plc_add_triangles(cmg_plc*, const int* idx, size_t count, int marker);
 
+/* An STL image in memory (binary when its size is 84 + 50 n, else ASCII) read as the
+ * reference's read_stl reads a file (src/io/stl.cpp): one triangular facet per STL
+ * facet, coincident vertices merged on their exact coordinates in order of first
+ * occurrence; records decoded and vertices merged on the GPU. Errors carry the
+ * reference's messages (CMG_ERR_INVALID_INPUT); a NaN coordinate is an error. */
+cmg_status cmg_plc_from_stl(const void* data, size_t size, cmg_plc** out, char* errbuf,
+                            size_t errbuf_len);
+
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */
 cmg_status cmg_plc_voxelize_ex(const cmg_plc*, const cmg_voxel_opts* opts, cmg_voxels** out,

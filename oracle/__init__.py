@@ -218,6 +218,14 @@ class Oracle:
         a, b, c, d = (_f64(x) for x in (a, b, c, d))
         return self.L.orc_orient3d_fast(*(_ptr(x, _dp) for x in (a, b, c, d)))
 
+    def stl_read(self, data: bytes):
+        """The reference STL reader restated on an in-memory image: (points, triangles,
+        error) with error "" on success."""
+        if not getattr(self, "_stl_bound", False):
+            _stl_bind(self.L, "orc_stl", [ctypes.c_char_p, ctypes.c_size_t])
+            self._stl_bound = True
+        return _stl_unpack(self.L, "orc_stl", self.L.orc_stl_read(data, len(data)))
+
     def stream(self, kind, soa, mode=COMPAT, threads=None):
         """Signs of n queries; soa is a (12|15, n) float64 array."""
         soa = _f64(soa)
@@ -228,6 +236,36 @@ class Oracle:
         fn(rows, ctypes.c_int64(n), ctypes.c_int(mode), _ptr(out, _i8p),
            ctypes.c_int(self.threads(threads)))
         return out
+
+
+
+def _stl_unpack(L, prefix, h):
+    """(points (n,3) float64, triangles (m,3) int32, error str) from a reader handle."""
+    try:
+        err = getattr(L, prefix + "_error")(h).decode()
+        if err:
+            return None, None, err
+        n = int(getattr(L, prefix + "_num_points")(h))
+        m = int(getattr(L, prefix + "_num_triangles")(h))
+        pts = np.ctypeslib.as_array(getattr(L, prefix + "_points")(h), (n * 3,)).reshape(n, 3).copy() \
+            if n else np.zeros((0, 3))
+        tri = np.ctypeslib.as_array(getattr(L, prefix + "_triangles")(h), (m * 3,)).reshape(m, 3).copy() \
+            if m else np.zeros((0, 3), np.int32)
+        return pts, tri.astype(np.int32), ""
+    finally:
+        getattr(L, prefix + "_free")(h)
+
+
+def _stl_bind(L, prefix, arg):
+    getattr(L, prefix + "_read").restype = ctypes.c_void_p
+    getattr(L, prefix + "_read").argtypes = arg
+    getattr(L, prefix + "_error").restype = ctypes.c_char_p
+    for f, r in (("_num_points", ctypes.c_int64), ("_num_triangles", ctypes.c_int64),
+                 ("_points", _dp), ("_triangles", _ip)):
+        getattr(L, prefix + f).restype = r
+        getattr(L, prefix + f).argtypes = [ctypes.c_void_p]
+    getattr(L, prefix + "_error").argtypes = [ctypes.c_void_p]
+    getattr(L, prefix + "_free").argtypes = [ctypes.c_void_p]
 
 
 class Reference:
@@ -325,6 +363,13 @@ class Reference:
                                ctypes.c_double(spacing), _ptr(d, _ip), _ptr(vox, _i64p),
                                ctypes.c_int64(len(vox)), _ptr(out, _dp))
         return out
+
+    def stl_read(self, path: str):
+        """The reference's read_stl on a file: (points, triangles, error)."""
+        if not getattr(self, "_stl_bound", False):
+            _stl_bind(self.L, "ref_stl", [ctypes.c_char_p])
+            self._stl_bound = True
+        return _stl_unpack(self.L, "ref_stl", self.L.ref_stl_read(path.encode()))
 
     def pred(self, name, *pts):
         args = [_f64(p) for p in pts]

@@ -89,6 +89,56 @@ def pred_case(ref, name, n, seed):
     save(name, **out)
 
 
+def stl_cases():
+    """(name, image bytes) of the STL fixtures: binary and ASCII variants and errors."""
+    cases = []
+    p, t = W.jittered_icosphere(2, 0.02, seed=4)
+    cases.append(("bin_icosphere", W.stl_binary(p * 3.7 - 1.25, t)))
+    # +0 and -0 (equal as coordinates), a repeated and a degenerate triangle
+    q = np.array([[0.0, 0.0, 0.0], [-0.0, 1.0, 0.0], [1.0, -0.0, 0.0], [0.0, 0.0, 1.0],
+                  [0.0, -0.0, -0.0], [2.5, 2.5, 2.5]])
+    tt = np.array([[0, 1, 2], [4, 2, 3], [1, 2, 3], [0, 1, 3], [1, 2, 3], [5, 5, 5]])
+    cases.append(("bin_signed_zero", W.stl_binary(q, tt)))
+    one = np.array([[0, 0, 0], [2, 0, 0], [0, 3, 0]], float)
+    cases.append(("bin_one", W.stl_binary(one, [[0, 1, 2]])))
+    tet = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    ttet = [[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]]
+    cases.append(("ascii_tetra", W.stl_ascii(tet, ttet)))
+    cases.append(("ascii_variants", W.stl_ascii(p * 0.3, t, fmt="{:.17g}", crlf=True,
+                                                comments=True, commas=True, upper=True)))
+    odd = (b"solid odd\n facet normal 0 0 1\n  outer loop\n"
+           b"   vertex 1e0 +2.5 -0\n   vertex 0x1p-2 .5 3E-1\n   vertex 7 8 9 extra tokens\n"
+           b"  endloop\n endfacet\nendsolid\n")
+    cases.append(("ascii_number_forms", odd))
+    cases.append(("ascii_short_vertex", b"solid bad\n  facet normal 0 0 1\n    outer loop\n"
+                                        b"      vertex 0 0\n    endloop\n  endfacet\nendsolid bad\n"))
+    cases.append(("ascii_non_numeric", b"solid bad\nvertex 0 0 0\nvertex 1 0 0\nvertex 0 1x 0\n"))
+    cases.append(("ascii_out_of_range", b"solid bad\nvertex 0 0 0\nvertex 1e400 0 0\nvertex 0 1 0\n"))
+    cases.append(("ascii_four_vertices", b"vertex 0 0 0\nvertex 1 0 0\nvertex 0 1 0\nvertex 0 0 1\n"))
+    cases.append(("empty", b""))
+    return cases
+
+
+def stl_case(ref, manifest):
+    out = {}
+    tmp = os.path.join(ROOT, "oracle", "_ref", "stl_fixture.stl")
+    names = []
+    for name, data in stl_cases():
+        with open(tmp, "wb") as f:
+            f.write(data)
+        pts, tri, err = ref.stl_read(tmp)
+        out[name + "_bytes"] = np.frombuffer(data, dtype=np.uint8)
+        out[name + "_error"] = np.array(err)
+        out[name + "_points"] = pts if pts is not None else np.zeros((0, 3))
+        out[name + "_triangles"] = tri if tri is not None else np.zeros((0, 3), np.int32)
+        names.append(name)
+    os.remove(tmp)
+    out["names"] = np.array(names)
+    save("stl", **out)
+    manifest["stl"] = ("STL images (binary and ASCII variants, signed zeros, repeated and degenerate "
+                       "triangles, number forms, errors) read by the reference's read_stl")
+
+
 def main():
     O.build(ref=True)
     ref = O.Reference()
@@ -141,6 +191,8 @@ def main():
 
     if want("predicates"):
         pred_case(ref, "predicates", 4096, seed=21)
+    if want("stl"):
+        stl_case(ref, manifest)
     manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
 
     with open(path, "w") as f:

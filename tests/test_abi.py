@@ -117,7 +117,12 @@ def test_out_of_scope_entry_points(lib):
     plc = lib.cmg_plc_create()
     try:
         assert lib.cmg_tetrahedralize(plc, opts, ctypes.byref(out), err, 256) == 5
-        assert lib.cmg_read_plc(b"x.stl", ctypes.byref(out), err, 256) == 5
+        assert lib.cmg_read_plc(b"x.poly", ctypes.byref(out), err, 256) == 5
+        # .stl is read here: a missing file is the reference's error, before any GPU work
+        assert lib.cmg_read_plc(b"no_such_dir/x.stl", ctypes.byref(out), err, 256) == 1
+        assert err.value == b"cannot open file for reading: no_such_dir/x.stl"
+        assert lib.cmg_read_plc(b"x.xyz", ctypes.byref(out), err, 256) == 1
+        assert err.value == b"unsupported file format for x.xyz"
         assert lib.cmg_mesh_num_points(None) == 0 and not lib.cmg_mesh_points(None)
         assert lib.cmg_options_set_plc(opts, 1) == 0
     finally:

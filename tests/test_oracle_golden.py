@@ -142,3 +142,17 @@ def test_oracle_gradient_matches_central_differences(orc):
     # vertices no cell's nearest triangle touches have zero gradient
     used = np.unique(tris[tri[tri >= 0]].ravel())
     assert np.all(grad[np.setdiff1d(np.arange(len(pts)), used)] == 0.0)
+
+
+def test_stl_reader_matches_reference(orc, golden):
+    """The STL restatement against the reference's read_stl on every fixture: points
+    bit for bit (first occurrence kept, signed zeros merged), triangles, errors."""
+    g = golden("stl")
+    for name in g["names"]:
+        name = str(name)
+        pts, tri, err = orc.stl_read(g[name + "_bytes"].tobytes())
+        assert err == str(g[name + "_error"]), name
+        if err:
+            continue
+        assert np.array_equal(pts.view(np.uint64), g[name + "_points"].view(np.uint64)), name
+        assert np.array_equal(tri, g[name + "_triangles"]), name
