@@ -10,7 +10,7 @@ surface) for every cell; a voxel query = one cell's occupancy bit + SDF value.
 The plain all-FP64 path (bit-identical to the reference) is timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sdf|batch|scale|stream]
+                    [--workload sdf|batch|scale|stream|stl]
 
 The default workload (sdf) is the headline above. The others measure the rest of
 the path, each printing one line of the same form:
@@ -18,8 +18,10 @@ the path, each printing one line of the same form:
           occupancy + mixed SDF, replayed as a CUDA graph, autotuned;
   scale   2000 ellipsoids (2.56M triangles) at 512^3: forward (occupancy + mixed
           SDF + nearest-feature checkpoint) and the adjoint per step;
-  stream  1e8 orient3d + 1e8 insphere sign queries (10 % exactly degenerate,
-          10 % within a few ulps), reference semantics.
+  stream  1e8 orient3d + 1e8 insphere sign queries (10 % exactly degenerate),
+          reference semantics;
+  stl     a binary STL image of the 2000 ellipsoids (2.56M triangles) read into a PLC
+          (records decoded, coincident vertices merged).
 
 Under torchrun each rank runs its own replica (weak scaling; the path shares
 nothing between meshes), the timed region is bracketed by barriers and the
@@ -748,6 +750,117 @@ def _stream_cpu(host, seconds, threads=None):
             "sample": f"{tot_q} queries (the first of each kind), reference semantics"}
 
 
+STL_METRIC = "triangles/s, binary STL read + coincident-vertex merge (2.56M triangles)"
+
+
+def _stl_workload():
+    """The scale workload's 2000 ellipsoids as a binary STL image (2.56M triangles,
+    128 MB) and the same surface as ASCII (the first 200 ellipsoids, 256k triangles)."""
+    from cybermeshgenerator_gb300 import workloads as W
+    pts, tris = W.ellipsoid_field()
+    ascii_tris = tris[: 200 * 1280]
+    return W.stl_binary(pts, tris), W.stl_ascii(pts, ascii_tris, fmt="{:.9g}"), len(tris), len(ascii_tris)
+
+
+def _stl_cpu(data, ntris, seconds, reps=1):
+    """The oracle's restatement of the reference reader (single thread, as the
+    reference's) on the image: triangles/s."""
+    import oracle
+    orc = oracle.Oracle()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        orc.stl_read(data)
+        n += 1
+        if n >= reps or time.perf_counter() - t0 > seconds:
+            break
+    return ntris * n / (time.perf_counter() - t0)
+
+
+def run_stl(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    data, adata, ntris, antris = _stl_workload()
+    for _ in range(args.warmup):
+        cm.plc_from_stl(data)
+    l0 = cm.gpu_launches()
+    merge_ms, wall = [], []
+    barrier(world)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            plc = cm.plc_from_stl(data)
+            wall.append(time.perf_counter() - t0)
+            merge_ms.append(cm.stl_last_timing()["merge_ms"])
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // args.steps
+    total_ms = max_over_ranks(sum(merge_ms), world)
+    value = ntris * world * args.steps / (total_ms * 1e-3)
+    npts = plc.num_points
+    config = {"workload": f"binary STL image of the 2000-ellipsoid field ({ntris} triangles, "
+                          f"{len(data)} bytes, {npts} merged points): records decoded and "
+                          "coincident vertices merged; value from the device phase (records "
+                          "resident in HBM), e2e from host image to host PLC arrays",
+              "triangles": int(ntris), "bytes": len(data), "points": int(npts),
+              "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
+    line = _base_line(STL_METRIC, "triangles/s", value, world, args, total_ms, "fp32->fp64",
+                      config, launches, clk.summary())
+    if rank == 0:
+        tm = cm.stl_last_timing()
+        hbm = _measured_hbm()
+        # algorithmic bytes: the 50-byte records read, merged points (24 B) and
+        # triangles (12 B) written
+        byts = 50 * ntris + 24 * npts + 12 * ntris
+        ach = byts / (sum(merge_ms) / len(merge_ms) * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": "decode + merge (k_stl_extract, k_weld_*)",
+                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                            "traffic": None, "phase_ms": tm,
+                            "work": "50 B per triangle read, 24 B per merged point and 12 B per "
+                                    "triangle written",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+        line["e2e"] = {"value": ntris / (sum(wall) / len(wall)), "unit": "triangles/s",
+                       "h2d_bytes_per_step": len(data),
+                       "d2h_bytes_per_step": int(24 * npts + 12 * ntris),
+                       "call": "cmg_plc_from_stl (host image -> PLC handle)"}
+        t0 = time.perf_counter()
+        aplc = cm.plc_from_stl(adata)
+        ta = time.perf_counter() - t0
+        line["ascii"] = {"value": antris / ta, "unit": "triangles/s", "triangles": int(antris),
+                         "bytes": len(adata), "phase_ms": cm.stl_last_timing(),
+                         "host_threads": os.cpu_count(),
+                         "note": "parsed on host threads, merged on the GPU"}
+        if not args.no_cpu:
+            v = _stl_cpu(data, ntris, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+                                    "sample": "the whole binary image, read by the oracle's "
+                                              "restatement of the reference reader (ordered map)"}
+            line["ascii"]["cpu_baseline"] = _stl_cpu(adata, antris, args.cpu_seconds)
+        del aplc
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def ref_stl(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    data, _, ntris, _ = _stl_workload()
+    v = _stl_cpu(data, ntris, args.cpu_seconds, reps=max(1, args.steps))
+    base = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+            "sample": "the whole binary image per step"}
+    print(json.dumps(_ref_line(STL_METRIC, "triangles/s", v, args,
+                               {"workload": "binary STL of the 2000-ellipsoid field",
+                                "parallelism": "1 cpu thread (the reference reader is serial)"},
+                               base, ntris)), flush=True)
+
+
 def _ref_line(metric, unit, value, args, config, base, units_per_step):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
@@ -811,16 +924,16 @@ def main():
                     help="mixed record access: 0 L1/L2, 1 staged in shared memory, -1 default")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="sdf", choices=["sdf", "batch", "scale", "stream"])
+    ap.add_argument("--workload", default="sdf", choices=["sdf", "batch", "scale", "stream", "stl"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         {"sdf": run_reference, "batch": ref_batch, "scale": ref_scale,
-         "stream": ref_stream}[args.workload](args)
+         "stream": ref_stream, "stl": ref_stl}[args.workload](args)
     else:
         {"sdf": run_ours, "batch": run_batch, "scale": run_scale,
-         "stream": run_stream}[args.workload](args)
+         "stream": run_stream, "stl": run_stl}[args.workload](args)
 
 
 if __name__ == "__main__":

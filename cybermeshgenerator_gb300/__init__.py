@@ -140,6 +140,14 @@ def plc_from_stl(data: bytes) -> PLC:
     return PLC(out.value)
 
 
+def stl_last_timing() -> Dict[str, float]:
+    """Phase times (ms, CUDA events) of the last STL read on the current device."""
+    a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+    _check(_clib.cmg_stl_last_timing(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+           ctypes.create_string_buffer(1))
+    return {"upload_ms": a.value, "merge_ms": b.value, "download_ms": c.value}
+
+
 @dataclass
 class VoxelGrid:
     """A regular grid from :func:`voxelize`: ``grid`` is (nx, ny, nz), uint8

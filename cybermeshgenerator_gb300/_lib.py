@@ -93,6 +93,8 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_plc_add_facet", I, [V, c_int_p, Z, I])
     sig("cmg_plc_add_triangles", I, [V, c_int_p, Z, I])
     sig("cmg_plc_from_stl", I, [V, Z, ctypes.POINTER(V), S, Z])
+    F = ctypes.POINTER(ctypes.c_float)
+    sig("cmg_stl_last_timing", I, [F, F, F])
     sig("cmg_plc_add_hole", I, [V, D, D, D])
     sig("cmg_plc_add_region", I, [V, D, D, D, D, D])
     sig("cmg_options_set_plc", I, [V, I])

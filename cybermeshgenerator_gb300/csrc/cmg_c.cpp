@@ -831,6 +831,16 @@ cmg_status cmg_plc_from_stl(const void* data, size_t n, cmg_plc** out, char* err
     return guarded(errbuf, len, [&] { *out = plc_from_stl(static_cast<const char*>(data), n); });
 }
 
+cmg_status cmg_stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms) {
+    if (!upload_ms || !merge_ms || !download_ms) return CMG_ERR_INVALID_INPUT;
+    try {
+        cmg::gpu::stl_last_timing(upload_ms, merge_ms, download_ms);
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
 // read_plc (src/io/dispatch.cpp:64-74): .stl through the GPU reader; the other formats
 // the reference reads are outside this library; anything else is unsupported.
 cmg_status cmg_read_plc(const char* path, cmg_plc** out, char* errbuf, size_t len) {

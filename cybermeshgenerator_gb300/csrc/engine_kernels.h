@@ -84,6 +84,9 @@ void adjoint_backward(int precision, const GridDesc& g, int64_t ncell, const dou
 // std::invalid_argument with its messages.
 void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vector<int>& tris,
               cudaStream_t st);
+// Phase times of the last stl_read on this device (CUDA events): upload of the
+// records (or parsed coordinates), decode + merge kernels, download of the arrays.
+void stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
 
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);

@@ -123,6 +123,8 @@ __global__ void k_weld_emit(int64_t nv, const double* __restrict__ v, const int*
 struct StlWork {
     Arena arena;
     std::mutex mu;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float ms[3] = {0.f, 0.f, 0.f};  // last call: upload, decode + merge, download
 };
 StlWork& stl_work() {
     static StlWork w[64];
@@ -274,13 +276,18 @@ void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vect
         A.reserve(A.need());
         plan(&raw, &v, &tab, &slot, &first, &flag, &rank, &stmp, &dp, &di, &fl);
     }
+    if (!W.ev[0])
+        for (cudaEvent_t& e : W.ev) CMG_CUDA(cudaEventCreate(&e));
+    CMG_CUDA(cudaEventRecord(W.ev[0], st));
     if (binary) {
         CMG_CUDA(cudaMemcpyAsync(raw, bytes + 84, 50ull * n, cudaMemcpyHostToDevice, st));
+        CMG_CUDA(cudaEventRecord(W.ev[1], st));
         k_stl_extract<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(
             reinterpret_cast<const uint16_t*>(raw), n, v);
         CMG_LAUNCH();
     } else {
         CMG_CUDA(cudaMemcpyAsync(v, hv.data(), sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, st));
+        CMG_CUDA(cudaEventRecord(W.ev[1], st));
     }
     CMG_CUDA(cudaMemsetAsync(fl, 0, 2 * sizeof(int), st));
     CMG_CUDA(cudaMemsetAsync(tab, 0xff, sizeof(int) * S, st));          // kEmpty
@@ -295,6 +302,7 @@ void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vect
     exclusive_scan(flag, rank, nv, stmp, st);
     k_weld_emit<<<gv, 256, 0, st>>>(nv, v, slot, first, rank, dp, di);
     CMG_LAUNCH();
+    CMG_CUDA(cudaEventRecord(W.ev[2], st));
     int hf[2] = {0, 0};
     int64_t np = 0;
     CMG_CUDA(cudaMemcpyAsync(hf, fl, sizeof(hf), cudaMemcpyDeviceToHost, st));
@@ -306,7 +314,17 @@ void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vect
     tris.resize(static_cast<size_t>(nv));
     CMG_CUDA(cudaMemcpyAsync(pts.data(), dp, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, st));
     CMG_CUDA(cudaMemcpyAsync(tris.data(), di, sizeof(int) * nv, cudaMemcpyDeviceToHost, st));
+    CMG_CUDA(cudaEventRecord(W.ev[3], st));
     CMG_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < 3; ++k) CMG_CUDA(cudaEventElapsedTime(&W.ms[k], W.ev[k], W.ev[k + 1]));
+}
+
+void stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms) {
+    StlWork& W = stl_work();
+    std::lock_guard<std::mutex> lk(W.mu);
+    *upload_ms = W.ms[0];
+    *merge_ms = W.ms[1];
+    *download_ms = W.ms[2];
 }
 
 }  // namespace cmg::gpu

@@ -89,6 +89,11 @@ cmg_status cmg_plc_add_triangles(cmg_plc*, const int* idx, size_t count, int mar
 cmg_status cmg_plc_from_stl(const void* data, size_t size, cmg_plc** out, char* errbuf,
                             size_t errbuf_len);
 
+/* Phase times (CUDA events) of the last STL read on the current device: upload of
+ * the records (binary) or parsed coordinates (ASCII), decode + merge kernels, download
+ * of the points and triangles. */
+cmg_status cmg_stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
+
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */
 cmg_status cmg_plc_voxelize_ex(const cmg_plc*, const cmg_voxel_opts* opts, cmg_voxels** out,
