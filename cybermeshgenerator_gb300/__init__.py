@@ -140,6 +140,24 @@ def plc_from_stl(data: bytes) -> PLC:
     return PLC(out.value)
 
 
+def self_intersections(plc: PLC) -> np.ndarray:
+    """Crossing pairs of fan triangles of the PLC's facets, as the reference's
+    cmg::detect::self_intersections: an (k, 8) int32 array of rows (facet_a, facet_b,
+    triangle a's three vertex indices, triangle b's), in the reference's order."""
+    if not isinstance(plc, PLC):
+        raise TypeError("plc must be a PLC")
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    _check(_clib.cmg_plc_self_intersections(plc._handle, ctypes.byref(out), err, 512), err)
+    try:
+        n = int(_clib.cmg_intersections_count(out.value))
+        if n == 0:
+            return np.zeros((0, 8), dtype=np.int32)
+        return np.ctypeslib.as_array(_clib.cmg_intersections_data(out.value), (n * 8,)).reshape(n, 8).copy()
+    finally:
+        _clib.cmg_intersections_destroy(out.value)
+
+
 def stl_last_timing() -> Dict[str, float]:
     """Phase times (ms, CUDA events) of the last STL read on the current device."""
     a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()

@@ -93,6 +93,10 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_plc_add_facet", I, [V, c_int_p, Z, I])
     sig("cmg_plc_add_triangles", I, [V, c_int_p, Z, I])
     sig("cmg_plc_from_stl", I, [V, Z, ctypes.POINTER(V), S, Z])
+    sig("cmg_plc_self_intersections", I, [V, ctypes.POINTER(V), S, Z])
+    sig("cmg_intersections_count", ctypes.c_int64, [V])
+    sig("cmg_intersections_data", c_int_p, [V])
+    sig("cmg_intersections_destroy", None, [V])
     F = ctypes.POINTER(ctypes.c_float)
     sig("cmg_stl_last_timing", I, [F, F, F])
     sig("cmg_plc_add_hole", I, [V, D, D, D])

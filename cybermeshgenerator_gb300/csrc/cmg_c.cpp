@@ -76,6 +76,10 @@ struct cmg_batch {
     bool ran = false;
 };
 
+struct cmg_intersections {
+    std::vector<int> rows;  // 8 per crossing pair: facet_a, facet_b, tri_a[3], tri_b[3]
+};
+
 struct cmg_sdf_plan {
     std::unique_ptr<cmg::gpu::Batch> batch;
     GridDesc g{};
@@ -799,6 +803,48 @@ const int* cmg_mesh_tets(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_faces(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_tet_markers(const cmg_mesh*) { return nullptr; }
 const int* cmg_mesh_face_markers(const cmg_mesh*) { return nullptr; }
+// ------------------------------------------------------------------ self-intersections
+cmg_status cmg_plc_self_intersections(const cmg_plc* plc, cmg_intersections** out, char* errbuf,
+                                      size_t len) {
+    if (out) *out = nullptr;
+    if (!plc || !out) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        // fan triangles in facet order with their facet (src/detect/self_intersection.cpp:153-164)
+        std::vector<int> tris, facet;
+        for (size_t f = 0; f + 1 < plc->foff.size(); ++f) {
+            const int* v = plc->fidx.data() + plc->foff[f];
+            const size_t n = plc->foff[f + 1] - plc->foff[f];
+            for (size_t i = 2; i < n; ++i) {
+                tris.insert(tris.end(), {v[0], v[i - 1], v[i]});
+                facet.push_back(static_cast<int>(f));
+            }
+        }
+        std::vector<std::pair<int, int>> pairs;
+        {
+            std::lock_guard<std::mutex> lk(gpu_mutex());
+            cmg::gpu::self_intersections(plc->points.data(),
+                                         static_cast<int64_t>(plc->points.size() / 3), tris.data(),
+                                         static_cast<int64_t>(tris.size() / 3), pairs, gpu_stream());
+        }
+        std::unique_ptr<cmg_intersections> r(new cmg_intersections);
+        r->rows.reserve(8 * pairs.size());
+        for (const auto& pq : pairs) {
+            const int i = pq.first, j = pq.second;
+            r->rows.insert(r->rows.end(), {facet[i], facet[j], tris[3 * i], tris[3 * i + 1],
+                                           tris[3 * i + 2], tris[3 * j], tris[3 * j + 1],
+                                           tris[3 * j + 2]});
+        }
+        *out = r.release();
+    });
+}
+int64_t cmg_intersections_count(const cmg_intersections* r) {
+    return r ? static_cast<int64_t>(r->rows.size() / 8) : 0;
+}
+const int* cmg_intersections_data(const cmg_intersections* r) {
+    return (r && !r->rows.empty()) ? r->rows.data() : nullptr;
+}
+void cmg_intersections_destroy(cmg_intersections* r) { delete r; }
+
 // The file extension, lower case (src/io/dispatch.cpp:19-26).
 std::string lower_ext(const std::string& path) {
     const auto dot = path.rfind('.');

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "cmg_types.h"
@@ -87,6 +88,12 @@ void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vect
 // Phase times of the last stl_read on this device (CUDA events): upload of the
 // records (or parsed coordinates), decode + merge kernels, download of the arrays.
 void stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
+
+// detect.cu: the pairs (i, j), i < j, of triangles (host arrays; an index outside
+// [0, npts) marks a triangle to skip) that share no vertex index and cross, in (i, j)
+// order, as the reference's self_intersections.
+void self_intersections(const double* pts, int64_t npts, const int* tris, int64_t ntris,
+                        std::vector<std::pair<int, int>>& pairs, cudaStream_t st);
 
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);

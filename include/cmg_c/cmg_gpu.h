@@ -94,6 +94,22 @@ cmg_status cmg_plc_from_stl(const void* data, size_t size, cmg_plc** out, char* 
  * of the points and triangles. */
 cmg_status cmg_stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
 
+/* ---- self-intersections ------------------------------------------------------ */
+/* Replaces cmg::detect::self_intersections (src/detect/self_intersection.cpp:150-188):
+ * every facet polygon flattened into a fan (v0, v[i-1], v[i]) in facet order; the pairs
+ * of fan triangles i < j that share no vertex index and cross (the Guigue-Devillers
+ * orientation test on the reference's orient3d signs; coplanar pairs do not cross),
+ * in (i, j) order. Triangles with an index outside the point range are skipped.
+ * A uniform-grid broad phase on the GPU replaces the reference's all-pairs loop; the
+ * result is the same list. Each row of the result holds 8 ints: facet_a, facet_b, the
+ * three vertex indices of triangle i, those of triangle j. */
+typedef struct cmg_intersections cmg_intersections;
+cmg_status cmg_plc_self_intersections(const cmg_plc*, cmg_intersections** out, char* errbuf,
+                                      size_t errbuf_len);
+int64_t cmg_intersections_count(const cmg_intersections*);
+const int* cmg_intersections_data(const cmg_intersections*);
+void cmg_intersections_destroy(cmg_intersections*);
+
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */
 cmg_status cmg_plc_voxelize_ex(const cmg_plc*, const cmg_voxel_opts* opts, cmg_voxels** out,

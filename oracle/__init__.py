@@ -226,6 +226,17 @@ class Oracle:
             self._stl_bound = True
         return _stl_unpack(self.L, "orc_stl", self.L.orc_stl_read(data, len(data)))
 
+    def self_intersections(self, pts, tris):
+        """(i, j) pairs, i < j, of crossing triangles (reference order), int64 (k, 2)."""
+        pts, tris = _f64(pts), _i32(tris)
+        self.L.orc_self_intersections.restype = ctypes.c_int64
+        n = self.L.orc_self_intersections(_ptr(pts, _dp), ctypes.c_int64(len(pts)), _ptr(tris, _ip),
+                                          ctypes.c_int64(len(tris)), None, ctypes.c_int64(0))
+        out = np.zeros((max(n, 1), 2), dtype=np.int64)
+        self.L.orc_self_intersections(_ptr(pts, _dp), ctypes.c_int64(len(pts)), _ptr(tris, _ip),
+                                      ctypes.c_int64(len(tris)), _ptr(out, _i64p), ctypes.c_int64(n))
+        return out[:n]
+
     def stream(self, kind, soa, mode=COMPAT, threads=None):
         """Signs of n queries; soa is a (12|15, n) float64 array."""
         soa = _f64(soa)
@@ -370,6 +381,19 @@ class Reference:
             _stl_bind(self.L, "ref_stl", [ctypes.c_char_p])
             self._stl_bound = True
         return _stl_unpack(self.L, "ref_stl", self.L.ref_stl_read(path.encode()))
+
+    def self_intersections(self, pts, tris):
+        """The reference's self_intersections on a PLC of one triangle per facet:
+        (k, 8) int32 rows (facet_a, facet_b, tri_a[3], tri_b[3]) in its order."""
+        pts, tris = _f64(pts), _i32(tris)
+        f = self.L.ref_self_intersections
+        f.restype = ctypes.c_longlong
+        n = f(_ptr(pts, _dp), ctypes.c_longlong(len(pts)), _ptr(tris, _ip), ctypes.c_longlong(len(tris)),
+              None, ctypes.c_longlong(0))
+        out = np.zeros((max(n, 1), 8), dtype=np.int32)
+        f(_ptr(pts, _dp), ctypes.c_longlong(len(pts)), _ptr(tris, _ip), ctypes.c_longlong(len(tris)),
+          _ptr(out, _ip), ctypes.c_longlong(n))
+        return out[:n]
 
     def pred(self, name, *pts):
         args = [_f64(p) for p in pts]

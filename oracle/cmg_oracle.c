@@ -926,3 +926,104 @@ void orc_sdf_grad(const double* pts, int64_t npts, const int* tris,
                 grad[3 * (int64_t)T[k] + a] += dLdd * (-lam[k] * (p[a] - q[a]) / d);
     }
 }
+
+/* ------------------------------------------------------------------ self-intersections
+ * Restatement of src/detect/self_intersection.cpp: every pair of fan triangles i < j
+ * that share no vertex index is tested with the Guigue-Devillers orientation test
+ * (O. Devillers, P. Guigue, "Faster Triangle-Triangle Intersection Tests", INRIA
+ * RR-4488, 2002), every decision a sign of the reference's robust::orient3d (the
+ * rounded determinant unless it is exactly zero, then the exact sign); coplanar pairs
+ * count as not crossing (:20-103, :110-188). */
+static int o3s(const double* a, const double* b, const double* c, const double* d) {
+    return orc_orient3d_sign(a, b, c, d, ORC_COMPAT);
+}
+
+/* The two intersection intervals on the line of the planes overlap. */
+static int gd_interval(const double* p1, const double* q1, const double* r1, const double* p2,
+                       const double* q2, const double* r2) {
+    if (o3s(q2, p2, p1, q1) > 0) return 0;
+    if (o3s(r2, p2, r1, p1) > 0) return 0;
+    return 1;
+}
+
+/* Triangle 2's vertex signs (s_p, s_q, s_r) with respect to triangle 1's plane; both
+ * triangles already rotated so that p1 is alone on its side of plane 2. */
+static int gd_core(const double* p1, const double* q1, const double* r1, const double* p2,
+                   const double* q2, const double* r2, int sp, int sq, int sr) {
+    if (sp > 0) {
+        if (sq > 0) return gd_interval(p1, r1, q1, r2, p2, q2);
+        if (sr > 0) return gd_interval(p1, r1, q1, q2, r2, p2);
+        return gd_interval(p1, q1, r1, p2, q2, r2);
+    }
+    if (sp < 0) {
+        if (sq < 0) return gd_interval(p1, q1, r1, r2, p2, q2);
+        if (sr < 0) return gd_interval(p1, q1, r1, q2, r2, p2);
+        return gd_interval(p1, r1, q1, p2, q2, r2);
+    }
+    if (sq > 0) {
+        if (sr >= 0) return gd_interval(p1, r1, q1, q2, r2, p2);
+        return gd_interval(p1, q1, r1, p2, q2, r2);
+    }
+    if (sq < 0) {
+        if (sr > 0) return gd_interval(p1, q1, r1, q2, r2, p2);
+        return gd_interval(p1, r1, q1, p2, q2, r2);
+    }
+    if (sr > 0) return gd_interval(p1, q1, r1, r2, p2, q2);
+    if (sr < 0) return gd_interval(p1, r1, q1, r2, p2, q2);
+    return 0; /* coplanar */
+}
+
+int orc_tri_tri_cross(const double* p1, const double* q1, const double* r1, const double* p2,
+                      const double* q2, const double* r2) {
+    const int a = o3s(p1, p2, q2, r2), b = o3s(q1, p2, q2, r2), c = o3s(r1, p2, q2, r2);
+    if (a * b > 0 && a * c > 0) return 0;
+    const int d = o3s(p2, q1, r1, p1), e = o3s(q2, q1, r1, p1), f = o3s(r2, q1, r1, p1);
+    if (d * e > 0 && d * f > 0) return 0;
+    if (a > 0) {
+        if (b > 0) return gd_core(r1, p1, q1, p2, r2, q2, d, f, e);
+        if (c > 0) return gd_core(q1, r1, p1, p2, r2, q2, d, f, e);
+        return gd_core(p1, q1, r1, p2, q2, r2, d, e, f);
+    }
+    if (a < 0) {
+        if (b < 0) return gd_core(r1, p1, q1, p2, q2, r2, d, e, f);
+        if (c < 0) return gd_core(q1, r1, p1, p2, q2, r2, d, e, f);
+        return gd_core(p1, q1, r1, p2, r2, q2, d, f, e);
+    }
+    if (b < 0) {
+        if (c >= 0) return gd_core(q1, r1, p1, p2, r2, q2, d, f, e);
+        return gd_core(p1, q1, r1, p2, q2, r2, d, e, f);
+    }
+    if (b > 0) {
+        if (c > 0) return gd_core(p1, q1, r1, p2, r2, q2, d, f, e);
+        return gd_core(q1, r1, p1, p2, q2, r2, d, e, f);
+    }
+    if (c > 0) return gd_core(r1, p1, q1, p2, q2, r2, d, e, f);
+    if (c < 0) return gd_core(r1, p1, q1, p2, r2, q2, d, f, e);
+    return 0; /* coplanar */
+}
+
+int64_t orc_self_intersections(const double* pts, int64_t npts, const int* tris, int64_t ntris,
+                               int64_t* out_pairs, int64_t cap) {
+    int64_t n = 0;
+    for (int64_t i = 0; i < ntris; ++i) {
+        const int* A = tris + 3 * i;
+        if (A[0] < 0 || A[0] >= npts || A[1] < 0 || A[1] >= npts || A[2] < 0 || A[2] >= npts) continue;
+        for (int64_t j = i + 1; j < ntris; ++j) {
+            const int* B = tris + 3 * j;
+            int shared = 0;
+            for (int x = 0; x < 3; ++x)
+                for (int y = 0; y < 3; ++y) shared |= A[x] == B[y];
+            if (shared) continue;
+            if (B[0] < 0 || B[0] >= npts || B[1] < 0 || B[1] >= npts || B[2] < 0 || B[2] >= npts) continue;
+            if (orc_tri_tri_cross(pts + 3 * A[0], pts + 3 * A[1], pts + 3 * A[2], pts + 3 * B[0],
+                                  pts + 3 * B[1], pts + 3 * B[2])) {
+                if (n < cap) {
+                    out_pairs[2 * n] = i;
+                    out_pairs[2 * n + 1] = j;
+                }
+                ++n;
+            }
+        }
+    }
+    return n;
+}

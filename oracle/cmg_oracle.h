@@ -127,6 +127,15 @@ void orc_sdf_grad(const double* pts, int64_t npts, const int* tris,
                   const orc_grid* g, const uint8_t* occ, const int* tri,
                   const double* w, const double* t, double* grad);
 
+/* Self-intersections (src/detect/self_intersection.cpp): the pairs (i, j), i < j, of
+ * triangles sharing no vertex index that cross by the Guigue-Devillers orientation test
+ * on the reference's orient3d signs; triangles with an index outside [0, npts) are
+ * skipped. Writes at most cap pairs (2 int64 each) in (i, j) order; returns the count. */
+int orc_tri_tri_cross(const double* p1, const double* q1, const double* r1, const double* p2,
+                      const double* q2, const double* r2);
+int64_t orc_self_intersections(const double* pts, int64_t npts, const int* tris, int64_t ntris,
+                               int64_t* out_pairs, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

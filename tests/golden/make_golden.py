@@ -119,6 +119,52 @@ def stl_cases():
     return cases
 
 
+def detect_cases():
+    """(name, points, triangles) of the self-intersection fixtures."""
+    cases = []
+    cases.append(("crossing", np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0], [0, -1, -1], [0, 1, -1],
+                                        [0, 0, 1]], float), np.array([[0, 1, 2], [3, 4, 5]])))
+    cp, ct = W.unit_box()
+    cases.append(("cube", cp, ct))
+    tet = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    cases.append(("tetra", tet, np.array([[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]])))
+    p, t = W.jittered_icosphere(2, 0.02, seed=3)
+    cases.append(("two_icospheres", np.vstack([p, p * 0.9 + 0.5]), np.vstack([t, t + len(p)])))
+    rng = np.random.default_rng(17)
+    soup = rng.random((450, 3))
+    cases.append(("random_soup", soup, np.arange(450).reshape(150, 3)))
+    # integer grid points: coplanar overlaps, vertex and edge contacts, repeated indices,
+    # an out-of-range index (skipped)
+    g = np.array([[x, y, z] for z in range(3) for y in range(3) for x in range(3)], float)
+    idx = lambda x, y, z: x + 3 * y + 9 * z
+    tri = [[idx(0, 0, 0), idx(2, 0, 0), idx(0, 2, 0)],      # z = 0
+           [idx(1, 1, 0), idx(2, 2, 0), idx(0, 2, 0)],      # z = 0, overlapping (coplanar)
+           [idx(1, 0, 1), idx(1, 0, 0), idx(1, 1, 2)],      # touches the first at a vertex/edge
+           [idx(0, 1, 0), idx(2, 1, 2), idx(0, 1, 2)],      # through the z = 0 triangles
+           [idx(1, 1, 1), idx(1, 1, 1), idx(2, 2, 2)],      # repeated index
+           [idx(0, 0, 2), idx(2, 0, 2), idx(1, 2, 0)],
+           [idx(2, 0, 1), idx(0, 2, 1), idx(0, 0, 1)],      # z = 1
+           [idx(1, 1, 0), idx(1, 1, 2), idx(2, 0, 1)],      # contains an edge point of the last
+           [idx(0, 0, 0), 99, idx(1, 1, 1)]]                # out of range
+    cases.append(("grid_degenerate", g, np.array(tri)))
+    return cases
+
+
+def detect_case(ref, manifest):
+    out = {}
+    names = []
+    for name, pts, tris in detect_cases():
+        out[name + "_points"] = np.asarray(pts, float)
+        out[name + "_triangles"] = np.asarray(tris, np.int32)
+        out[name + "_hits"] = ref.self_intersections(pts, tris)
+        names.append(name)
+    out["names"] = np.array(names)
+    save("detect", **out)
+    manifest["detect"] = ("self-intersection configurations (the reference tests' crossing, cube and "
+                          "tetrahedron, overlapping icospheres, a random soup, degenerate grid "
+                          "contacts) with the reference's self_intersections rows")
+
+
 def stl_case(ref, manifest):
     out = {}
     tmp = os.path.join(ROOT, "oracle", "_ref", "stl_fixture.stl")
@@ -193,6 +239,8 @@ def main():
         pred_case(ref, "predicates", 4096, seed=21)
     if want("stl"):
         stl_case(ref, manifest)
+    if want("detect"):
+        detect_case(ref, manifest)
     manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
 
     with open(path, "w") as f:

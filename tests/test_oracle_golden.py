@@ -156,3 +156,14 @@ def test_stl_reader_matches_reference(orc, golden):
             continue
         assert np.array_equal(pts.view(np.uint64), g[name + "_points"].view(np.uint64)), name
         assert np.array_equal(tri, g[name + "_triangles"]), name
+
+
+def test_self_intersections_match_reference(orc, golden):
+    """The self-intersection restatement against the reference's self_intersections on
+    every fixture: the same (i, j) pairs in the same order."""
+    g = golden("detect")
+    for name in g["names"]:
+        name = str(name)
+        got = orc.self_intersections(g[name + "_points"], g[name + "_triangles"])
+        want = g[name + "_hits"]
+        assert np.array_equal(got, want[:, :2].astype(np.int64)), name
