@@ -10,7 +10,7 @@ surface) for every cell; a voxel query = one cell's occupancy bit + SDF value.
 The plain all-FP64 path (bit-identical to the reference) is timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sdf|batch|scale|stream|stl]
+                    [--workload sdf|batch|scale|stream|stl|detect]
 
 The default workload (sdf) is the headline above. The others measure the rest of
 the path, each printing one line of the same form:
@@ -21,7 +21,8 @@ the path, each printing one line of the same form:
   stream  1e8 orient3d + 1e8 insphere sign queries (10 % exactly degenerate),
           reference semantics;
   stl     a binary STL image of the 2000 ellipsoids (2.56M triangles) read into a PLC
-          (records decoded, coincident vertices merged).
+          (records decoded, coincident vertices merged);
+  detect  the self-intersection preflight of the same 2.56M triangles.
 
 Under torchrun each rank runs its own replica (weak scaling; the path shares
 nothing between meshes), the timed region is bracketed by barriers and the
@@ -861,6 +862,101 @@ def ref_stl(args):
                                base, ntris)), flush=True)
 
 
+DETECT_METRIC = "triangles/s, self-intersection preflight (2.56M triangles, all-pairs semantics)"
+
+
+def _detect_cpu(pts, tris, seconds):
+    """The oracle's all-pairs restatement of the reference's self_intersections on the
+    first m triangles (m sized to the budget): pair tests/s, extrapolated to the whole
+    mesh's T(T-1)/2 pairs (the reference's cost)."""
+    import oracle
+    orc = oracle.Oracle()
+    m = 2000
+    t0 = time.perf_counter()
+    orc.self_intersections(pts, tris[:m])
+    dt = time.perf_counter() - t0
+    m = int(min(len(tris), m * max(1.0, (seconds / max(dt, 1e-6)) ** 0.5)))
+    t0 = time.perf_counter()
+    orc.self_intersections(pts, tris[:m])
+    dt = time.perf_counter() - t0
+    pair_rate = m * (m - 1) / 2 / dt
+    T = len(tris)
+    return T / (T * (T - 1) / 2 / pair_rate), m
+
+
+def run_detect(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    pts, tris = _scale_workload()
+    plc = cm.PLC.from_arrays(pts, tris)
+    for _ in range(args.warmup):
+        cm.self_intersections(plc)
+    l0 = cm.gpu_launches()
+    dev_ms, wall = [], []
+    barrier(world)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            hits = cm.self_intersections(plc)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(float(cm._clib.cmg_self_intersections_last_ms()))
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // args.steps
+    total_ms = max_over_ranks(sum(dev_ms), world)
+    T = len(tris)
+    value = T * world * args.steps / (total_ms * 1e-3)
+    config = {"workload": f"the 2000-ellipsoid field ({T} triangles, disjoint): every pair of "
+                          "triangles sharing no vertex tested for crossing (grid broad phase, "
+                          "Guigue-Devillers on the reference's orient3d signs); value from the "
+                          "device phase, e2e through cmg_plc_self_intersections",
+              "triangles": int(T), "hits": int(len(hits)), "l2": "inputs larger than L2",
+              "parallelism": f"replicas x{world}"}
+    line = _base_line(DETECT_METRIC, "triangles/s", value, world, args, total_ms, "fp64+exact",
+                      config, launches, clk.summary())
+    if rank == 0:
+        hbm = _measured_hbm()
+        byts = T * (12 + 72)  # indices + the three vertices read once per triangle
+        ach = byts / (sum(dev_ms) / len(dev_ms) * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": "k_det_boxes + k_det_bin + k_det_pairs",
+                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                            "traffic": None, "device_ms": sum(dev_ms) / len(dev_ms),
+                            "work": "84 B per triangle (indices and vertices read once); the pair "
+                                    "tests are orient3d signs on nearby triangles",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+        line["e2e"] = {"value": T / (sum(wall) / len(wall)), "unit": "triangles/s",
+                       "h2d_bytes_per_step": int(pts.nbytes + tris.astype(np.int32).nbytes),
+                       "d2h_bytes_per_step": 8, "call": "cmg_plc_self_intersections (PLC handle)"}
+        if not args.no_cpu:
+            v, m = _detect_cpu(pts, tris, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+                                    "sample": f"all pairs of the first {m} triangles timed, the pair "
+                                              f"rate extrapolated to the {T}-triangle mesh's "
+                                              "T(T-1)/2 pairs (extrapolated)"}
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def ref_detect(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    pts, tris = _scale_workload()
+    v, m = _detect_cpu(pts, tris, max(10.0, args.cpu_seconds))
+    base = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+            "sample": f"all pairs of the first {m} triangles, extrapolated to T(T-1)/2 pairs"}
+    print(json.dumps(_ref_line(DETECT_METRIC, "triangles/s", v, args,
+                               {"workload": "self-intersections of the 2000-ellipsoid field",
+                                "parallelism": "1 cpu thread (the reference loop is serial)"},
+                               base, len(tris))), flush=True)
+
+
 def _ref_line(metric, unit, value, args, config, base, units_per_step):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
@@ -924,16 +1020,17 @@ def main():
                     help="mixed record access: 0 L1/L2, 1 staged in shared memory, -1 default")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="sdf", choices=["sdf", "batch", "scale", "stream", "stl"])
+    ap.add_argument("--workload", default="sdf",
+                    choices=["sdf", "batch", "scale", "stream", "stl", "detect"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         {"sdf": run_reference, "batch": ref_batch, "scale": ref_scale,
-         "stream": ref_stream, "stl": ref_stl}[args.workload](args)
+         "stream": ref_stream, "stl": ref_stl, "detect": ref_detect}[args.workload](args)
     else:
         {"sdf": run_ours, "batch": run_batch, "scale": run_scale,
-         "stream": run_stream, "stl": run_stl}[args.workload](args)
+         "stream": run_stream, "stl": run_stl, "detect": run_detect}[args.workload](args)
 
 
 if __name__ == "__main__":

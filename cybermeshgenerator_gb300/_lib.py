@@ -97,6 +97,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_intersections_count", ctypes.c_int64, [V])
     sig("cmg_intersections_data", c_int_p, [V])
     sig("cmg_intersections_destroy", None, [V])
+    sig("cmg_self_intersections_last_ms", ctypes.c_float, [])
     F = ctypes.POINTER(ctypes.c_float)
     sig("cmg_stl_last_timing", I, [F, F, F])
     sig("cmg_plc_add_hole", I, [V, D, D, D])

@@ -844,6 +844,7 @@ const int* cmg_intersections_data(const cmg_intersections* r) {
     return (r && !r->rows.empty()) ? r->rows.data() : nullptr;
 }
 void cmg_intersections_destroy(cmg_intersections* r) { delete r; }
+float cmg_self_intersections_last_ms(void) { return cmg::gpu::self_intersections_last_ms(); }
 
 // The file extension, lower case (src/io/dispatch.cpp:19-26).
 std::string lower_ext(const std::string& path) {

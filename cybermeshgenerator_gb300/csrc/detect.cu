@@ -203,9 +203,16 @@ __global__ void k_det_pairs(int64_t nentries, const int* __restrict__ list, cons
 
 }  // namespace
 
+namespace {
+float g_last_ms = 0.f;  // device time of the last call's broad + narrow phase
+}
+
+float self_intersections_last_ms() { return g_last_ms; }
+
 void self_intersections(const double* h_pts, int64_t npts, const int* h_tris, int64_t ntris,
                         std::vector<std::pair<int, int>>& pairs, cudaStream_t st) {
     pairs.clear();
+    g_last_ms = 0.f;
     if (ntris < 2) return;
     if (ntris >= (int64_t(1) << 31)) throw std::invalid_argument("self_intersections: too many triangles");
     // grid over the valid triangles' points: cell edge ~ twice the mean box extent
@@ -292,12 +299,23 @@ void self_intersections(const double* h_pts, int64_t npts, const int* h_tris, in
     exclusive_scan(cellcnt, celloff, ncell, stmp, st);
     CMG_CUDA(cudaMemcpyAsync(&nent, celloff + ncell, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CMG_CUDA(cudaStreamSynchronize(st));
+    cudaEvent_t e0, e1;
+    CMG_CUDA(cudaEventCreate(&e0));
+    CMG_CUDA(cudaEventCreate(&e1));
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } ev{e0, e1};
     for (int attempt = 0; attempt < 2; ++attempt) {
         // the entry list (and, on a second attempt, the output) sized; inputs re-uploaded
         // because a grown arena moved them
         sized(nent);
         CMG_CUDA(cudaMemcpyAsync(d_pts, h_pts, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
         CMG_CUDA(cudaMemcpyAsync(d_tris, h_tris, sizeof(int) * 3 * ntris, cudaMemcpyHostToDevice, st));
+        CMG_CUDA(cudaEventRecord(e0, st));
         k_det_boxes<<<gt, 256, 0, st>>>(ntris, d_tris, d_pts, npts, G, box, cnt);
         CMG_LAUNCH();
         CMG_CUDA(cudaMemsetAsync(cellcnt, 0, sizeof(int) * ncell, st));
@@ -313,9 +331,11 @@ void self_intersections(const double* h_pts, int64_t npts, const int* h_tris, in
                 nent, list, celloff, ncell, box, G, d_tris, d_pts, out, nout, cap);
             CMG_LAUNCH();
         }
+        CMG_CUDA(cudaEventRecord(e1, st));
         unsigned long long found = 0;
         CMG_CUDA(cudaMemcpyAsync(&found, nout, sizeof(found), cudaMemcpyDeviceToHost, st));
         CMG_CUDA(cudaStreamSynchronize(st));
+        CMG_CUDA(cudaEventElapsedTime(&g_last_ms, e0, e1));
         if (found <= cap) {
             std::vector<long long> h(found);
             if (found)

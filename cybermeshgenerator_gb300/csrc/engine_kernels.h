@@ -94,6 +94,8 @@ void stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
 // order, as the reference's self_intersections.
 void self_intersections(const double* pts, int64_t npts, const int* tris, int64_t ntris,
                         std::vector<std::pair<int, int>>& pairs, cudaStream_t st);
+// Device time (CUDA events) of the last call's boxes, binning and pair tests.
+float self_intersections_last_ms();
 
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);

@@ -109,6 +109,9 @@ cmg_status cmg_plc_self_intersections(const cmg_plc*, cmg_intersections** out, c
 int64_t cmg_intersections_count(const cmg_intersections*);
 const int* cmg_intersections_data(const cmg_intersections*);
 void cmg_intersections_destroy(cmg_intersections*);
+/* Device time in ms (CUDA events) of the last self-intersection search: boxes,
+ * binning and pair tests, without the host transfers. */
+float cmg_self_intersections_last_ms(void);
 
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */
