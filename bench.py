@@ -957,6 +957,110 @@ def ref_detect(args):
                                base, len(tris))), flush=True)
 
 
+SIMPLIFY_METRIC = "input triangles/s, grid vertex clustering (2.56M triangles, grid 34)"
+
+
+def _simplify_cpu(pts, tris, grid, seconds, reps=1):
+    """The oracle's restatement of the reference's simplify (single thread, as the
+    reference's) on the whole surface: input triangles/s."""
+    import oracle
+    orc = oracle.Oracle()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        orc.simplify(pts, tris, grid)
+        n += 1
+        if n >= reps or time.perf_counter() - t0 > seconds:
+            break
+    return len(tris) * n / (time.perf_counter() - t0)
+
+
+def run_simplify(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    pts, tris = _scale_workload()
+    plc = cm.PLC.from_arrays(pts, tris)
+    grid = 34
+    for _ in range(args.warmup):
+        cm.simplify(plc, grid)
+    l0 = cm.gpu_launches()
+    dev_ms, wall = [], []
+    barrier(world)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            out = cm.simplify(plc, grid)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(cm.simplify_last_timing()["cluster_ms"])
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // args.steps
+    total_ms = max_over_ranks(sum(dev_ms), world)
+    T, P = len(tris), len(pts)
+    value = T * world * args.steps / (total_ms * 1e-3)
+    nrep, nkept = out.num_points, len(out.triangles)
+    config = {"workload": f"the 2000-ellipsoid field ({T} triangles, {P} points) simplified at "
+                          f"the reference's default grid {grid} ({nrep} representatives, {nkept} "
+                          "triangles kept); value from the device phase (points and facets "
+                          "resident in HBM), e2e through cmg_plc_simplify (host PLC to host PLC)",
+              "triangles": int(T), "points": int(P), "grid": grid, "representatives": int(nrep),
+              "kept": int(nkept), "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
+    line = _base_line(SIMPLIFY_METRIC, "triangles/s", value, world, args, total_ms, "fp64",
+                      config, launches, clk.summary())
+    if rank == 0:
+        hbm = _measured_hbm()
+        # algorithmic bytes: points (24 B) and facets (12 B indices + 8 B offset) read
+        # once, representatives (24 B) and kept triangles (12 B) written
+        byts = 24 * P + 20 * T + 24 * nrep + 12 * nkept
+        ach = byts / (sum(dev_ms) / len(dev_ms) * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": "clustering (k_bbox .. k_tri_out, 13 kernels "
+                                                      "+ scans and the radix sort)",
+                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                            "traffic": None, "phase_ms": cm.simplify_last_timing(),
+                            "work": "24 B per point and 20 B per facet read, 24 B per "
+                                    "representative and 12 B per kept triangle written",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+        line["e2e"] = {"value": T / (sum(wall) / len(wall)), "unit": "triangles/s",
+                       "h2d_bytes_per_step": int(24 * P + 20 * T + 8),
+                       "d2h_bytes_per_step": int(24 * nrep + 12 * nkept),
+                       "call": "cmg_plc_simplify (PLC handle -> PLC handle)"}
+        # a fine grid keeps most triangles: the dedupe table and output dominate
+        t0 = time.perf_counter()
+        fine = cm.simplify(plc, 512)
+        tf = time.perf_counter() - t0
+        line["grid512"] = {"device_triangles_per_s": T / (cm.simplify_last_timing()["cluster_ms"] * 1e-3),
+                           "e2e_triangles_per_s": T / tf, "representatives": int(fine.num_points),
+                           "kept": int(len(fine.triangles))}
+        if not args.no_cpu:
+            v = _simplify_cpu(pts, tris, grid, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+                                    "sample": "the whole surface at grid 34, simplified by the "
+                                              "oracle's restatement of the reference's simplify"}
+            line["grid512"]["cpu_baseline"] = _simplify_cpu(pts, tris, 512, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def ref_simplify(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    pts, tris = _scale_workload()
+    v = _simplify_cpu(pts, tris, 34, args.cpu_seconds, reps=max(1, args.steps))
+    base = {"value": v, "unit": "triangles/s", "cores": 1, "kind": "port",
+            "sample": "the whole surface at grid 34 per step"}
+    print(json.dumps(_ref_line(SIMPLIFY_METRIC, "triangles/s", v, args,
+                               {"workload": "simplify of the 2000-ellipsoid field at grid 34",
+                                "parallelism": "1 cpu thread (the reference is serial)"},
+                               base, len(tris))), flush=True)
+
+
 def _ref_line(metric, unit, value, args, config, base, units_per_step):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
@@ -1021,16 +1125,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="sdf",
-                    choices=["sdf", "batch", "scale", "stream", "stl", "detect"])
+                    choices=["sdf", "batch", "scale", "stream", "stl", "detect", "simplify"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         {"sdf": run_reference, "batch": ref_batch, "scale": ref_scale,
-         "stream": ref_stream, "stl": ref_stl, "detect": ref_detect}[args.workload](args)
+         "stream": ref_stream, "stl": ref_stl, "detect": ref_detect,
+         "simplify": ref_simplify}[args.workload](args)
     else:
         {"sdf": run_ours, "batch": run_batch, "scale": run_scale,
-         "stream": run_stream, "stl": run_stl, "detect": run_detect}[args.workload](args)
+         "stream": run_stream, "stl": run_stl, "detect": run_detect,
+         "simplify": run_simplify}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -166,6 +166,28 @@ def stl_last_timing() -> Dict[str, float]:
     return {"upload_ms": a.value, "merge_ms": b.value, "download_ms": c.value}
 
 
+def simplify(plc: PLC, grid: int = 34) -> PLC:
+    """Simplify a PLC surface by grid vertex clustering and return a new PLC, as the
+    reference's ``simplify`` (bindings/python/src/cybermesh/__init__.py:400-413 over
+    src/simplify/simplify.cpp:48-112), on the GPU with bit-identical points and the
+    same triangles in the same order. ``grid`` is the number of cells along the longest
+    bounding-box axis."""
+    if not isinstance(plc, PLC):
+        raise TypeError("plc must be a PLC")
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(256)
+    _check(_clib.cmg_plc_simplify(plc._handle, int(grid), ctypes.byref(out), err, 256), err)
+    return PLC(out.value)
+
+
+def simplify_last_timing() -> Dict[str, float]:
+    """Phase times (ms, CUDA events) of the last simplify on the current device."""
+    a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+    _check(_clib.cmg_simplify_last_timing(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+           ctypes.create_string_buffer(1))
+    return {"upload_ms": a.value, "cluster_ms": b.value, "download_ms": c.value}
+
+
 @dataclass
 class VoxelGrid:
     """A regular grid from :func:`voxelize`: ``grid`` is (nx, ny, nz), uint8
@@ -491,4 +513,6 @@ def library_path() -> str:
 
 __all__ = ["orient3d_stream", "insphere_stream", "orient3d_signs", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
            "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
-           "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT"]
+           "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT",
+           "read_plc", "plc_from_stl", "self_intersections", "simplify", "stl_last_timing",
+           "simplify_last_timing"]

@@ -100,6 +100,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_self_intersections_last_ms", ctypes.c_float, [])
     F = ctypes.POINTER(ctypes.c_float)
     sig("cmg_stl_last_timing", I, [F, F, F])
+    sig("cmg_simplify_last_timing", I, [F, F, F])
     sig("cmg_plc_add_hole", I, [V, D, D, D])
     sig("cmg_plc_add_region", I, [V, D, D, D, D, D])
     sig("cmg_options_set_plc", I, [V, I])

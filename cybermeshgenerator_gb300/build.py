@@ -23,7 +23,7 @@ BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(HERE, "libcmg_c.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["scan.cu", "occupancy.cu", "sdf.cu", "sdf_sub.cu", "engine.cu", "peak.cu", "noalloc.cu", "predicates.cu", "adjoint.cu", "stl.cu", "detect.cu"]
+CU_SOURCES = ["scan.cu", "occupancy.cu", "sdf.cu", "sdf_sub.cu", "engine.cu", "peak.cu", "noalloc.cu", "predicates.cu", "adjoint.cu", "stl.cu", "detect.cu", "simplify.cu"]
 CXX_SOURCES = ["cmg_c.cpp"]
 
 

@@ -935,12 +935,44 @@ cmg_status cmg_write_plc(const char* path, const cmg_plc* p, char* errbuf, size_
     set_err(errbuf, len, kNotHere);
     return CMG_ERR_NOT_IMPLEMENTED;
 }
+// simplify (src/simplify/simplify.cpp:48-112) on the GPU: the result holds the
+// representative points and one single-triangle facet (marker 0) per kept triangle,
+// with no holes or regions, as the reference's.
 cmg_status cmg_plc_simplify(const cmg_plc* in, int grid, cmg_plc** out, char* errbuf, size_t len) {
-    (void)grid;
     if (out) *out = nullptr;
     if (!in || !out) return CMG_ERR_INVALID_INPUT;
-    set_err(errbuf, len, kNotHere);
-    return CMG_ERR_NOT_IMPLEMENTED;
+    return guarded(errbuf, len, [&] {
+        // simplify.cpp:49-54, answered before any device is touched
+        if (in->points.empty()) throw CoreError{CMG_ERR_INVALID_INPUT, "simplify: PLC has no points"};
+        if (grid < 1) throw CoreError{CMG_ERR_INVALID_INPUT, "simplify: grid must be >= 1"};
+        std::vector<double> pts;
+        std::vector<int> tris;
+        {
+            std::lock_guard<std::mutex> lk(gpu_mutex());
+            cmg::gpu::simplify(in->points.data(), static_cast<int64_t>(in->points.size() / 3),
+                               in->fidx.data(), static_cast<int64_t>(in->fidx.size()),
+                               in->foff.data(), static_cast<int64_t>(in->foff.size()) - 1, grid, pts,
+                               tris, gpu_stream());
+        }
+        std::unique_ptr<cmg_plc> p(new cmg_plc{});
+        p->points = std::move(pts);
+        const size_t nt = tris.size() / 3;
+        p->fidx = std::move(tris);
+        p->foff.resize(nt + 1);
+        for (size_t f = 0; f <= nt; ++f) p->foff[f] = 3 * f;
+        p->markers.assign(nt, 0);
+        *out = p.release();
+    });
+}
+
+cmg_status cmg_simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms) {
+    if (!upload_ms || !cluster_ms || !download_ms) return CMG_ERR_INVALID_INPUT;
+    try {
+        cmg::gpu::simplify_last_timing(upload_ms, cluster_ms, download_ms);
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
 }
 
 const char* cmg_version(void) { return "0.5.0"; }

@@ -97,6 +97,16 @@ void self_intersections(const double* pts, int64_t npts, const int* tris, int64_
 // Device time (CUDA events) of the last call's boxes, binning and pair tests.
 float self_intersections_last_ms();
 
+// simplify.cu: grid vertex clustering of the points and the fan triangles of the
+// facets (fidx / foff: facet f's polygon is fidx[foff[f] .. foff[f+1]), nfacets + 1
+// offsets), as the reference's cmg::simplify::simplify. Throws std::invalid_argument
+// with the reference's message on invalid input.
+void simplify(const double* pts, int64_t npts, const int* fidx, int64_t nidx, const size_t* foff,
+              int64_t nfacets, int grid, std::vector<double>& out_pts, std::vector<int>& out_tris,
+              cudaStream_t st);
+// Device times of the last simplify: host-to-device copy, clustering, device-to-host copy.
+void simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms);
+
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);
 

@@ -106,6 +106,14 @@ cmg_status cmg_read_points(const char* path, cmg_plc** out, char* errbuf, size_t
 cmg_status cmg_read_mesh(const char* path, cmg_mesh** out, char* errbuf, size_t len);
 cmg_status cmg_write_mesh(const char* path, const cmg_mesh*, char* errbuf, size_t len);
 cmg_status cmg_write_plc(const char* path, const cmg_plc*, char* errbuf, size_t len);
+/* Replaces cmg_plc_simplify (bindings/c/src/cmg_c.cpp:222-240 over
+ * src/simplify/simplify.cpp:48-112): grid vertex clustering on the GPU with the
+ * reference's cells, representative numbering (first vertex order), centroids (sums
+ * in vertex order, bit for bit) and triangle order; degenerate and repeated
+ * triangles dropped. Errors as the reference's ("simplify: PLC has no points",
+ * "simplify: grid must be >= 1", "simplify: degenerate (zero-extent) surface"), plus
+ * "simplify: non-finite point coordinate" and "simplify: facet vertex index out of
+ * range" where the reference's behaviour is undefined. */
 cmg_status cmg_plc_simplify(const cmg_plc*, int grid, cmg_plc** out, char* errbuf,
                             size_t errbuf_len);
 

@@ -94,6 +94,10 @@ cmg_status cmg_plc_from_stl(const void* data, size_t size, cmg_plc** out, char* 
  * of the points and triangles. */
 cmg_status cmg_stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
 
+/* Phase times (CUDA events) of the last cmg_plc_simplify on the current device:
+ * upload of points and facets, clustering kernels, download of the result. */
+cmg_status cmg_simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms);
+
 /* ---- self-intersections ------------------------------------------------------ */
 /* Replaces cmg::detect::self_intersections (src/detect/self_intersection.cpp:150-188):
  * every facet polygon flattened into a fan (v0, v[i-1], v[i]) in facet order; the pairs

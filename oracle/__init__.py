@@ -237,6 +237,24 @@ class Oracle:
                                       ctypes.c_int64(len(tris)), _ptr(out, _i64p), ctypes.c_int64(n))
         return out[:n]
 
+    def simplify(self, pts, tris, grid):
+        """Grid vertex clustering restated: (points (r,3), triangles (m,3) int32, error)
+        with error "" on success (points and triangles None on error)."""
+        pts = _f64(pts).reshape(-1, 3)
+        tris = _i32(tris).reshape(-1, 3)
+        f = self.L.orc_simplify
+        f.restype = ctypes.c_int64
+        op = np.zeros((max(len(pts), 1), 3))
+        ot = np.zeros((max(len(tris), 1), 3), dtype=np.int32)
+        m = ctypes.c_int64()
+        err = ctypes.create_string_buffer(256)
+        r = f(_ptr(pts, _dp), ctypes.c_int64(len(pts)), _ptr(tris, _ip), ctypes.c_int64(len(tris)),
+              ctypes.c_int(int(grid)), _ptr(op, _dp), _ptr(ot, _ip), ctypes.byref(m), err,
+              ctypes.c_size_t(256))
+        if r < 0:
+            return None, None, err.value.decode()
+        return op[:r].copy(), ot[:m.value].copy(), ""
+
     def stream(self, kind, soa, mode=COMPAT, threads=None):
         """Signs of n queries; soa is a (12|15, n) float64 array."""
         soa = _f64(soa)
@@ -394,6 +412,24 @@ class Reference:
         f(_ptr(pts, _dp), ctypes.c_longlong(len(pts)), _ptr(tris, _ip), ctypes.c_longlong(len(tris)),
           _ptr(out, _ip), ctypes.c_longlong(n))
         return out[:n]
+
+    def simplify(self, pts, tris, grid):
+        """The reference's simplify on a PLC of one triangle per facet: (points,
+        triangles, error) as Oracle.simplify."""
+        pts = _f64(pts).reshape(-1, 3)
+        tris = _i32(tris).reshape(-1, 3)
+        f = self.L.ref_simplify
+        f.restype = ctypes.c_longlong
+        op = np.zeros((max(len(pts), 1), 3))
+        ot = np.zeros((max(len(tris), 1), 3), dtype=np.int32)
+        m = ctypes.c_longlong()
+        err = ctypes.create_string_buffer(256)
+        r = f(_ptr(pts, _dp), ctypes.c_longlong(len(pts)), _ptr(tris, _ip), ctypes.c_longlong(len(tris)),
+              ctypes.c_int(int(grid)), _ptr(op, _dp), ctypes.c_longlong(len(op)), _ptr(ot, _ip),
+              ctypes.c_longlong(len(ot)), ctypes.byref(m), err, ctypes.c_longlong(256))
+        if r < 0:
+            return None, None, err.value.decode()
+        return op[:r].copy(), ot[:m.value].copy(), ""
 
     def pred(self, name, *pts):
         args = [_f64(p) for p in pts]

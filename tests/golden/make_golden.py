@@ -165,6 +165,61 @@ def detect_case(ref, manifest):
                           "contacts) with the reference's self_intersections rows")
 
 
+def simplify_cases():
+    """(name, points, triangles, grid) of the simplify fixtures."""
+    cases = []
+    # the reference tests' UV spheres at their grids (tests/test_simplify.cpp:138-174)
+    for (n, g) in ((24, 8), (20, 10), (28, 8), (28, 24), (8, 0)):
+        p, t = W.uv_sphere(1.0, n, n)
+        cases.append((f"uvsphere{n}_g{g}", p, t, g))
+    p, t = W.jittered_icosphere(3, 0.02, seed=5)
+    for g in (1, 3, 34):
+        cases.append((f"icosphere_g{g}", p, t, g))
+    p, t = W.sh_sphere(nlon=64, nlat=32, seed=4)
+    cases.append(("shsphere64_g34", p, t, 34))
+    # vertices on cell boundaries, signed zeros, collapsed triangles
+    q = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [-0.0, 0.5, 0.25],
+                  [0.5, -0.0, 0.75], [0.25, 0.25, 0.25]], float)
+    tq = np.array([[0, 1, 2], [0, 2, 3], [0, 3, 1], [1, 2, 3], [4, 5, 6], [0, 4, 5]])
+    for g in (2, 4):
+        cases.append((f"boundaries_g{g}", q, tq, g))
+    # repeated triangles, also reversed: the first occurrence's orientation is kept
+    p, t = W.jittered_icosphere(2, 0.01, seed=6)
+    cases.append(("repeats_g6", p, np.vstack([t, t[::-1, ::-1], t[:17]]), 6))
+    # 64-bit key wrap: with grid 2^22 the cells ix and ix + 2^20 share a key
+    w = np.array([[0, 0, 0], [0.25, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    cases.append(("wrap_g4194304", w, np.array([[0, 1, 2], [1, 2, 3], [0, 2, 3]]), 1 << 22))
+    cases.append(("icosphere_gmax", *W.jittered_icosphere(2, 0.01, seed=7), 2 ** 31 - 1))
+    rng = np.random.default_rng(23)
+    soup = np.round(rng.normal(size=(300, 3)) * 8) / 8
+    cases.append(("quantized_soup_g7", soup, rng.integers(0, 300, size=(500, 3)), 7))
+    cases.append(("points_only_g5", rng.random((40, 3)), np.zeros((0, 3), np.int32), 5))
+    cases.append(("no_points", np.zeros((0, 3)), np.zeros((0, 3), np.int32), 8))
+    cases.append(("grid_negative", q, tq, -3))
+    cases.append(("flat", np.ones((5, 3)), np.array([[0, 1, 2]]), 4))
+    return cases
+
+
+def simplify_case(ref, manifest):
+    out = {}
+    names = []
+    for name, pts, tris, g in simplify_cases():
+        rp, rt, err = ref.simplify(pts, tris, g)
+        out[name + "_points"] = np.asarray(pts, float).reshape(-1, 3)
+        out[name + "_triangles"] = np.asarray(tris, np.int32).reshape(-1, 3)
+        out[name + "_grid"] = np.array(g, np.int64)
+        out[name + "_error"] = np.array(err)
+        out[name + "_out_points"] = rp if rp is not None else np.zeros((0, 3))
+        out[name + "_out_triangles"] = rt if rt is not None else np.zeros((0, 3), np.int32)
+        names.append(name)
+    out["names"] = np.array(names)
+    save("simplify", **out)
+    manifest["simplify"] = ("grid vertex clustering (the reference tests' UV spheres at their grids, "
+                            "icospheres at grids 1/3/34/2^31-1, cell boundaries and signed zeros, "
+                            "repeated and reversed triangles, 64-bit key wrap, errors) with the "
+                            "reference's simplify output")
+
+
 def stl_case(ref, manifest):
     out = {}
     tmp = os.path.join(ROOT, "oracle", "_ref", "stl_fixture.stl")
@@ -241,6 +296,8 @@ def main():
         stl_case(ref, manifest)
     if want("detect"):
         detect_case(ref, manifest)
+    if want("simplify"):
+        simplify_case(ref, manifest)
     manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
 
     with open(path, "w") as f:

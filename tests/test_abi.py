@@ -89,6 +89,27 @@ def test_empty_plc_is_invalid_input(lib):
         lib.cmg_plc_destroy(plc)
 
 
+def test_simplify_validation(lib):
+    # simplify.cpp:49-54: no points, then grid < 1 -> InvalidInput, answered before any
+    # GPU work
+    from cybermeshgenerator_gb300 import _lib as L
+    plc = lib.cmg_plc_create()
+    out = ctypes.c_void_p(123)
+    err = ctypes.create_string_buffer(128)
+    try:
+        assert lib.cmg_plc_simplify(None, 8, ctypes.byref(out), err, 128) == 1
+        assert out.value is None
+        assert lib.cmg_plc_simplify(plc, 0, ctypes.byref(out), err, 128) == 1
+        assert err.value == b"simplify: PLC has no points"
+        pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], dtype=np.float64)
+        lib.cmg_plc_set_points(plc, pts.ctypes.data_as(L.c_double_p), 3)
+        assert lib.cmg_plc_simplify(plc, 0, ctypes.byref(out), err, 128) == 1
+        assert err.value == b"simplify: grid must be >= 1"
+        assert lib.cmg_plc_simplify(plc, 8, None, err, 128) == 1
+    finally:
+        lib.cmg_plc_destroy(plc)
+
+
 def test_facet_validation_and_readback(lib):
     from cybermeshgenerator_gb300 import _lib as L
     plc = lib.cmg_plc_create()

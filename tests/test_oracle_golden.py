@@ -167,3 +167,41 @@ def test_self_intersections_match_reference(orc, golden):
         got = orc.self_intersections(g[name + "_points"], g[name + "_triangles"])
         want = g[name + "_hits"]
         assert np.array_equal(got, want[:, :2].astype(np.int64)), name
+
+
+def test_simplify_matches_reference(orc, golden):
+    """The simplify restatement against the reference's simplify on every fixture:
+    representative points bit for bit, kept triangles in order, errors."""
+    g = golden("simplify")
+    for name in g["names"]:
+        name = str(name)
+        pts, tri, err = orc.simplify(g[name + "_points"], g[name + "_triangles"], int(g[name + "_grid"]))
+        assert err == str(g[name + "_error"]), name
+        if err:
+            continue
+        assert np.array_equal(pts.view(np.uint64), g[name + "_out_points"].view(np.uint64)), name
+        assert np.array_equal(tri, g[name + "_out_triangles"]), name
+
+
+def test_simplify_reference_properties(golden):
+    """The reference tests' own checks on its fixtures (tests/test_simplify.cpp:138-174):
+    a coarser surface enclosing nearly the same volume, fewer triangles at a coarser
+    grid."""
+    g = golden("simplify")
+
+    def volume(p, t):
+        a, b, c = p[t[:, 0]], p[t[:, 1]], p[t[:, 2]]
+        return abs(np.einsum("ij,ij->i", a, np.cross(b, c)).sum()) / 6.0
+
+    p, t = g["uvsphere24_g8_points"], g["uvsphere24_g8_triangles"]
+    q, u = g["uvsphere24_g8_out_points"], g["uvsphere24_g8_out_triangles"]
+    assert 0 < len(u) < len(t)
+    assert abs(volume(q, u) - volume(p, t)) / volume(p, t) < 0.15
+    assert len(g["uvsphere28_g8_out_triangles"]) <= len(g["uvsphere28_g24_out_triangles"])
+    # every kept triangle has three distinct corners and no sorted triple repeats
+    for name in g["names"]:
+        name = str(name)
+        u = g[name + "_out_triangles"]
+        if len(u):
+            assert np.all((u[:, 0] != u[:, 1]) & (u[:, 1] != u[:, 2]) & (u[:, 0] != u[:, 2]))
+            assert len(np.unique(np.sort(u, axis=1), axis=0)) == len(u)
