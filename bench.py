@@ -1061,6 +1061,134 @@ def ref_simplify(args):
                                base, len(tris))), flush=True)
 
 
+SIZING_METRIC = "queries/s, background sizing field (663,552-tetrahedron field, 1e7 queries)"
+SIZING_TEST_FLOPS = 96  # one containment test: four orient3d determinants (23 flops) + four divides
+
+
+def _sizing_workload(n=10_000_000):
+    """A 48^3-cell Kuhn background mesh of the unit cube (663,552 tetrahedra, 117,649
+    nodes, interior nodes jittered by 0.3 cells) with random node sizes, and n queries:
+    half uniform over the box grown by 10 % per side (about 42 % of those outside the
+    mesh), the rest on nodes, edge midpoints and face centroids."""
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(48, 0.3, seed=11)
+    S = np.random.default_rng(11).uniform(0.01, 0.2, len(P))
+    Q = W.sizing_queries(P, T, n, seed=12)
+    return P, T, S, Q
+
+
+def _sizing_cpu(P, T, S, Q, seconds, threads=None):
+    """The oracle's restatement of the reference's closure (a scan of every tetrahedron
+    per query) on all host threads, over a random sample of the queries sized to the
+    budget: queries/s."""
+    import oracle
+    orc = oracle.Oracle()
+    rng = np.random.default_rng(5)
+    m = 64
+    while True:
+        idx = rng.choice(len(Q), m, replace=False)
+        t0 = time.perf_counter()
+        orc.sizing(P, T, S, 1.0, Q[idx], threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > seconds / 4 or m >= len(Q):
+            return m / dt, m, orc.threads(threads)
+        m = int(min(len(Q), m * max(2.0, seconds / max(dt, 1e-3) / 2)))
+
+
+def run_sizing(args):
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import build as B
+    if rank == 0 or world == 1:
+        B.build()
+    barrier(world)
+    P, T, S, Q = _sizing_workload()
+    n = len(Q)
+    t0 = time.perf_counter()
+    field = cm.SizingField(P, T, S, 1.0)
+    build_s = time.perf_counter() - t0
+    dq = torch.from_numpy(Q).cuda()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        field.eval(dq)
+    torch.cuda.synchronize()
+    l0 = cm.gpu_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier(world)
+    with Clocks(local) as clk:
+        for a, b in ev:
+            a.record(stream)
+            out = field.eval(dq)
+            b.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    launches = (cm.gpu_launches() - l0) // args.steps
+    dev_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = max_over_ranks(sum(dev_ms), world)
+    value = n * world * args.steps / (total_ms * 1e-3)
+    st = field.stats()
+    config = {"workload": f"background sizing field of a 48^3-cell Kuhn mesh ({len(T)} "
+                          f"tetrahedra, {len(P)} nodes) at {n} queries (half uniform over the "
+                          "box grown by 10 %, half on nodes, edge midpoints and face centroids); "
+                          "value from the device evaluation (queries resident in HBM), e2e "
+                          "through cmg_sizing_eval with host arrays",
+              "tetrahedra": int(len(T)), "nodes": int(len(P)), "queries": int(n),
+              "inside": int(st["inside"]), "nearest": int(st["nearest"]), "slow": int(st["slow"]),
+              "global_tets": int(st["global_tets"]), "cell_entries": int(st["binned_pairs"]),
+              "build_s": build_s, "l2": "inputs larger than L2",
+              "parallelism": f"replicas x{world}"}
+    line = _base_line(SIZING_METRIC, "queries/s", value, world, args, total_ms, "fp64",
+                      config, launches, clk.summary())
+    if rank == 0:
+        p64 = cm.peak_flops(True)
+        flops = st["tests"] * SIZING_TEST_FLOPS
+        ms = sum(dev_ms) / len(dev_ms)
+        ach, frac = fraction_of_peak(flops, ms, p64)
+        line["roofline"] = {"bound": "fp64", "kernel": "k_sizing_eval (+ k_sizing_slow)",
+                            "achieved": ach / 1e12, "peak": p64 / 1e12, "unit": "TFLOP/s",
+                            "frac": frac, "traffic": None,
+                            "tests_per_query": st["tests"] / n,
+                            "candidates_per_query": st["candidates"] / n,
+                            "work": f"{SIZING_TEST_FLOPS} flops per full containment test "
+                                    "(four orient3d determinants + four divides), tests counted "
+                                    "on the device",
+                            "peak_source": "measured DFMA microbenchmark (FMA = 2 flops)"}
+        wall = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            host = field.eval(Q)
+            wall.append(time.perf_counter() - t0)
+        assert np.array_equal(host.view(np.uint64), out.cpu().numpy().view(np.uint64))
+        line["e2e"] = {"value": n / (sum(wall) / len(wall)), "unit": "queries/s",
+                       "h2d_bytes_per_step": int(Q.nbytes), "d2h_bytes_per_step": int(8 * n),
+                       "call": "cmg_sizing_eval (host queries -> host sizes)",
+                       "phase_ms": {k: field.stats()[k] for k in ("upload_ms", "eval_ms", "download_ms")}}
+        if not args.no_cpu:
+            v, m, th = _sizing_cpu(P, T, S, Q, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": "queries/s", "cores": th, "kind": "port",
+                                    "sample": f"{m} random queries of the workload, each scanning "
+                                              "the tetrahedra in order as the reference's closure"}
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def ref_sizing(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    P, T, S, Q = _sizing_workload()
+    v, m, th = _sizing_cpu(P, T, S, Q, max(10.0, args.cpu_seconds))
+    base = {"value": v, "unit": "queries/s", "cores": th, "kind": "port",
+            "sample": f"{m} random queries of the workload"}
+    print(json.dumps(_ref_line(SIZING_METRIC, "queries/s", v, args,
+                               {"workload": "background sizing field, 663,552 tetrahedra",
+                                "parallelism": "cpu threads"}, base, len(Q))), flush=True)
+
+
 def _ref_line(metric, unit, value, args, config, base, units_per_step):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
@@ -1125,18 +1253,19 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="sdf",
-                    choices=["sdf", "batch", "scale", "stream", "stl", "detect", "simplify"])
+                    choices=["sdf", "batch", "scale", "stream", "stl", "detect", "simplify",
+                             "sizing"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         {"sdf": run_reference, "batch": ref_batch, "scale": ref_scale,
          "stream": ref_stream, "stl": ref_stl, "detect": ref_detect,
-         "simplify": ref_simplify}[args.workload](args)
+         "simplify": ref_simplify, "sizing": ref_sizing}[args.workload](args)
     else:
         {"sdf": run_ours, "batch": run_batch, "scale": run_scale,
          "stream": run_stream, "stl": run_stl, "detect": run_detect,
-         "simplify": run_simplify}[args.workload](args)
+         "simplify": run_simplify, "sizing": run_sizing}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -188,6 +188,74 @@ def simplify_last_timing() -> Dict[str, float]:
     return {"upload_ms": a.value, "cluster_ms": b.value, "download_ms": c.value}
 
 
+class SizingField:
+    """The background-mesh sizing field of the reference's
+    ``cmg::sizing::from_background(mesh, node_sizes, scale)``
+    (src/sizing/background.cpp:58-74) on the GPU: ``field(p)`` is the closure's value at
+    one point, ``field.eval(queries)`` at many ((n, 3) NumPy array, or a CUDA float64
+    torch tensor evaluated on the current stream), bit for bit the reference's: the
+    sizes interpolated in the first tetrahedron (in order) that contains the point,
+    else the nearest node's, times ``scale``. ``tets`` holds 4 node indices per row;
+    ``node_sizes`` is padded with 0 or truncated to the node count."""
+
+    def __init__(self, points, tets, node_sizes, scale: float = 1.0) -> None:
+        P = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        T = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1, 4)
+        S = np.ascontiguousarray(node_sizes, dtype=np.float64).ravel()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        self._h = None
+        _check(_clib.cmg_sizing_create(P.ctypes.data_as(_L.c_double_p), len(P),
+                                       T.ctypes.data_as(_L.c_int_p), len(T),
+                                       S.ctypes.data_as(_L.c_double_p), len(S), float(scale),
+                                       ctypes.byref(h), err, 256), err)
+        self._h = h.value
+
+    def eval(self, queries, which: bool = False):
+        """Sizes at the queries; with ``which``, also the answering tetrahedron per query
+        (-1: the nearest node's size)."""
+        err = ctypes.create_string_buffer(256)
+        try:
+            import torch
+            is_tensor = isinstance(queries, torch.Tensor)
+        except ImportError:
+            is_tensor = False
+        if is_tensor:
+            if not queries.is_cuda or queries.dtype != torch.float64:
+                raise TypeError("queries must be a CUDA float64 tensor")
+            q = queries.reshape(-1, 3).contiguous()
+            n = q.shape[0]
+            out = torch.empty(n, dtype=torch.float64, device=q.device)
+            w = torch.empty(n, dtype=torch.int32, device=q.device) if which else None
+            st = torch.cuda.current_stream(q.device).cuda_stream
+            _check(_clib.cmg_sizing_eval_device(self._h, q.data_ptr(), n, out.data_ptr(),
+                                                w.data_ptr() if which else None, st, err, 256), err)
+            return (out, w) if which else out
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 3)
+        out = np.empty(len(q))
+        w = np.empty(len(q), dtype=np.int32) if which else None
+        _check(_clib.cmg_sizing_eval(self._h, q.ctypes.data_as(_L.c_double_p), len(q),
+                                     out.ctypes.data_as(_L.c_double_p),
+                                     w.ctypes.data_as(_L.c_int_p) if which else None, err, 256), err)
+        return (out, w) if which else out
+
+    def __call__(self, p) -> float:
+        return float(self.eval(np.asarray(p, dtype=np.float64).reshape(1, 3))[0])
+
+    def stats(self) -> Dict[str, float]:
+        s = _L.SizingStats()
+        _check(_clib.cmg_sizing_get_stats(self._h, ctypes.byref(s)), ctypes.create_string_buffer(1))
+        return s.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _clib.cmg_sizing_destroy(self._h)
+            self._h = None
+
+    def __del__(self) -> None:
+        self.close()
+
+
 @dataclass
 class VoxelGrid:
     """A regular grid from :func:`voxelize`: ``grid`` is (nx, ny, nz), uint8
@@ -486,6 +554,20 @@ def orient3d_signs(points, tets) -> np.ndarray:
     return out
 
 
+def orient3d_batch(points, tets) -> np.ndarray:
+    """robust::orient3d_batch on the GPU: the orient3d value of each candidate
+    tetrahedron (tets (M, 4) indices into points (N, 3)), bit for bit the reference's."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    t = np.ascontiguousarray(tets, dtype=np.int32)
+    out = np.zeros(len(t))
+    st = _clib.cmg_orient3d_batch(pts.ctypes.data_as(_L.c_double_p), len(pts),
+                                  t.ctypes.data_as(_L.c_int_p), len(t),
+                                  out.ctypes.data_as(_L.c_double_p))
+    if st != 0:
+        raise RuntimeError(f"cmg_orient3d_batch failed with status {st}")
+    return out
+
+
 def gpu_launches() -> int:
     """Kernels launched by the library in this process."""
     return int(_clib.cmg_gpu_launches())
@@ -511,8 +593,8 @@ def library_path() -> str:
     return _L.library_path()
 
 
-__all__ = ["orient3d_stream", "insphere_stream", "orient3d_signs", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
+__all__ = ["orient3d_stream", "insphere_stream", "orient3d_signs", "orient3d_batch", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
            "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
            "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT",
            "read_plc", "plc_from_stl", "self_intersections", "simplify", "stl_last_timing",
-           "simplify_last_timing"]
+           "simplify_last_timing", "SizingField"]

@@ -71,6 +71,17 @@ class PredStats(ctypes.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class SizingStats(ctypes.Structure):
+    _fields_ = [("binned_pairs", ctypes.c_int64), ("global_tets", ctypes.c_int64),
+                ("inside", ctypes.c_int64), ("nearest", ctypes.c_int64), ("slow", ctypes.c_int64),
+                ("tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
+                ("upload_ms", ctypes.c_float), ("eval_ms", ctypes.c_float),
+                ("download_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def library_path() -> str:
     return os.environ.get("CMG_C_LIB") or IN_TREE
 
@@ -98,6 +109,12 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_intersections_data", c_int_p, [V])
     sig("cmg_intersections_destroy", None, [V])
     sig("cmg_self_intersections_last_ms", ctypes.c_float, [])
+    sig("cmg_sizing_create", I, [c_double_p, ctypes.c_int64, c_int_p, ctypes.c_int64, c_double_p,
+                                 ctypes.c_int64, D, ctypes.POINTER(V), S, Z])
+    sig("cmg_sizing_eval", I, [V, c_double_p, ctypes.c_int64, c_double_p, c_int_p, S, Z])
+    sig("cmg_sizing_eval_device", I, [V, V, ctypes.c_int64, V, V, V, S, Z])
+    sig("cmg_sizing_get_stats", I, [V, ctypes.POINTER(SizingStats)])
+    sig("cmg_sizing_destroy", None, [V])
     F = ctypes.POINTER(ctypes.c_float)
     sig("cmg_stl_last_timing", I, [F, F, F])
     sig("cmg_simplify_last_timing", I, [F, F, F])
@@ -162,6 +179,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     for n in ("cmg_orient3d_stream", "cmg_insphere_stream"):
         sig(n, I, [ctypes.POINTER(V), ctypes.c_int64, I, I, V, ctypes.POINTER(PredStats), V, S, Z])
     sig("cmg_orient3d_signs", I, [c_double_p, I, c_int_p, I, c_int_p])
+    sig("cmg_orient3d_batch", I, [c_double_p, I, c_int_p, I, c_double_p])
     sig("cmg_gpu_occupancy_static", I, [V, ctypes.c_int64, V, ctypes.c_int64, c_double_p, D,
                                         c_int_p, I, V, V, S, Z])
     # differentiable signed distance

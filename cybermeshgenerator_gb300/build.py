@@ -23,7 +23,9 @@ BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(HERE, "libcmg_c.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["scan.cu", "occupancy.cu", "sdf.cu", "sdf_sub.cu", "engine.cu", "peak.cu", "noalloc.cu", "predicates.cu", "adjoint.cu", "stl.cu", "detect.cu", "simplify.cu"]
+CU_SOURCES = ["scan.cu", "occupancy.cu", "sdf.cu", "sdf_sub.cu", "engine.cu", "peak.cu", "noalloc.cu", "predicates.cu", "adjoint.cu", "stl.cu", "detect.cu", "simplify.cu", "sizing.cu"]
+# per-file flags: sizing.cu rounds every product and sum separately, as the reference does
+CU_FLAGS = {"sizing.cu": ["-fmad=false"]}
 CXX_SOURCES = ["cmg_c.cpp"]
 
 
@@ -64,8 +66,8 @@ def build(jobs: int | None = None, verbose: bool = False) -> str:
         s, o = os.path.join(CSRC, src), os.path.join(BUILD, src + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
-            steps.append([nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                          "-Xcompiler", "-ffp-contract=off", "-c", s, "-o", o])
+            steps.append([nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", *CU_FLAGS.get(src, []),
+                          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-c", s, "-o", o])
     for src in CXX_SOURCES:
         s, o = os.path.join(CSRC, src), os.path.join(BUILD, src + ".o")
         objs.append(o)

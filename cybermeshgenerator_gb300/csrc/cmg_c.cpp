@@ -975,6 +975,95 @@ cmg_status cmg_simplify_last_timing(float* upload_ms, float* cluster_ms, float* 
     return CMG_OK;
 }
 
+// ------------------------------------------------------------------ sizing field
+struct cmg_sizing {
+    cmg::gpu::SizingField* f = nullptr;
+    ~cmg_sizing() {
+        if (f) cmg::gpu::sizing_destroy(f);
+    }
+};
+
+// from_background (src/sizing/background.cpp:58-74): the closure's data moved to the
+// device once; evaluations run in batches.
+cmg_status cmg_sizing_create(const double* points, int64_t npoints, const int* tets, int64_t ntets,
+                             const double* node_sizes, int64_t nsizes, double scale,
+                             cmg_sizing** out, char* errbuf, size_t len) {
+    if (out) *out = nullptr;
+    if (!out || npoints < 0 || ntets < 0 || nsizes < 0 || (npoints && !points) ||
+        (ntets && !tets) || (nsizes && !node_sizes))
+        return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        // inputs whose behaviour is undefined in the reference, refused before any device work
+        for (int64_t i = 0; i < 3 * npoints; ++i)
+            if (!std::isfinite(points[i]))
+                throw CoreError{CMG_ERR_INVALID_INPUT, "sizing: non-finite background point"};
+        for (int64_t k = 0; k < 4 * ntets; ++k)
+            if (tets[k] < 0 || tets[k] >= npoints)
+                throw CoreError{CMG_ERR_INVALID_INPUT, "sizing: tetrahedron vertex index out of range"};
+        std::unique_ptr<cmg_sizing> s(new cmg_sizing);
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        s->f = cmg::gpu::sizing_create(points, npoints, tets, ntets, node_sizes, nsizes, scale,
+                                       gpu_stream());
+        *out = s.release();
+    });
+}
+
+cmg_status cmg_sizing_eval(cmg_sizing* s, const double* queries, int64_t n, double* out, int* which,
+                           char* errbuf, size_t len) {
+    if (!s || n < 0 || (n && (!queries || !out))) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cmg::gpu::sizing_eval_host(s->f, queries, n, out, which, gpu_stream());
+    });
+}
+
+cmg_status cmg_sizing_eval_device(cmg_sizing* s, const double* d_queries, int64_t n, double* d_out,
+                                  int* d_which, void* stream, char* errbuf, size_t len) {
+    if (!s || n < 0 || (n && (!d_queries || !d_out))) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cmg::gpu::sizing_eval_device(s->f, d_queries, n, d_out, d_which,
+                                     static_cast<cudaStream_t>(stream));  // NULL: the default stream
+    });
+}
+
+cmg_status cmg_sizing_get_stats(cmg_sizing* s, cmg_sizing_stats* out) {
+    if (!s || !out) return CMG_ERR_INVALID_INPUT;
+    try {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        const cmg::gpu::SizingStats r = cmg::gpu::sizing_stats(s->f, gpu_stream());
+        out->binned_pairs = r.binned_pairs;
+        out->global_tets = r.global_tets;
+        out->inside = r.inside;
+        out->nearest = r.nearest;
+        out->slow = r.slow;
+        out->tests = r.tests;
+        out->candidates = r.candidates;
+        out->upload_ms = r.upload_ms;
+        out->eval_ms = r.eval_ms;
+        out->download_ms = r.download_ms;
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
+void cmg_sizing_destroy(cmg_sizing* s) { delete s; }
+
+cmg_status cmg_orient3d_batch(const double* xyz, int npts, const int* tets, int n, double* out_value) {
+    if (n <= 0) return CMG_OK;
+    if (!xyz || !tets || !out_value || npts <= 0) return CMG_ERR_INVALID_INPUT;
+    for (int64_t i = 0; i < 4 * static_cast<int64_t>(n); ++i)
+        if (tets[i] < 0 || tets[i] >= npts) return CMG_ERR_INVALID_INPUT;
+    try {
+        std::lock_guard<std::mutex> lk(gpu_mutex());
+        cmg::gpu::orient3d_batch(xyz, npts, tets, n, out_value, gpu_stream());
+    } catch (...) {
+        return CMG_ERR_INTERNAL;
+    }
+    return CMG_OK;
+}
+
 const char* cmg_version(void) { return "0.5.0"; }
 
 }  // extern "C"

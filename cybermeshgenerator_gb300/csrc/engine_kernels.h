@@ -107,6 +107,32 @@ void simplify(const double* pts, int64_t npts, const int* fidx, int64_t nidx, co
 // Device times of the last simplify: host-to-device copy, clustering, device-to-host copy.
 void simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms);
 
+// sizing.cu: the background sizing field (cmg::sizing::from_background) as a device
+// object evaluated for batches of queries with the reference's results bit for bit.
+struct SizingField;
+struct SizingStats {
+    int64_t binned_pairs = 0, global_tets = 0;           // construction
+    int64_t inside = 0, nearest = 0, slow = 0;           // last evaluation: answers by kind
+    int64_t tests = 0, candidates = 0;                   // full tests, candidates seen
+    float upload_ms = 0.f, eval_ms = 0.f, download_ms = 0.f;  // last host evaluation
+};
+// Throws std::invalid_argument on a non-finite node or an index outside the nodes.
+SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64_t nt,
+                           const double* sizes, int64_t ns, double scale, cudaStream_t st);
+void sizing_destroy(SizingField* f);
+// q: 3 n device doubles; out: n device doubles; which (may be null): the answering
+// tetrahedron per query, or -1 for the nearest node. Asynchronous on st.
+void sizing_eval_device(SizingField* f, const double* q, int64_t n, double* out, int* which,
+                        cudaStream_t st);
+// Host arrays: copies in, evaluates, copies out (synchronous).
+void sizing_eval_host(SizingField* f, const double* q, int64_t n, double* out, int* which,
+                      cudaStream_t st);
+SizingStats sizing_stats(SizingField* f, cudaStream_t st);
+// robust::orient3d_batch (host arrays, synchronous): the orient3d value of each of n
+// candidate tetrahedra (4 indices into pts each).
+void orient3d_batch(const double* pts, int64_t np, const int* tets, int64_t n, double* out,
+                    cudaStream_t st);
+
 // peak.cu: FMA throughput (FLOP/s, FMA = 2) of the current device.
 double peak_flops(bool fp64);
 

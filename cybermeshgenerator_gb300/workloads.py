@@ -475,3 +475,50 @@ def stl_ascii(points, triangles, fmt: str = "{:.9g}", crlf: bool = False,
             out.append("   ")
     out.append("endsolid cmg")
     return (nl.join(out) + nl).encode()
+
+
+def kuhn_tet_mesh(n: int = 8, jitter: float = 0.0, seed: int = 1, lo=(0.0, 0.0, 0.0),
+                  side: float = 1.0):
+    """A conforming background tetrahedral mesh of the cube [lo, lo + side]^3: an n^3 grid
+    of cells, each split into the six Kuhn tetrahedra around its main diagonal (node
+    (i,j,k) -> (i+1,j+1,k+1) through one axis step at a time), interior nodes moved by up
+    to `jitter` cell sizes. Returns (points (N, 3) float64, tets (6 n^3, 4) int32)."""
+    rng = np.random.default_rng(seed)
+    g = np.arange(n + 1, dtype=np.float64) / n
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    if jitter > 0:
+        inner = np.all((pts > 0) & (pts < 1), axis=1)
+        pts[inner] += rng.uniform(-jitter, jitter, size=(int(inner.sum()), 3)) / n
+    pts = np.asarray(lo, dtype=np.float64) + side * pts
+    I, J, K = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    base = np.stack([I.ravel(), J.ravel(), K.ravel()], axis=1)          # cells in (i, j, k) order
+    step = np.eye(3, dtype=np.int64)
+    nid = lambda v: (v[:, 0] * (n + 1) + v[:, 1]) * (n + 1) + v[:, 2]
+    tets = np.empty((len(base), 6, 4), dtype=np.int32)
+    for p, perm in enumerate(((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0))):
+        a = base
+        b = a + step[perm[0]]
+        c = b + step[perm[1]]
+        d = c + step[perm[2]]
+        tets[:, p] = np.stack([nid(a), nid(b), nid(c), nid(d)], axis=1)
+    return pts, tets.reshape(-1, 4)
+
+
+def sizing_queries(points, tets, n: int, seed: int = 2, outside: float = 0.1):
+    """Queries for a background sizing field: uniform points over the mesh's box grown by
+    `outside` of its extent on every side (some fall outside the mesh and take the
+    nearest node's size), plus exact nodes, edge midpoints and face centroids (points
+    on shared faces, where the first tetrahedron in order must win)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = points.min(0), points.max(0)
+    ext = (hi - lo).max()
+    m = n // 2
+    q = [rng.uniform(lo - outside * ext, hi + outside * ext, size=(m, 3))]
+    k = (n - m) // 3
+    q.append(points[rng.integers(0, len(points), size=k)])
+    t = tets[rng.integers(0, len(tets), size=k)]
+    q.append(0.5 * (points[t[:, 0]] + points[t[:, 1]]))
+    t = tets[rng.integers(0, len(tets), size=n - m - 2 * k)]
+    q.append((points[t[:, 0]] + points[t[:, 1]] + points[t[:, 2]]) / 3.0)
+    return np.ascontiguousarray(np.vstack(q))

@@ -98,6 +98,36 @@ cmg_status cmg_stl_last_timing(float* upload_ms, float* merge_ms, float* downloa
  * upload of points and facets, clustering kernels, download of the result. */
 cmg_status cmg_simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms);
 
+/* ---- background sizing field ------------------------------------------------- */
+/* Replaces cmg::sizing::from_background (src/sizing/background.cpp:58-74), whose
+ * closure scans every tetrahedron per query: the background mesh (points, 4 indices per
+ * tetrahedron) and node sizes (padded with 0 or truncated to the node count) move to
+ * the GPU once; each evaluation returns, per query, the reference's closure value bit
+ * for bit: (w0 s0 + w1 s1 + w2 s2 + w3 s3) * scale in the first tetrahedron whose
+ * orient3d weights are all >= -1e-9, else the nearest node's size * scale. `which`
+ * (may be NULL) receives the answering tetrahedron or -1 (nearest node). Errors:
+ * "sizing: non-finite background point", "sizing: tetrahedron vertex index out of
+ * range" (undefined behaviour in the reference). */
+typedef struct cmg_sizing cmg_sizing;
+typedef struct cmg_sizing_stats {
+    int64_t binned_pairs, global_tets;  /* construction: cell entries, tetrahedra every query tests */
+    int64_t inside, nearest, slow;      /* last evaluation: answers in a tetrahedron, by the
+                                           nearest node; queries outside the binned domain */
+    int64_t tests, candidates;          /* full containment tests, candidates seen */
+    float upload_ms, eval_ms, download_ms;  /* last host evaluation (CUDA events) */
+} cmg_sizing_stats;
+cmg_status cmg_sizing_create(const double* points, int64_t npoints, const int* tets, int64_t ntets,
+                             const double* node_sizes, int64_t nsizes, double scale,
+                             cmg_sizing** out, char* errbuf, size_t errbuf_len);
+/* Host arrays (queries: 3 n doubles; out: n doubles; which: n ints or NULL). */
+cmg_status cmg_sizing_eval(cmg_sizing*, const double* queries, int64_t n, double* out, int* which,
+                           char* errbuf, size_t errbuf_len);
+/* Device arrays, asynchronous on `stream` (a cudaStream_t; NULL: the default stream). */
+cmg_status cmg_sizing_eval_device(cmg_sizing*, const double* d_queries, int64_t n, double* d_out,
+                                  int* d_which, void* stream, char* errbuf, size_t errbuf_len);
+cmg_status cmg_sizing_get_stats(cmg_sizing*, cmg_sizing_stats* out);
+void cmg_sizing_destroy(cmg_sizing*);
+
 /* ---- self-intersections ------------------------------------------------------ */
 /* Replaces cmg::detect::self_intersections (src/detect/self_intersection.cpp:150-188):
  * every facet polygon flattened into a fan (v0, v[i-1], v[i]) in facet order; the pairs
@@ -264,6 +294,10 @@ cmg_status cmg_insphere_stream(const double* const* coords, int64_t n, int mode,
  * tetrahedra tets[4*n] (indices into xyz), signs equal to the scalar
  * robust::orient3d's for every candidate, computed entirely on the GPU. */
 cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int n, int* out_sign);
+/* Replaces robust::orient3d_batch (src/predicates/robust.cpp:52-66): the orient3d
+ * VALUE of every candidate (the rounded determinant when it is not zero, else the
+ * adaptive routine's answer), bit for bit, computed on the GPU. */
+cmg_status cmg_orient3d_batch(const double* xyz, int npts, const int* tets, int n, double* out_value);
 
 /* ---- occupancy without allocation ----------------------------------------- */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc (a host

@@ -255,6 +255,32 @@ class Oracle:
             return None, None, err.value.decode()
         return op[:r].copy(), ot[:m.value].copy(), ""
 
+    def orient3d_values(self, soa):
+        """robust::orient3d values of n queries; soa is a (12, n) float64 array."""
+        soa = _f64(soa)
+        n = soa.shape[1]
+        rows = (_dp * 12)(*[_ptr(soa[i], _dp) for i in range(12)])
+        out = np.zeros(n)
+        self.L.orc_orient3d_values(rows, ctypes.c_int64(n), _ptr(out, _dp))
+        return out
+
+    def sizing(self, points, tets, sizes, scale, queries, threads=None):
+        """The background sizing field at the queries: (sizes (n,), answering tetrahedron
+        or -1 per query (n,) int64). Node sizes are padded with 0 or truncated to the
+        node count, as the reference does."""
+        P = _f64(points).reshape(-1, 3)
+        T = _i32(tets).reshape(-1, 4)
+        S = np.zeros(len(P))
+        sz = np.asarray(sizes, dtype=np.float64).ravel()[: len(P)]
+        S[: len(sz)] = sz
+        Q = _f64(queries).reshape(-1, 3)
+        out = np.zeros(len(Q))
+        which = np.zeros(len(Q), dtype=np.int64)
+        self.L.orc_sizing_eval(_ptr(P, _dp), ctypes.c_int64(len(P)), _ptr(T, _ip), ctypes.c_int64(len(T)),
+                               _ptr(S, _dp), ctypes.c_double(scale), _ptr(Q, _dp), ctypes.c_int64(len(Q)),
+                               _ptr(out, _dp), _ptr(which, _i64p), ctypes.c_int(self.threads(threads)))
+        return out, which
+
     def stream(self, kind, soa, mode=COMPAT, threads=None):
         """Signs of n queries; soa is a (12|15, n) float64 array."""
         soa = _f64(soa)
@@ -430,6 +456,20 @@ class Reference:
         if r < 0:
             return None, None, err.value.decode()
         return op[:r].copy(), ot[:m.value].copy(), ""
+
+    def sizing(self, points, tets, sizes, scale, queries):
+        """The reference's from_background closure evaluated at each query (sizes as
+        given: the reference pads or truncates them itself)."""
+        P = _f64(points).reshape(-1, 3)
+        T = _i32(tets).reshape(-1, 4)
+        S = _f64(np.asarray(sizes, dtype=np.float64).ravel())
+        Q = _f64(queries).reshape(-1, 3)
+        out = np.zeros(len(Q))
+        self.L.ref_sizing_eval(_ptr(P, _dp), ctypes.c_longlong(len(P)), _ptr(T, _ip),
+                               ctypes.c_longlong(len(T)), _ptr(S, _dp), ctypes.c_longlong(len(S)),
+                               ctypes.c_double(scale), _ptr(Q, _dp), ctypes.c_longlong(len(Q)),
+                               _ptr(out, _dp))
+        return out
 
     def pred(self, name, *pts):
         args = [_f64(p) for p in pts]

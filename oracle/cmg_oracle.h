@@ -57,6 +57,16 @@ typedef struct orc_occ_stats {
 enum { ORC_COMPAT = 0, ORC_EXACT = 1 };
 
 /* ---- predicates ---------------------------------------------------------- */
+/* robust::orient3d's value (sizing_oracle.c): the rounded determinant when it is not
+ * zero, else the adaptive routine's answer. */
+double orc_orient3d_value(const double* pa, const double* pb, const double* pc, const double* pd);
+void orc_orient3d_values(const double* const* soa, int64_t n, double* out);
+/* Background sizing field (sizing_oracle.c): sizes (np entries, already padded or
+ * truncated) interpolated in the first containing tetrahedron, else the nearest
+ * node's; which[q] = the answering tetrahedron or -1 (may be NULL). */
+void orc_sizing_eval(const double* P, int64_t np, const int* T, int64_t nt, const double* S,
+                     double scale, const double* Q, int64_t nq, double* out, int64_t* which,
+                     int nthreads);
 double orc_orient3d_fast(const double* pa, const double* pb, const double* pc,
                          const double* pd);
 double orc_insphere_fast(const double* pa, const double* pb, const double* pc,

@@ -220,6 +220,117 @@ def simplify_case(ref, manifest):
                             "reference's simplify output")
 
 
+def sizing_cases():
+    """(name, points, tets, node sizes, scale, queries) of the sizing-field fixtures."""
+    rng = np.random.default_rng(31)
+    specials = np.array([[np.nan, 0.5, 0.5], [np.inf, 0.5, 0.5], [-np.inf, 0, 0],
+                         [0.5, np.inf, -np.inf], [1e3, -2e3, 5e2], [40.0, 0.5, 0.5]])
+    cases = []
+    # the reference test's background: a cube of six tetrahedra, size 0.2 + 0.5 x
+    # (tests/test_sizing.cpp:85-108)
+    P, T = W.kuhn_tet_mesh(1)
+    S = 0.2 + 0.5 * P[:, 0]
+    Q = np.vstack([P, [[0.5, 0.5, 0.5]], W.sizing_queries(P, T, 300, seed=1), specials])
+    cases.append(("cube6", P, T, S, 1.0, Q))
+    cases.append(("cube6_half", P, T, np.full(len(P), 0.4), 0.5, Q[:40]))
+    P, T = W.kuhn_tet_mesh(3, 0.3, seed=4)
+    S = rng.uniform(0.05, 0.5, len(P))
+    cases.append(("kuhn3_jitter", P, T, S, 0.5, np.vstack([W.sizing_queries(P, T, 1500, seed=2), specials])))
+    # two overlapping meshes (non-conforming): in the overlap the first index answers
+    P1, T1 = W.kuhn_tet_mesh(2, 0.2, seed=5)
+    P2, T2 = W.kuhn_tet_mesh(2, 0.2, seed=6, lo=(0.3, 0.2, 0.1))
+    P = np.vstack([P1, P2])
+    T = np.vstack([T2 + len(P1), T1])
+    S = rng.uniform(0.1, 1.0, len(P))
+    cases.append(("overlap", P, T, S, 1.0, W.sizing_queries(P, T, 1200, seed=3)))
+    # slivers (four nearly coplanar nodes), a tiny tetrahedron and flat ones (D == 0)
+    P, T = W.kuhn_tet_mesh(2, 0.0, seed=1)
+    extra = np.array([[0.2, 0.2, 0.5], [0.8, 0.2, 0.5], [0.5, 0.8, 0.5], [0.5, 0.4, 0.5 + 1e-13],
+                      [0.31, 0.47, 0.53], [0.31 + 1e-7, 0.47, 0.53], [0.31, 0.47 + 1e-7, 0.53],
+                      [0.31, 0.47, 0.53 + 1e-7], [0.1, 0.1, 0.1], [0.9, 0.1, 0.1], [0.5, 0.9, 0.1]])
+    b = len(P)
+    P = np.vstack([P, extra])
+    T = np.vstack([[[b, b + 1, b + 2, b + 3]], [[b + 4, b + 5, b + 6, b + 7]],
+                   [[b + 8, b + 9, b + 10, b + 8]], [[b, b + 1, b + 2, b]], T])
+    S = rng.uniform(0.1, 1.0, len(P))
+    Q = np.vstack([W.sizing_queries(P, T, 800, seed=4), extra, (extra[:4].mean(0))[None],
+                   extra[4:8].mean(0)[None] + 1e-9])
+    cases.append(("slivers_flat", P, T, S, 1.0, Q))
+    # short and long size arrays
+    P, T = W.kuhn_tet_mesh(2, 0.1, seed=7)
+    Q = W.sizing_queries(P, T, 400, seed=5)
+    cases.append(("short_sizes", P, T, rng.uniform(0.1, 1.0, 10), 1.0, Q))
+    cases.append(("long_sizes", P, T, rng.uniform(0.1, 1.0, len(P) + 7), 1.0, Q))
+    # nearest-node ties: queries outside the mesh on its symmetry planes
+    P, T = W.kuhn_tet_mesh(2)
+    Q = np.array([[0.5, 0.5, 2.0], [0.25, 0.5, -1.0], [1.75, 0.5, 0.5], [0.5, -0.75, 0.25],
+                  [-1.0, -1.0, -1.0], [0.75, 1.5, 0.75]])
+    cases.append(("nearest_ties", P, T, np.arange(len(P), dtype=np.float64), 1.0, Q))
+    cases.append(("empty", np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros(0), 1.0,
+                  np.array([[0.2, 0.2, 0.0], [np.nan, 0, 0]])))
+    return cases
+
+
+def _o3_fast(a, b, c, d):
+    adx, ady, adz = a - d
+    bdx, bdy, bdz = b - d
+    cdx, cdy, cdz = c - d
+    return adz * (bdx * cdy - cdx * bdy) + bdz * (cdx * ady - adx * cdy) + cdz * (adx * bdy - bdx * ady)
+
+
+def o3_value_queries():
+    """(n, 4, 3) orient3d inputs whose rounded determinant is zero, reaching every stage
+    of the adaptive routine (points exactly on the plane z = x after large offsets, some
+    nudged by one ulp; nearly coplanar and collinear points), plus random ones."""
+    rng = np.random.default_rng(77)
+    out = []
+    while len(out) < 3000:
+        B = rng.normal(size=(4, 3))
+        k = len(out) % 3
+        if k == 0:
+            B[:, 2] = B[:, 0]
+            off = rng.choice([1e3, 1e6, 12345.678, 3e8, 1e12]) * rng.random()
+            B[:, 0] += off
+            B[:, 2] += off
+            B[:, 1] += rng.choice([0.0, off])
+            if rng.random() < 0.5:
+                i, j = rng.integers(0, 4), rng.integers(0, 3)
+                B[i, j] = np.nextafter(B[i, j], np.inf if rng.random() < 0.5 else -np.inf)
+        elif k == 1:
+            a_, b_ = rng.normal(size=2)
+            B[:, 2] = a_ * B[:, 0] + b_ * B[:, 1]
+            B += rng.choice([0.0, 1.0, 1e3, 0.1])
+        else:
+            B[3] = B[0] + rng.random() * (B[1] - B[0])
+            B += rng.choice([0.0, 1.0, 1e6])
+        if _o3_fast(*B) == 0.0:
+            out.append(B)
+    out += list(rng.normal(size=(500, 4, 3)))
+    return np.ascontiguousarray(np.array(out))
+
+
+def sizing_case(ref, manifest):
+    out = {}
+    names = []
+    for name, P, T, S, scale, Q in sizing_cases():
+        out[name + "_points"] = np.asarray(P, float).reshape(-1, 3)
+        out[name + "_tets"] = np.asarray(T, np.int32).reshape(-1, 4)
+        out[name + "_sizes"] = np.asarray(S, float)
+        out[name + "_scale"] = np.array(scale)
+        out[name + "_queries"] = np.asarray(Q, float).reshape(-1, 3)
+        out[name + "_values"] = ref.sizing(P, T, S, scale, Q)
+        names.append(name)
+    out["names"] = np.array(names)
+    Pq = o3_value_queries()
+    out["o3_points"] = Pq
+    out["o3_values"] = np.array([ref.pred("orient3d", *p) for p in Pq])
+    save("sizing", **out)
+    manifest["sizing"] = ("background sizing fields (the reference test's six-tetrahedron cube, a "
+                          "jittered mesh, overlapping meshes, slivers, a tiny and flat tetrahedra, "
+                          "short and long size arrays, nearest-node ties, far / NaN / infinite "
+                          "queries, an empty mesh) with the reference's closure values")
+
+
 def stl_case(ref, manifest):
     out = {}
     tmp = os.path.join(ROOT, "oracle", "_ref", "stl_fixture.stl")
@@ -298,6 +409,8 @@ def main():
         detect_case(ref, manifest)
     if want("simplify"):
         simplify_case(ref, manifest)
+    if want("sizing"):
+        sizing_case(ref, manifest)
     manifest["predicates"] = "4096 orient3d + 4096 insphere queries (25% exact-degenerate, 25% near)"
 
     with open(path, "w") as f:

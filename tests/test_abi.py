@@ -110,6 +110,27 @@ def test_simplify_validation(lib):
         lib.cmg_plc_destroy(plc)
 
 
+def test_sizing_validation(lib):
+    # a non-finite node or an index outside the nodes is refused before any GPU work
+    from cybermeshgenerator_gb300 import _lib as L
+    out = ctypes.c_void_p(123)
+    err = ctypes.create_string_buffer(128)
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    tet = np.array([0, 1, 2, 4], dtype=np.int32)
+    sz = np.ones(4)
+    args = lambda p, t: (p.ctypes.data_as(L.c_double_p), 4, t.ctypes.data_as(L.c_int_p), 1,
+                         sz.ctypes.data_as(L.c_double_p), 4, 1.0, ctypes.byref(out), err, 128)
+    assert lib.cmg_sizing_create(*args(pts, tet)) == 1
+    assert err.value == b"sizing: tetrahedron vertex index out of range"
+    assert out.value is None
+    bad = pts.copy()
+    bad[2, 1] = np.nan
+    assert lib.cmg_sizing_create(*args(bad, np.array([0, 1, 2, 3], dtype=np.int32))) == 1
+    assert err.value == b"sizing: non-finite background point"
+    assert lib.cmg_sizing_create(None, 4, None, 0, None, 0, 1.0, ctypes.byref(out), err, 128) == 1
+    assert lib.cmg_sizing_eval(None, None, 0, None, None, err, 128) == 1
+
+
 def test_facet_validation_and_readback(lib):
     from cybermeshgenerator_gb300 import _lib as L
     plc = lib.cmg_plc_create()

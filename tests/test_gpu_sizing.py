@@ -1,0 +1,133 @@
+"""The background sizing field on the GPU against the reference's from_background
+closure (fixtures made by it) and the oracle restatement: sizes bit for bit, the
+answering tetrahedron equal to the oracle's; the orient3d values it interpolates with
+(robust::orient3d_batch); host and device evaluation; binned, global and slow-path
+queries; the reference test's own properties."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+def test_orient3d_batch_values_match_reference(cm, golden):
+    g = golden("sizing")
+    P = g["o3_points"]
+    pts = P.reshape(-1, 3)
+    tets = np.arange(len(pts), dtype=np.int32).reshape(-1, 4)
+    assert _same(cm.orient3d_batch(pts, tets), g["o3_values"])
+
+
+def test_fixtures_match_reference(cm, golden):
+    g = golden("sizing")
+    for name in g["names"]:
+        name = str(name)
+        f = cm.SizingField(g[name + "_points"], g[name + "_tets"], g[name + "_sizes"],
+                           float(g[name + "_scale"]))
+        got = f.eval(g[name + "_queries"])
+        assert _same(got, g[name + "_values"]), name
+
+
+def _check_against_oracle(cm, orc, P, T, S, scale, Q):
+    f = cm.SizingField(P, T, S, scale)
+    got, which = f.eval(Q, which=True)
+    want, wwhich = orc.sizing(P, T, S, scale, Q)
+    assert _same(got, want)
+    assert np.array_equal(which.astype(np.int64), wwhich)
+    return f
+
+
+@pytest.mark.parametrize("n,jitter", [(6, 0.0), (12, 0.35)])
+def test_kuhn_meshes_match_oracle(cm, orc, n, jitter):
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(n, jitter, seed=n)
+    S = np.random.default_rng(n).uniform(0.05, 1.0, len(P))
+    Q = W.sizing_queries(P, T, 20000, seed=n)
+    f = _check_against_oracle(cm, orc, P, T, S, 0.75, Q)
+    st = f.stats()
+    assert st["inside"] > 0 and st["nearest"] > 0 and st["global_tets"] == 0
+
+
+def test_global_and_slow_paths(cm, orc):
+    """Slivers and a tiny tetrahedron (the global list), queries far outside the domain
+    and non-finite ones (the reference's scan on the device), flat tetrahedra."""
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(5, 0.2, seed=3)
+    rng = np.random.default_rng(8)
+    c = P.mean(0)
+    extra, tets = [], []
+    for k in range(40):
+        base = len(P) + len(extra)
+        o = rng.uniform(0.1, 0.9, 3)
+        a, b = rng.normal(size=3), rng.normal(size=3)
+        d = a * rng.random() + b * rng.random()
+        nrm = np.cross(a, b)
+        nrm /= np.linalg.norm(nrm)
+        extra += [o, o + 0.1 * a, o + 0.1 * b, o + 0.05 * d + 1e-12 * nrm]   # a sliver
+        tets.append([base, base + 1, base + 2, base + 3])
+    for k in range(10):
+        base = len(P) + len(extra)
+        o = rng.uniform(0.1, 0.9, 3)
+        extra += [o, o + [1e-8, 0, 0], o + [0, 1e-8, 0], o + [0, 0, 1e-8]]  # tiny
+        tets.append([base, base + 1, base + 2, base + 3])
+    P2 = np.vstack([P, np.array(extra)])
+    T2 = np.vstack([np.array(tets, dtype=np.int32)[::2], T, np.array(tets, dtype=np.int32)[1::2],
+                    [[0, 1, 2, 0]]])
+    S = rng.uniform(0.1, 1.0, len(P2))
+    Q = np.vstack([W.sizing_queries(P2, T2, 6000, seed=9),
+                   np.array(extra) + rng.normal(size=(len(extra), 3)) * 1e-9,
+                   c + rng.normal(size=(200, 3)) * 50.0,
+                   [[np.nan, 0, 0], [np.inf, 0.5, 0.5], [0.5, -np.inf, 0.5]]])
+    f = _check_against_oracle(cm, orc, P2, T2, S, 1.0, Q)
+    st = f.stats()
+    assert st["global_tets"] > 0 and st["slow"] >= 203
+
+
+def test_device_eval_matches_host(cm):
+    torch = pytest.importorskip("torch")
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(8, 0.3, seed=2)
+    S = np.random.default_rng(2).uniform(0.1, 1.0, len(P))
+    Q = W.sizing_queries(P, T, 50000, seed=7)
+    f = cm.SizingField(P, T, S, 2.0)
+    host, hw = f.eval(Q, which=True)
+    dev, dw = f.eval(torch.from_numpy(Q).cuda(), which=True)
+    torch.cuda.synchronize()
+    assert _same(dev.cpu().numpy(), host)
+    assert np.array_equal(dw.cpu().numpy(), hw)
+    # one point through the closure form
+    assert f(Q[3]) == host[3]
+
+
+def test_reference_test_properties(cm):
+    """tests/test_sizing.cpp:85-108 on the GPU."""
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(1)
+    f = cm.SizingField(P, T, 0.2 + 0.5 * P[:, 0])
+    assert abs(f(P[1]) - (0.2 + 0.5 * P[1, 0])) < 1e-6
+    mid = f([0.5, 0.5, 0.5])
+    assert 0.2 < mid < 0.7 and abs(mid - 0.45) < 0.05
+    full = cm.SizingField(P, T, np.full(len(P), 0.4), 1.0)
+    half = cm.SizingField(P, T, np.full(len(P), 0.4), 0.5)
+    q = [0.5, 0.5, 0.5]
+    assert abs(half(q) - 0.5 * full(q)) < 1e-9 and abs(full(q) - 0.4) < 1e-6
+
+
+def test_large_field_sample_matches_oracle(cm, orc):
+    """The 48^3-cell Kuhn field of the bench (663,552 tetrahedra): one million queries on
+    the GPU; a sample of them against the oracle's full scan."""
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(48, 0.3, seed=11)
+    S = np.random.default_rng(11).uniform(0.01, 0.2, len(P))
+    Q = W.sizing_queries(P, T, 1_000_000, seed=12)
+    f = cm.SizingField(P, T, S, 1.0)
+    got, which = f.eval(Q, which=True)
+    idx = np.random.default_rng(13).choice(len(Q), 400, replace=False)
+    want, wwhich = orc.sizing(P, T, S, 1.0, Q[idx])
+    assert _same(got[idx], want)
+    assert np.array_equal(which[idx].astype(np.int64), wwhich)
+    st = f.stats()
+    assert st["inside"] + st["nearest"] == len(Q)

@@ -205,3 +205,40 @@ def test_simplify_reference_properties(golden):
         if len(u):
             assert np.all((u[:, 0] != u[:, 1]) & (u[:, 1] != u[:, 2]) & (u[:, 0] != u[:, 2]))
             assert len(np.unique(np.sort(u, axis=1), axis=0)) == len(u)
+
+
+def test_orient3d_values_match_reference(orc, golden):
+    """robust::orient3d VALUES (not just signs) restated: 3000 inputs whose rounded
+    determinant is zero (every adaptive stage, the exact expansion's top component
+    included) and 500 random ones, bit for bit against the reference."""
+    g = golden("sizing")
+    P = g["o3_points"]
+    soa = np.stack([P[:, i, j] for i in range(4) for j in range(3)])
+    got = orc.orient3d_values(soa)
+    assert np.array_equal(got.view(np.uint64), g["o3_values"].view(np.uint64))
+    assert np.count_nonzero(g["o3_values"][:3000]) > 0
+
+
+def test_sizing_matches_reference(orc, golden):
+    """The sizing-field restatement against the reference's from_background closure on
+    every fixture, bit for bit (NaN where the reference gives NaN)."""
+    g = golden("sizing")
+    for name in g["names"]:
+        name = str(name)
+        got, which = orc.sizing(g[name + "_points"], g[name + "_tets"], g[name + "_sizes"],
+                                float(g[name + "_scale"]), g[name + "_queries"])
+        assert np.array_equal(got.view(np.uint64), g[name + "_values"].view(np.uint64)), name
+
+
+def test_sizing_reference_properties(orc):
+    """tests/test_sizing.cpp:85-108 on the restatement: exact at a node, about 0.45 at
+    the centre of the six-tetrahedron cube, scale 0.5 halves a constant field."""
+    from cybermeshgenerator_gb300 import workloads as W
+    P, T = W.kuhn_tet_mesh(1)
+    S = 0.2 + 0.5 * P[:, 0]
+    v, _ = orc.sizing(P, T, S, 1.0, np.vstack([P[1], [0.5, 0.5, 0.5]]))
+    assert abs(v[0] - (0.2 + 0.5 * P[1, 0])) < 1e-6
+    assert 0.2 < v[1] < 0.7 and abs(v[1] - 0.45) < 0.05
+    full, _ = orc.sizing(P, T, np.full(len(P), 0.4), 1.0, [[0.5, 0.5, 0.5]])
+    half, _ = orc.sizing(P, T, np.full(len(P), 0.4), 0.5, [[0.5, 0.5, 0.5]])
+    assert abs(half[0] - 0.5 * full[0]) < 1e-9 and abs(full[0] - 0.4) < 1e-6
