@@ -1137,7 +1137,8 @@ def run_sizing(args):
                           "through cmg_sizing_eval with host arrays",
               "tetrahedra": int(len(T)), "nodes": int(len(P)), "queries": int(n),
               "inside": int(st["inside"]), "nearest": int(st["nearest"]), "slow": int(st["slow"]),
-              "global_tets": int(st["global_tets"]), "cell_entries": int(st["binned_pairs"]),
+              "global_tets": int(st["global_tets"]), "far_tets": int(st["far_tets"]),
+              "cell_entries": int(st["binned_pairs"]),
               "build_s": build_s, "l2": "inputs larger than L2",
               "parallelism": f"replicas x{world}"}
     line = _base_line(SIZING_METRIC, "queries/s", value, world, args, total_ms, "fp64",

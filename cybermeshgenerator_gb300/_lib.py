@@ -73,6 +73,7 @@ class PredStats(ctypes.Structure):
 
 class SizingStats(ctypes.Structure):
     _fields_ = [("binned_pairs", ctypes.c_int64), ("global_tets", ctypes.c_int64),
+                ("far_tets", ctypes.c_int64),
                 ("inside", ctypes.c_int64), ("nearest", ctypes.c_int64), ("slow", ctypes.c_int64),
                 ("tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
                 ("upload_ms", ctypes.c_float), ("eval_ms", ctypes.c_float),

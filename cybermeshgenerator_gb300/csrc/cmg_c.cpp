@@ -1034,6 +1034,7 @@ cmg_status cmg_sizing_get_stats(cmg_sizing* s, cmg_sizing_stats* out) {
         const cmg::gpu::SizingStats r = cmg::gpu::sizing_stats(s->f, gpu_stream());
         out->binned_pairs = r.binned_pairs;
         out->global_tets = r.global_tets;
+        out->far_tets = r.far_tets;
         out->inside = r.inside;
         out->nearest = r.nearest;
         out->slow = r.slow;

@@ -111,7 +111,7 @@ void simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_m
 // object evaluated for batches of queries with the reference's results bit for bit.
 struct SizingField;
 struct SizingStats {
-    int64_t binned_pairs = 0, global_tets = 0;           // construction
+    int64_t binned_pairs = 0, global_tets = 0, far_tets = 0;  // construction
     int64_t inside = 0, nearest = 0, slow = 0;           // last evaluation: answers by kind
     int64_t tests = 0, candidates = 0;                   // full tests, candidates seen
     float upload_ms = 0.f, eval_ms = 0.f, download_ms = 0.f;  // last host evaluation

@@ -345,14 +345,92 @@ struct __align__(16) TetRec {
     P3 v[4];
     double D;        // orient3d(v0, v1, v2, v3) value; 0 never answers
     double s[4];     // node sizes
-    double blo[3];   // bounding box inflated by the margin, rounded outward
-    double bhi[3];
 };
+
+// What a candidate is screened with before the full test, all in FP32 (the FP64 pipe
+// of this part is narrow): the inflated box rounded outward, and the barycentric
+// coordinates lambda_i(p) = [i == 3] + g_i . (p - v3) with the error terms that make the
+// screen safe. A candidate is dropped only when some lambda_i provably lies below thr =
+// -1e-9 - e64, where e64 bounds |w_i - lambda_i| for the reference's rounded w_i
+// everywhere in the inflated box: its test would fail.
+struct __align__(16) TetFilt {
+    float blo[3], bhi[3];  // inflated box, rounded outward
+    float v3h[3], v3l[3];  // v3 = hi + lo to 2^-48
+    float g[12];           // g_0 .. g_3, rounded to FP32
+    float eg;              // bound on |g (exact) - g (FP64)| per component
+    float thr;             // NaN: no screen
+};
+
+// A query in the screen's terms: p rounded down and up (the box test) and as hi + lo.
+struct Q32 {
+    float lo[3], hi[3];
+    float ph[3], pl[3];
+};
+
+__device__ __forceinline__ Q32 make_q32(const P3& p) {
+    Q32 q;
+    const double c[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        q.lo[a] = __double2float_rd(c[a]);
+        q.hi[a] = __double2float_ru(c[a]);
+        q.ph[a] = __double2float_rn(c[a]);
+        q.pl[a] = __double2float_rn(c[a] - static_cast<double>(q.ph[a]));
+    }
+    return q;
+}
+
+__device__ __forceinline__ bool outside_box(const TetFilt& f, const Q32& q) {
+    return q.hi[0] < f.blo[0] || q.lo[0] > f.bhi[0] || q.hi[1] < f.blo[1] || q.lo[1] > f.bhi[1] ||
+           q.hi[2] < f.blo[2] || q.lo[2] > f.bhi[2];
+}
+
+// True when the screen proves the reference's test fails for this candidate.
+__device__ __forceinline__ bool screened_out(const TetFilt& f, const Q32& q) {
+    if (!(f.thr <= 0.0f)) return false;
+    float x[3], ex[3];
+    float S = 0.0f, E = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // x = (ph - v3h) + (pl - v3l): three roundings, and the two hi/lo splits
+        const float d1 = q.ph[a] - f.v3h[a], d2 = q.pl[a] - f.v3l[a];
+        x[a] = d1 + d2;
+        const float r = __fadd_ru(__fadd_ru(fabsf(d1), fabsf(d2)), fabsf(x[a]));
+        ex[a] = __fmaf_ru(r, 6.0e-8f, __fmul_ru(__fadd_ru(fabsf(q.ph[a]), fabsf(f.v3h[a])), 7.2e-15f));
+        S = __fadd_ru(S, fabsf(x[a]));
+        E = __fadd_ru(E, ex[a]);
+    }
+    const float egt = __fmul_ru(f.eg, __fadd_ru(S, E));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float gx = f.g[3 * i], gy = f.g[3 * i + 1], gz = f.g[3 * i + 2];
+        const float est = fmaf(gx, x[0], fmaf(gy, x[1], fmaf(gz, x[2], i == 3 ? 1.0f : 0.0f)));
+        const float A = __fmaf_ru(fabsf(gx), fabsf(x[0]),
+                                  __fmaf_ru(fabsf(gy), fabsf(x[1]), __fmul_ru(fabsf(gz), fabsf(x[2]))));
+        const float GE = __fmaf_ru(fabsf(gx), ex[0], __fmaf_ru(fabsf(gy), ex[1], __fmul_ru(fabsf(gz), ex[2])));
+        const float gs = __fadd_ru(__fadd_ru(fabsf(gx), fabsf(gy)), fabsf(gz));
+        // rounding of g (2^-24) and of the three fused steps (3 2^-24) on A; the error of
+        // g in FP64 (eg) on |x| + its error; |g| times the error of x; the constant 1 of
+        // lambda_3 in the fused steps; flushed tiny x
+        float bound = __fmaf_ru(A, 2.41e-7f, __fmul_ru(__fadd_ru(egt, GE), 1.01f));
+        bound = __fmaf_ru(gs, 1.2e-38f, __fadd_ru(bound, i == 3 ? 2e-7f : 0.0f));
+        if (__fadd_ru(est, bound) < f.thr) return true;
+    }
+    return false;
+}
 
 struct Grid {
     double lo[3];
     double h;
     int n[3];
+};
+
+// A grid's corner and cell size rounded down and up to FP32, and the bound on how far
+// a point may lie beyond the faces of the cell a rounded quotient put it in.
+struct GridF {
+    float lo_rd[3], lo_ru[3];
+    float h_rd, h_ru;
+    float tol[3];
 };
 
 __device__ __forceinline__ int cell_axis(double x, double lo, double h, int n) {
@@ -390,6 +468,9 @@ __global__ void __launch_bounds__(kThreads) k_tet_prep(const double* __restrict_
                                                        const double* __restrict__ sizes, Grid g,
                                                        double3 dlo, double3 dhi,
                                                        TetRec* __restrict__ rec,
+                                                       TetFilt* __restrict__ filt,
+                                                       int* __restrict__ far,
+                                                       double* __restrict__ farbox,
                                                        int* __restrict__ kind,
                                                        int* __restrict__ ncell,
                                                        int* __restrict__ cellbox) {
@@ -398,6 +479,9 @@ __global__ void __launch_bounds__(kThreads) k_tet_prep(const double* __restrict_
     const int4 q = tets[t];
     const int id[4] = {q.x, q.y, q.z, q.w};
     TetRec r;
+    TetFilt fl;
+    fl.thr = __int_as_float(0x7fc00000);  // NaN: no screen
+    fl.eg = 0.0f;
     double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
     for (int k = 0; k < 4; ++k) {
         r.v[k] = P3{pts[3 * static_cast<int64_t>(id[k])], pts[3 * static_cast<int64_t>(id[k]) + 1],
@@ -411,9 +495,23 @@ __global__ void __launch_bounds__(kThreads) k_tet_prep(const double* __restrict_
     }
     r.D = o3_value(r.v[0], r.v[1], r.v[2], r.v[3]);
     ncell[t] = 0;
+    far[t] = 0;
+    {
+        const double v3[3] = {r.v[3].x, r.v[3].y, r.v[3].z};
+        for (int a = 0; a < 3; ++a) {
+            fl.v3h[a] = __double2float_rn(v3[a]);
+            fl.v3l[a] = __double2float_rn(v3[a] - static_cast<double>(fl.v3h[a]));
+        }
+    }
+    double blo[3], bhi[3];
     if (r.D == 0.0) {
         kind[t] = kNever;
+        for (int a = 0; a < 3; ++a) {
+            fl.blo[a] = __int_as_float(0x7f800000);  // never inside
+            fl.bhi[a] = __int_as_float(0xff800000);
+        }
         rec[t] = r;
+        filt[t] = fl;
         return;
     }
     // error model: |D_fl - D| <= 16 u P_D, P_D <= 6 L^3; per weight |w - lambda| <= c (delta + L)^3
@@ -438,32 +536,91 @@ __global__ void __launch_bounds__(kThreads) k_tet_prep(const double* __restrict_
             dmax = fmax(dmax, fmax(__dsub_ru(lo[0], dlo.x), __dsub_ru(dhi.x, hi[0])));
             dmax = fmax(dmax, fmax(__dsub_ru(lo[1], dlo.y), __dsub_ru(dhi.y, hi[1])));
             dmax = fmax(dmax, fmax(__dsub_ru(lo[2], dlo.z), __dsub_ru(dhi.z, hi[2])));
-            if (gap_positive(m, L, c) && (dmax <= m || gap_positive(dmax * (1.0 + 1e-12), L, c)))
+            if (gap_positive(m, L, c)) {
                 k_out = kBinned;
+                if (dmax > m && !gap_positive(dmax * (1.0 + 1e-12), L, c)) {
+                    // g turns negative again before the domain's far corner: queries
+                    // beyond rfar (where g is still positive) must test this tetrahedron too
+                    double a0 = m, a1 = dmax;
+                    for (int it = 0; it < 80; ++it) {
+                        const double mid = 0.5 * (a0 + a1);
+                        if (gap_positive(mid, L, c)) a0 = mid;
+                        else a1 = mid;
+                    }
+                    const double rfar = a0 * (1.0 - 1e-9);
+                    if (rfar > m && gap_positive(rfar, L, c)) {
+                        for (int a = 0; a < 3; ++a) {
+                            farbox[6 * t + a] = __dsub_rd(lo[a], rfar);
+                            farbox[6 * t + 3 + a] = __dadd_ru(hi[a], rfar);
+                        }
+                        far[t] = 1;
+                    } else {
+                        k_out = kGlobal;
+                    }
+                }
+            }
+            if (k_out == kBinned) {
+                // barycentric gradients: (e1 x e2, e2 x e0, e0 x e1) / D and minus their sum
+                const double e0[3] = {r.v[0].x - r.v[3].x, r.v[0].y - r.v[3].y, r.v[0].z - r.v[3].z};
+                const double e1[3] = {r.v[1].x - r.v[3].x, r.v[1].y - r.v[3].y, r.v[1].z - r.v[3].z};
+                const double e2[3] = {r.v[2].x - r.v[3].x, r.v[2].y - r.v[3].y, r.v[2].z - r.v[3].z};
+                const double* pr[3][2] = {{e1, e2}, {e2, e0}, {e0, e1}};
+                double gsum[3] = {0.0, 0.0, 0.0};
+                for (int i = 0; i < 3; ++i) {
+                    const double* u = pr[i][0];
+                    const double* v = pr[i][1];
+                    const double cr[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                                          u[0] * v[1] - u[1] * v[0]};
+                    for (int a = 0; a < 3; ++a) {
+                        const double ga = cr[a] / r.D;
+                        fl.g[3 * i + a] = __double2float_rn(ga);
+                        gsum[a] += ga;
+                    }
+                }
+                for (int a = 0; a < 3; ++a) fl.g[9 + a] = __double2float_rn(-gsum[a]);
+                // per component: the cross product (rounded differences, products and
+                // difference), the division by the rounded D, and for g_3 the two sums
+                const double eg = 3.0 * (rho + 12.0 * kU) * 2.0 * L * L / Dlb * 1.01;
+                const double tm = L + m;
+                const double e64 = c * tm * tm * tm * 1.01;
+                if (eg < 1e30 && e64 < 1e-3) {
+                    fl.eg = __double2float_ru(eg);
+                    fl.thr = __fsub_rd(__double2float_rd(kEps), __double2float_ru(e64));
+                }
+            }
         }
     }
     for (int a = 0; a < 3; ++a) {
-        r.blo[a] = __dsub_rd(lo[a], m);
-        r.bhi[a] = __dadd_ru(hi[a], m);
+        blo[a] = __dsub_rd(lo[a], m);
+        bhi[a] = __dadd_ru(hi[a], m);
+        fl.blo[a] = __double2float_rd(blo[a]);
+        fl.bhi[a] = __double2float_ru(bhi[a]);
     }
     if (k_out == kGlobal) {
-        // the whole domain: a global tetrahedron has no box check
-        r.blo[0] = r.blo[1] = r.blo[2] = -DBL_MAX;
-        r.bhi[0] = r.bhi[1] = r.bhi[2] = DBL_MAX;
+        // the whole domain: a global tetrahedron has no box check and no screen
+        for (int a = 0; a < 3; ++a) {
+            fl.blo[a] = __int_as_float(0xff800000);
+            fl.bhi[a] = __int_as_float(0x7f800000);
+        }
+        fl.thr = __int_as_float(0x7fc00000);
     }
     if (k_out == kBinned) {
         int c0[3], c1[3];
         int64_t cnt = 1;
         const double glo[3] = {g.lo[0], g.lo[1], g.lo[2]};
         for (int a = 0; a < 3; ++a) {
-            c0[a] = cell_axis(r.blo[a], glo[a], g.h, g.n[a]);
-            c1[a] = cell_axis(r.bhi[a], glo[a], g.h, g.n[a]);
+            c0[a] = cell_axis(blo[a], glo[a], g.h, g.n[a]);
+            c1[a] = cell_axis(bhi[a], glo[a], g.h, g.n[a]);
             cnt *= (c1[a] - c0[a] + 1);
         }
         if (cnt > kMaxCellsPerTet) {
             k_out = kGlobal;
-            r.blo[0] = r.blo[1] = r.blo[2] = -DBL_MAX;
-            r.bhi[0] = r.bhi[1] = r.bhi[2] = DBL_MAX;
+            far[t] = 0;
+            for (int a = 0; a < 3; ++a) {
+                fl.blo[a] = __int_as_float(0xff800000);
+                fl.bhi[a] = __int_as_float(0x7f800000);
+            }
+            fl.thr = __int_as_float(0x7fc00000);
         } else {
             ncell[t] = static_cast<int>(cnt);
             for (int a = 0; a < 3; ++a) {
@@ -474,6 +631,7 @@ __global__ void __launch_bounds__(kThreads) k_tet_prep(const double* __restrict_
     }
     kind[t] = k_out;
     rec[t] = r;
+    filt[t] = fl;
 }
 
 // (cell, tetrahedron) pairs in tetrahedron order, and per-cell counts.
@@ -531,11 +689,14 @@ __global__ void __launch_bounds__(kThreads) k_node_keys(const double* __restrict
 __global__ void __launch_bounds__(kThreads) k_node_gather(const double* __restrict__ pts,
                                                           const double* __restrict__ sizes,
                                                           int64_t np, const uint32_t* __restrict__ order,
-                                                          Node4* __restrict__ node) {
+                                                          Node4* __restrict__ node,
+                                                          float4* __restrict__ nodef) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= np) return;
     const int64_t v = order[i];
     node[i] = Node4{pts[3 * v], pts[3 * v + 1], pts[3 * v + 2], static_cast<double>(v)};
+    nodef[i] = make_float4(__double2float_rn(pts[3 * v]), __double2float_rn(pts[3 * v + 1]),
+                           __double2float_rn(pts[3 * v + 2]), 0.0f);
 }
 
 // ------------------------------------------------------------ evaluation
@@ -546,12 +707,18 @@ struct Field {
     double3 dlo, dhi;  // fast-path domain
     Grid tg, ng;       // tetrahedron grid over the domain, node grid over the nodes' box
     const TetRec* rec;
+    const TetFilt* filt;
     const int* kind;
     const int64_t* tcell_off;  // tg cells + 1
     const uint32_t* tcell_tet;
     const int* global;
+    int64_t nfar;
+    const int* farlist;        // binned tetrahedra also tested by queries beyond their far box
+    const double* farbox;      // per tetrahedron: lo[3], hi[3] of the box inflated by rfar
     const int64_t* ncell_off;  // ng cells + 1
     const Node4* node;       // sorted nodes: x, y, z, original index
+    const float4* nodef;     // the same nodes rounded to FP32 (pruning only)
+    GridF ngf;               // the node grid in FP32, rounded outward
     const double* pts;         // nodes in their own order (the scan of the slow path)
     const double* sizes;       // padded to np
 };
@@ -567,13 +734,22 @@ __device__ __forceinline__ double dist2(const Node4& n, const P3& p) {
 }
 
 // Nearest node by rings of cells around p's (clamped) cell; stops once every unvisited
-// node's rounded squared distance provably exceeds the best found.
-__device__ int64_t nearest_node(const Field& F, const P3& p) {
+// node's rounded squared distance provably exceeds the best found. Cells and nodes are
+// pruned in FP32 with outward rounding before any node pays the reference's FP64
+// squared distance: skipped only when even their lower bound exceeds the best.
+__device__ int64_t nearest_node(const Field& F, const P3& p, const Q32& q) {
     const Grid& g = F.ng;
+    const GridF& gf = F.ngf;
     const double pc[3] = {p.x, p.y, p.z};
     int c[3];
-    for (int a = 0; a < 3; ++a) c[a] = cell_axis(pc[a], g.lo[a], g.h, g.n[a]);
+    float tolf[3];
+    for (int a = 0; a < 3; ++a) {
+        c[a] = cell_axis(pc[a], g.lo[a], g.h, g.n[a]);
+        // a node's cell comes from a rounded quotient: it may lie this far beyond its faces
+        tolf[a] = __fmaf_ru(fabsf(q.ph[a]), 3.6e-15f, gf.tol[a]);
+    }
     double best = DBL_MAX;
+    float best_f = __int_as_float(0x7f800000);
     int64_t bi = -1;
     const int kmax = max(g.n[0], max(g.n[1], g.n[2]));
     for (int k = 0; k <= kmax; ++k) {
@@ -589,14 +765,36 @@ __device__ int64_t nearest_node(const Field& F, const P3& p) {
                         z = c[2] + k - 1;  // interior of the shell: jump to its far face
                         continue;
                     }
+                    const int cx[3] = {x, y, z};
+                    float lb = 0.0f;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const float clo = __fsub_rd(__fmaf_rd(static_cast<float>(cx[a]), gf.h_rd, gf.lo_rd[a]), tolf[a]);
+                        const float chi = __fadd_ru(__fmaf_ru(static_cast<float>(cx[a] + 1), gf.h_ru, gf.lo_ru[a]), tolf[a]);
+                        const float d = fmaxf(0.0f, fmaxf(__fsub_rd(clo, q.hi[a]), __fsub_rd(q.lo[a], chi)));
+                        lb = __fmaf_rd(d, d, lb);
+                    }
+                    if (__fmul_rd(lb, 0.999999f) > best_f) continue;
                     const int64_t cell = (static_cast<int64_t>(x) * g.n[1] + y) * g.n[2] + z;
                     for (int64_t j = F.ncell_off[cell]; j < F.ncell_off[cell + 1]; ++j) {
+                        const float4 nf = F.nodef[j];
+                        const float nfa[3] = {nf.x, nf.y, nf.z};
+                        float lbn = 0.0f;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            const float dd = fabsf(nfa[a] - q.ph[a]);
+                            const float e = __fmul_ru(__fadd_ru(fabsf(nfa[a]), fabsf(q.ph[a])), 1.2e-7f);
+                            const float d = fmaxf(0.0f, __fsub_rd(__fmul_rd(dd, 0.99999988f), e));
+                            lbn = __fmaf_rd(d, d, lbn);
+                        }
+                        if (__fmul_rd(lbn, 0.999999f) > best_f) continue;
                         const Node4 nd = F.node[j];
                         const double d = dist2(nd, p);
                         const int64_t id = static_cast<int64_t>(nd.w);
                         if (d < best || (d == best && id < bi)) {
                             best = d;
                             bi = id;
+                            best_f = __double2float_ru(best);
                         }
                     }
                 }
@@ -634,50 +832,99 @@ __device__ __forceinline__ void warp_count(unsigned v, unsigned long long* dst) 
     if ((threadIdx.x & 31) == 0 && t) atomicAdd(dst, static_cast<unsigned long long>(t));
 }
 
+// Sort keys of the queries: the cell of the tetrahedron grid (the evaluation then runs
+// in cell order: neighbouring threads share candidates and take the same branch), or
+// the cell count for the queries the reference's scan answers (sorted last).
+__global__ void __launch_bounds__(kThreads) k_query_keys(Field F, const double* __restrict__ q,
+                                                         int64_t n, uint32_t* __restrict__ key,
+                                                         uint32_t* __restrict__ val,
+                                                         int* __restrict__ nslow) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const P3 p{q[3 * i], q[3 * i + 1], q[3 * i + 2]};
+    const bool fin = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+    const Grid& g = F.tg;
+    uint32_t k;
+    if (!fin || p.x < F.dlo.x || p.x > F.dhi.x || p.y < F.dlo.y || p.y > F.dhi.y || p.z < F.dlo.z ||
+        p.z > F.dhi.z) {
+        k = static_cast<uint32_t>(static_cast<int64_t>(g.n[0]) * g.n[1] * g.n[2]);
+        atomicAdd(nslow, 1);
+    } else {
+        k = static_cast<uint32_t>((static_cast<int64_t>(cell_axis(p.x, g.lo[0], g.h, g.n[0])) * g.n[1] +
+                                   cell_axis(p.y, g.lo[1], g.h, g.n[1])) * g.n[2] +
+                                  cell_axis(p.z, g.lo[2], g.h, g.n[2]));
+    }
+    key[i] = k;
+    val[i] = static_cast<uint32_t>(i);
+}
+
 __global__ void __launch_bounds__(kThreads) k_sizing_eval(Field F, const double* __restrict__ q,
+                                                          const uint32_t* __restrict__ skey,
+                                                          const uint32_t* __restrict__ order,
                                                           int64_t n, double* __restrict__ out,
                                                           int* __restrict__ which,
-                                                          int* __restrict__ slow,
-                                                          int* __restrict__ nslow,
                                                           EvalCounters* __restrict__ ctr) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t pos = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     unsigned inside = 0, nearest = 0, tests = 0, boxed = 0;
-    if (i < n) {
+    const int64_t ncells = static_cast<int64_t>(F.tg.n[0]) * F.tg.n[1] * F.tg.n[2];
+    if (pos < n && static_cast<int64_t>(skey[pos]) < ncells) {
+        const int64_t i = order[pos];
         const P3 p{q[3 * i], q[3 * i + 1], q[3 * i + 2]};
-        const bool fin = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
-        if (!fin || p.x < F.dlo.x || p.x > F.dhi.x || p.y < F.dlo.y || p.y > F.dhi.y ||
-            p.z < F.dlo.z || p.z > F.dhi.z) {
-            slow[atomicAdd(nslow, 1)] = static_cast<int>(i);
-        } else {
-            const Grid& g = F.tg;
-            const int64_t cell = (static_cast<int64_t>(cell_axis(p.x, g.lo[0], g.h, g.n[0])) * g.n[1] +
-                                  cell_axis(p.y, g.lo[1], g.h, g.n[1])) * g.n[2] +
-                                 cell_axis(p.z, g.lo[2], g.h, g.n[2]);
+        {
+            const int64_t cell = skey[pos];
             int64_t ia = F.tcell_off[cell];
             const int64_t ea = F.tcell_off[cell + 1];
-            int64_t ib = 0;
-            const int64_t eb = F.nglobal;
-            // candidates of the cell and the global list, merged ascending: the first
-            // that passes is the reference's answer
-            while (ia < ea || ib < eb) {
-                const int64_t ta = ia < ea ? static_cast<int64_t>(F.tcell_tet[ia]) : INT64_MAX;
-                const int64_t tb = ib < eb ? static_cast<int64_t>(F.global[ib]) : INT64_MAX;
-                int64_t t;
-                if (ta < tb) {
-                    t = ta;
-                    ++ia;
-                } else {
-                    t = tb;
-                    ++ib;
+            int64_t ib = 0, ic = 0;
+            const int64_t eb = F.nglobal, ec = F.nfar;
+            // next far-list entry this query must test (it lies beyond the far box)
+            auto next_far = [&]() -> int64_t {
+                for (; ic < ec; ++ic) {
+                    const int64_t t = F.farlist[ic];
+                    const double* fb = F.farbox + 6 * t;
+                    if (p.x < fb[0] || p.x > fb[3] || p.y < fb[1] || p.y > fb[4] || p.z < fb[2] ||
+                        p.z > fb[5])
+                        return t;
                 }
-                const TetRec& r = F.rec[t];
-                ++boxed;
-                if (p.x < r.blo[0] || p.x > r.bhi[0] || p.y < r.blo[1] || p.y > r.bhi[1] ||
-                    p.z < r.blo[2] || p.z > r.bhi[2])
-                    continue;
+                return INT64_MAX;
+            };
+            int64_t tc = next_far();
+            const Q32 q32 = make_q32(p);
+            // candidates of the cell, the global list and the far list, merged ascending:
+            // the first that passes is the reference's answer. Each lane screens ahead to
+            // its next surviving candidate; the full tests then run with the warp
+            // reconverged (the six tetrahedra of one cell of a structured mesh share a
+            // box, so testing in the screening loop would run them one lane group at a time)
+            for (;;) {
+                int64_t t = -1;
+                while (ia < ea || ib < eb || tc != INT64_MAX) {
+                    const int64_t ta = ia < ea ? static_cast<int64_t>(F.tcell_tet[ia]) : INT64_MAX;
+                    const int64_t tb = ib < eb ? static_cast<int64_t>(F.global[ib]) : INT64_MAX;
+                    int64_t t0;
+                    bool far_hit = false;
+                    if (ta <= tb && ta <= tc) {
+                        t0 = ta;
+                        ++ia;
+                    } else if (tb <= tc) {
+                        t0 = tb;
+                        ++ib;
+                    } else {
+                        t0 = tc;
+                        ++ic;
+                        tc = next_far();
+                        far_hit = true;  // beyond the far box: no box or screen applies
+                    }
+                    ++boxed;
+                    if (!far_hit) {
+                        const TetFilt& fc = F.filt[t0];
+                        if (outside_box(fc, q32) || screened_out(fc, q32)) continue;
+                    }
+                    t = t0;
+                    break;
+                }
+                if (t < 0) break;
                 ++tests;
                 double sz;
-                if (interp(r, p, sz)) {
+                if (interp(F.rec[t], p, sz)) {
                     out[i] = sz * F.scale;
                     if (which) which[i] = static_cast<int>(t);
                     inside = 1;
@@ -685,7 +932,7 @@ __global__ void __launch_bounds__(kThreads) k_sizing_eval(Field F, const double*
                 }
             }
             if (!inside) {
-                const int64_t bi = F.np > 0 ? nearest_node(F, p) : 0;
+                const int64_t bi = F.np > 0 ? nearest_node(F, p, q32) : 0;
                 out[i] = (F.np > 0 ? F.sizes[bi] : 0.0) * F.scale;
                 if (which) which[i] = -1;
                 nearest = 1;
@@ -702,8 +949,8 @@ __global__ void __launch_bounds__(kThreads) k_sizing_eval(Field F, const double*
 // query, 32 tetrahedra at a time in order (the first passing one answers), then the
 // nearest node by a warp-wide (distance, index) minimum with the reference's rules.
 __global__ void __launch_bounds__(kThreads) k_sizing_slow(Field F, const double* __restrict__ q,
-                                                          const int* __restrict__ slow,
-                                                          const int* __restrict__ nslow,
+                                                          const uint32_t* __restrict__ order,
+                                                          int64_t n, const int* __restrict__ nslow,
                                                           double* __restrict__ out,
                                                           int* __restrict__ which,
                                                           EvalCounters* __restrict__ ctr) {
@@ -712,7 +959,7 @@ __global__ void __launch_bounds__(kThreads) k_sizing_slow(Field F, const double*
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     const int ns = *nslow;
     for (int64_t s = w; s < ns; s += nw) {
-        const int64_t i = slow[s];
+        const int64_t i = order[n - ns + s];
         const P3 p{q[3 * i], q[3 * i + 1], q[3 * i + 2]};
         int64_t found = -1;
         double val = 0.0;
@@ -806,13 +1053,36 @@ Grid make_grid(const double lo[3], const double hi[3], double target_cells, int6
     return g;
 }
 
+float down(double x) {
+    float f = static_cast<float>(x);
+    return static_cast<double>(f) > x ? std::nextafter(f, -INFINITY) : f;
+}
+float up(double x) {
+    float f = static_cast<float>(x);
+    return static_cast<double>(f) < x ? std::nextafter(f, INFINITY) : f;
+}
+
+GridF grid_f(const Grid& g) {
+    GridF f{};
+    for (int a = 0; a < 3; ++a) {
+        f.lo_rd[a] = down(g.lo[a]);
+        f.lo_ru[a] = up(g.lo[a]);
+        f.tol[a] = up(16.0 * kU * (std::fabs(g.lo[a]) + (g.n[a] + 1.0) * g.h) * 1.01);
+    }
+    f.h_rd = down(g.h);
+    f.h_ru = up(g.h);
+    return f;
+}
+
 }  // namespace
 
 struct SizingField {
     Field f{};
     std::vector<void*> owned;
     EvalCounters* ctr = nullptr;
-    int* slow = nullptr;
+    uint32_t* skey = nullptr;   // per evaluation: sort keys (cells), query order, sort space
+    uint32_t* order = nullptr;
+    char* sort_tmp = nullptr;
     int* nslow = nullptr;
     int64_t slow_cap = 0;
     double* dq = nullptr;
@@ -889,6 +1159,9 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
     F.pts = dp;
 
     TetRec* rec = S->alloc<TetRec>(nt);
+    TetFilt* filt = S->alloc<TetFilt>(nt);
+    int* farflag = S->alloc<int>(nt);
+    double* farbox = S->alloc<double>(6 * nt);
     int* kind = S->alloc<int>(nt);
     int* ncell = S->alloc<int>(nt);
     int* cellbox = S->alloc<int>(6 * nt);
@@ -912,8 +1185,8 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
     } free_tmp{tmp};
     uint32_t* tkey = nullptr;
     if (nt > 0) {
-        k_tet_prep<<<blocks(nt), kThreads, 0, st>>>(dp, dt, nt, dsz, F.tg, F.dlo, F.dhi, rec, kind,
-                                                    ncell, cellbox);
+        k_tet_prep<<<blocks(nt), kThreads, 0, st>>>(dp, dt, nt, dsz, F.tg, F.dlo, F.dhi, rec, filt,
+                                                    farflag, farbox, kind, ncell, cellbox);
         CMG_LAUNCH();
         int64_t* poff = static_cast<int64_t*>(talloc(sizeof(int64_t) * (nt + 1)));
         int64_t* stmp = static_cast<int64_t*>(talloc(sizeof(int64_t) * scan_tmp_elems(std::max(nt, tcells))));
@@ -943,14 +1216,30 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
         k_compact<<<blocks(nt), kThreads, 0, st>>>(nt, flag, gpos, glist);
         CMG_LAUNCH();
         F.global = glist;
+        // far list, ascending
+        int64_t nfar = 0;
+        int64_t* fpos = static_cast<int64_t*>(talloc(sizeof(int64_t) * (nt + 1)));
+        exclusive_scan(farflag, fpos, nt, stmp, st);
+        CMG_CUDA(cudaMemcpyAsync(&nfar, fpos + nt, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        int* flist = S->alloc<int>(nfar);
+        k_compact<<<blocks(nt), kThreads, 0, st>>>(nt, farflag, fpos, flist);
+        CMG_LAUNCH();
+        F.farlist = flist;
+        F.nfar = nfar;
+        F.farbox = farbox;
     } else {
         int64_t* stmp = static_cast<int64_t*>(talloc(sizeof(int64_t) * scan_tmp_elems(tcells)));
         exclusive_scan(tcnt, toff, tcells, stmp, st);
         F.tcell_tet = S->alloc<uint32_t>(1);
         F.global = S->alloc<int>(1);
+        F.farlist = S->alloc<int>(1);
+        F.farbox = farbox;
+        F.nfar = 0;
     }
     F.nglobal = nglobal;
     F.rec = rec;
+    F.filt = filt;
     F.kind = kind;
     F.tcell_off = toff;
 
@@ -959,6 +1248,7 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
     int* ncnt = static_cast<int*>(talloc(sizeof(int) * ncells));
     int64_t* noff = S->alloc<int64_t>(ncells + 1);
     Node4* node = S->alloc<Node4>(np);
+    float4* nodef = S->alloc<float4>(np);
     CMG_CUDA(cudaMemsetAsync(ncnt, 0, sizeof(int) * ncells, st));
     int64_t* stmp = static_cast<int64_t*>(talloc(sizeof(int64_t) * scan_tmp_elems(ncells)));
     if (np > 0) {
@@ -970,16 +1260,19 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
         while ((int64_t(1) << bits) < ncells) ++bits;
         void* stmp2 = talloc(radix_sort_tmp_bytes(np));
         radix_sort_pairs(nkey, nval, np, bits, stmp2, st);
-        k_node_gather<<<blocks(np), kThreads, 0, st>>>(dp, dsz, np, nval, node);
+        k_node_gather<<<blocks(np), kThreads, 0, st>>>(dp, dsz, np, nval, node, nodef);
         CMG_LAUNCH();
     }
     exclusive_scan(ncnt, noff, ncells, stmp, st);
     F.ncell_off = noff;
     F.node = node;
+    F.nodef = nodef;
+    F.ngf = grid_f(F.ng);
     S->ctr = S->alloc<EvalCounters>(1);
     CMG_CUDA(cudaStreamSynchronize(st));  // the temporaries are freed on return
     S->last.binned_pairs = npairs;
     S->last.global_tets = nglobal;
+    S->last.far_tets = F.nfar;
     return S.release();
 }
 
@@ -1019,15 +1312,24 @@ void sizing_eval_device(SizingField* S, const double* q, int64_t n, double* out,
     if (n >= (int64_t(1) << 31)) throw std::invalid_argument("sizing: too many queries in one call");
     if (n > S->slow_cap) {
         const int64_t cap = std::max<int64_t>(n, 2 * S->slow_cap);
-        S->slow = S->alloc<int>(cap);
+        S->skey = S->alloc<uint32_t>(cap);
+        S->order = S->alloc<uint32_t>(cap);
+        S->sort_tmp = S->alloc<char>(radix_sort_tmp_bytes(cap));
         S->slow_cap = cap;
     }
     if (!S->nslow) S->nslow = S->alloc<int>(1);
     CMG_CUDA(cudaMemsetAsync(S->nslow, 0, sizeof(int), st));
     CMG_CUDA(cudaMemsetAsync(S->ctr, 0, sizeof(EvalCounters), st));
-    k_sizing_eval<<<blocks(n), kThreads, 0, st>>>(S->f, q, n, out, which, S->slow, S->nslow, S->ctr);
+    k_query_keys<<<blocks(n), kThreads, 0, st>>>(S->f, q, n, S->skey, S->order, S->nslow);
     CMG_LAUNCH();
-    k_sizing_slow<<<152 * 4, kThreads, 0, st>>>(S->f, q, S->slow, S->nslow, out, which, S->ctr);
+    const int64_t tcells = int64_t(S->f.tg.n[0]) * S->f.tg.n[1] * S->f.tg.n[2];
+    int bits = 1;
+    while ((int64_t(1) << bits) <= tcells) ++bits;
+    radix_sort_pairs(S->skey, S->order, n, bits, S->sort_tmp, st);
+    k_sizing_eval<<<blocks(n), kThreads, 0, st>>>(S->f, q, S->skey, S->order, n, out, which, S->ctr);
+    CMG_LAUNCH();
+    // the slow queries are the tail of the sorted order
+    k_sizing_slow<<<152 * 4, kThreads, 0, st>>>(S->f, q, S->order, n, S->nslow, out, which, S->ctr);
     CMG_LAUNCH();
 }
 

@@ -111,6 +111,7 @@ cmg_status cmg_simplify_last_timing(float* upload_ms, float* cluster_ms, float* 
 typedef struct cmg_sizing cmg_sizing;
 typedef struct cmg_sizing_stats {
     int64_t binned_pairs, global_tets;  /* construction: cell entries, tetrahedra every query tests */
+    int64_t far_tets;                   /* binned tetrahedra also tested by queries far from them */
     int64_t inside, nearest, slow;      /* last evaluation: answers in a tetrahedron, by the
                                            nearest node; queries outside the binned domain */
     int64_t tests, candidates;          /* full containment tests, candidates seen */

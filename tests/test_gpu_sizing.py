@@ -13,6 +13,15 @@ def _same(a, b):
     return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
 
 
+def _same_as_oracle(a, b):
+    """Bit for bit, except that a NaN equals any NaN: the oracle runs on the host CPU,
+    whose default NaN differs between architectures (x86, where the reference's
+    fixtures were made and the GPU agrees with them bit for bit, gives the negative
+    one; Arm the positive one)."""
+    a, b = np.asarray(a), np.asarray(b)
+    return bool(np.all((a.view(np.uint64) == b.view(np.uint64)) | (np.isnan(a) & np.isnan(b))))
+
+
 def test_orient3d_batch_values_match_reference(cm, golden):
     g = golden("sizing")
     P = g["o3_points"]
@@ -35,7 +44,7 @@ def _check_against_oracle(cm, orc, P, T, S, scale, Q):
     f = cm.SizingField(P, T, S, scale)
     got, which = f.eval(Q, which=True)
     want, wwhich = orc.sizing(P, T, S, scale, Q)
-    assert _same(got, want)
+    assert _same_as_oracle(got, want)
     assert np.array_equal(which.astype(np.int64), wwhich)
     return f
 
@@ -127,7 +136,10 @@ def test_large_field_sample_matches_oracle(cm, orc):
     got, which = f.eval(Q, which=True)
     idx = np.random.default_rng(13).choice(len(Q), 400, replace=False)
     want, wwhich = orc.sizing(P, T, S, 1.0, Q[idx])
-    assert _same(got[idx], want)
+    assert _same_as_oracle(got[idx], want)
     assert np.array_equal(which[idx].astype(np.int64), wwhich)
     st = f.stats()
     assert st["inside"] + st["nearest"] == len(Q)
+    # one jittered sliver of this field has a far regime: it stays binned, and only
+    # queries beyond its far box test it again
+    assert st["far_tets"] >= 1 and st["global_tets"] == 0
