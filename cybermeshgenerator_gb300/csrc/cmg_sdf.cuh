@@ -11,6 +11,7 @@ namespace cmg::gpu {
 namespace sdf {
 
 constexpr float kU32 = 5.9604645e-8f;  // 2^-24
+constexpr double kU64 = 1.1102230246251565e-16;  // 2^-53
 
 // ------------------------------------------------------------------ FP64 Ericson
 // Squared distance and region, reference operation order (src/voxelize/

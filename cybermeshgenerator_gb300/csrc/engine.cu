@@ -85,6 +85,7 @@ struct Batch::Impl {
     // sdf
     float4* tinfo = nullptr;
     float4* tinfo_lo = nullptr;
+    float4* tnorm = nullptr;  // unit normal (FP32) and its error bound
     void* trec = nullptr;
     float4* tlo = nullptr;
     float4* thi = nullptr;
@@ -174,6 +175,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
         if (sdf) {
             impl_->tinfo = carve<float4>(A, ntris_);
             impl_->tinfo_lo = carve<float4>(A, ntris_);
+            impl_->tnorm = carve<float4>(A, ntris_);
             impl_->trec = carve<char>(A, 144 * static_cast<size_t>(ntris_));
             impl_->tlo = carve<float4>(A, ntris_);
             impl_->thi = carve<float4>(A, ntris_);
@@ -365,7 +367,7 @@ void Batch::run_impl(bool sizing) {
     CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
     CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
     CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 2 * nseg, st));
-    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tlo, I.thi,
+    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tnorm, I.tlo, I.thi,
                         I.tbin, I.bincnt, I.large_cnt, I.emax_bits, st);
     exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);
     exclusive_scan(I.large_cnt, I.large_off, nseg, I.scan_tmp, st);
@@ -406,7 +408,7 @@ void Batch::run_impl(bool sizing) {
     if (opts_.brick == 16)
         launch_sdf_sub(opts_.precision, opts_.stage != 0, opts_.grab, dsegs_, nseg, I.work, nwork_,
                        queue_, I.soup, I.tinfo,
-                       I.tinfo_lo, I.trec, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
+                       I.tinfo_lo, I.trec, I.tnorm, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
                        sdf32_, sdf64_, near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
     else
         launch_sdf_eval(opts_.precision, opts_.brick, dsegs_, nseg, I.work, nbrick_, queue_,

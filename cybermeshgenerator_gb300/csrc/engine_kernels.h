@@ -29,7 +29,8 @@ int occ_row_cols();
 // sdf.cu
 // trec: one 144-byte translation-invariant FP32 record per triangle (sdf::TriRec).
 void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
-                         float4* tinfo, float4* tinfo_lo, void* trec, float4* tlo, float4* thi,
+                         float4* tinfo, float4* tinfo_lo, void* trec, float4* tnorm, float4* tlo,
+                         float4* thi,
                          int64_t* tbin, int* bincnt, int* large_cnt, unsigned* emax_bits,
                          cudaStream_t st);
 void launch_bin_fill(int64_t ntris, const int64_t* tbin, const int64_t* bin_off, int* bincur,
@@ -62,7 +63,7 @@ int sdf_sub_grid(int precision, bool stage);
 void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, int nseg,
                     const uint32_t* work, int64_t nwork, unsigned long long* queue, const double* soup,
                     const float4* tinfo, const float4* tinfo_lo, const void* trec,
-                    const int64_t* cand_off, const int* cand, const float* brick_emax,
+                    const float4* tnorm, const int64_t* cand_off, const int* cand, const float* brick_emax,
                     float band_cells, const uint8_t* occ, float* sdf32, double* sdf64,
                     int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats, int grid,
                     cudaStream_t st);

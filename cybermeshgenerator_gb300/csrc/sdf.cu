@@ -50,6 +50,7 @@ __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru
 __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64_t ntris,
                                const double* __restrict__ soup, float4* __restrict__ tinfo,
                                float4* __restrict__ tinfo_lo, TriRec* __restrict__ trec,
+                               float4* __restrict__ tnorm,
                                float4* __restrict__ tlo, float4* __restrict__ thi,
                                int64_t* __restrict__ tbin, int* __restrict__ bincnt,
                                int* __restrict__ large_cnt, unsigned* __restrict__ emax_bits) {
@@ -118,6 +119,16 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         }
         for (int q = 0; q < 3; ++q) r.nn[q] = static_cast<float>(n3[q]);
         r.ok = nl > 0.0 ? 1.f : 0.f;
+        // unit normal in FP32 and a bound on its distance from the exact one: the cross
+        // product of rounded edges errs by at most 21 u |u| |v| (as a vector), which
+        // turns its direction by at most twice that over |u x v|; then the
+        // normalisation and the FP32 rounding of the components
+        if (tnorm) {
+            const double lu = sqrt(ux * ux + uy * uy + uz * uz), lv = sqrt(vx * vx + vy * vy + vz * vz);
+            const double en = nl > 0.0 ? 50.0 * kU64 * lu * lv / nl + 1.2e-7 : 0.0;
+            tnorm[t] = make_float4(static_cast<float>(n3[0]), static_cast<float>(n3[1]),
+                                   static_cast<float>(n3[2]), round_up_f(en));
+        }
         r.pad_[0] = r.pad_[1] = 0.f;
         trec[t] = r;
     }
@@ -875,12 +886,13 @@ __global__ void k_work_keys(const int* __restrict__ cand_cnt, int64_t n, uint32_
 
 // ------------------------------------------------------------------ launchers
 void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
-                         float4* tinfo, float4* tinfo_lo, void* trec, float4* tlo, float4* thi,
+                         float4* tinfo, float4* tinfo_lo, void* trec, float4* tnorm, float4* tlo,
+                         float4* thi,
                          int64_t* tbin, int* bincnt, int* large_cnt, unsigned* emax_bits,
                          cudaStream_t st) {
     if (ntris == 0) return;
     k_sdf_tri_prep<<<static_cast<unsigned>((ntris + 255) / 256), 256, 0, st>>>(
-        segs, nseg, ntris, soup, tinfo, tinfo_lo, static_cast<TriRec*>(trec), tlo, thi, tbin,
+        segs, nseg, ntris, soup, tinfo, tinfo_lo, static_cast<TriRec*>(trec), tnorm, tlo, thi, tbin,
         bincnt, large_cnt, emax_bits);
     CMG_LAUNCH();
 }

@@ -87,11 +87,16 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
           int64_t nwork, int grab_n, unsigned long long* __restrict__ queue,
           const double* __restrict__ soup,
           const float4* __restrict__ tinfo, const float4* __restrict__ tinfo_lo,
-          const TriRec* __restrict__ trec, const int64_t* __restrict__ cand_off,
+          const TriRec* __restrict__ trec, const float4* __restrict__ tnorm,
+          const int64_t* __restrict__ cand_off,
           const int* __restrict__ cand, const float* __restrict__ brick_emax, float band_cells,
           Out o, Stats* __restrict__ st) {
     constexpr int kCap = Cap<STAGE>::value;
     __shared__ float4 s_c[kCap];  // centroid relative to the sub-brick centre, radius
+    // FP64 path: unit normal and plane offset n . centroid, and a bound on the error of
+    // the plane distances computed from them
+    __shared__ float4 s_nrm[PREC == kPrecFP64 ? kCap : 1];
+    __shared__ float s_pe[PREC == kPrecFP64 ? kCap : 1];
     __shared__ int s_t[kCap];
     __shared__ TriRec s_rec[STAGE ? kCap : 1];
     __shared__ int s_n;
@@ -244,14 +249,30 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
 #pragma unroll
                 for (int i = 0; i < kBatch; ++i) {
                     bool take = false;
-                    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 e = make_float4(0.f, 0.f, 0.f, 0.f), nv = e;
+                    float pe = 0.f;
                     const int t = tt[i];
                     if (t >= 0) {
                         e.x = (hh[i].x - chx) + (ll[i].x - clx);
                         e.y = (hh[i].y - chy) + (ll[i].y - cly);
                         e.z = (hh[i].z - chz) + (ll[i].z - clz);
                         e.w = hh[i].w;
-                        take = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z) - e.w <= limf;
+                        const float dc = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z);
+                        // FP64 cells: the plane's distance from a cell is at most its
+                        // distance from the triangle, so a triangle whose plane stays
+                        // beyond every cell's reach (U + r from the centre) cannot be
+                        // nearest to any of them. pe bounds the plane distances' error
+                        // at any cell of the sub-brick (normal error n.w; rounding of the
+                        // FP32 centroid, cell offsets and dot products). In the mixed
+                        // path an FP32 distance costs about as much as this test, which
+                        // is left out there.
+                        take = dc - e.w <= limf;
+                        if (PREC == kPrecFP64 && take) {
+                            nv = tnorm[t];
+                            pe = (nv.w + 12.f * kU32) * (dc + r4) * 1.1f + 1e-30f;
+                            nv.w = fmaf(nv.x, e.x, fmaf(nv.y, e.y, nv.z * e.z));
+                            take = fabsf(nv.w) - pe <= limf;
+                        }
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, take);
                     int base = 0;
@@ -260,6 +281,10 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     if (take) {
                         const int pos = base + __popc(m & ((1u << lane) - 1u));
                         s_c[pos] = e;
+                        if (PREC == kPrecFP64) {
+                            s_nrm[pos] = nv;
+                            s_pe[pos] = pe;
+                        }
                         s_t[pos] = t;
                         if (STAGE) {
                             const float4* src = reinterpret_cast<const float4*>(trec + t);
@@ -279,8 +304,15 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 const float4 e = s_c[j];
                 const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
                 const float lim = (bestd + e.w) * (1.f + 16.f * kU32) + 16.f * kU32 * r4;
-                const bool need = valid && dx * dx + dy * dy + dz * dz <= lim * lim;
+                bool need = valid && dx * dx + dy * dy + dz * dz <= lim * lim;
                 if (!__any_sync(0xffffffffu, need)) continue;
+                if (PREC == kPrecFP64) {
+                    // and the plane: its distance from the cell bounds the triangle's below
+                    const float4 nv = s_nrm[j];
+                    const float pd = fabsf(fmaf(nv.x, px, fmaf(nv.y, py, fmaf(nv.z, pz, -nv.w))));
+                    need = need && pd - s_pe[j] <= bestd * (1.f + 16.f * kU32) + 16.f * kU32 * r4;
+                    if (!__any_sync(0xffffffffu, need)) continue;
+                }
                 const int t = s_t[j];
                 if (PREC == kPrecMixed) {
                     TriRec rr;
@@ -436,7 +468,7 @@ int sdf_sub_grid(int precision, bool stage) {
 void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, int nseg,
                     const uint32_t* work, int64_t nwork, unsigned long long* queue, const double* soup,
                     const float4* tinfo, const float4* tinfo_lo, const void* trec,
-                    const int64_t* cand_off, const int* cand, const float* brick_emax,
+                    const float4* tnorm, const int64_t* cand_off, const int* cand, const float* brick_emax,
                     float band_cells, const uint8_t* occ, float* sdf32, double* sdf64,
                     int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats, int grid,
                     cudaStream_t st) {
@@ -446,15 +478,15 @@ void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, in
     if (grab != 1 && grab != 2 && grab != 4 && grab != 8) grab = 1;
     if (precision == kPrecMixed && stage)
         k_sdf_sub<kPrecMixed, true><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
             brick_emax, band_cells, o, stats);
     else if (precision == kPrecMixed)
         k_sdf_sub<kPrecMixed, false><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
             brick_emax, band_cells, o, stats);
     else
         k_sdf_sub<kPrecFP64, false><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, cand_off, cand,
+            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
             brick_emax, band_cells, o, stats);
     CMG_LAUNCH();
 }
