@@ -103,6 +103,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
     __shared__ long long s_item;
     __shared__ unsigned long long s_red[kSubThreads / 32];
     __shared__ int s_band;
+    __shared__ unsigned s_rmax;  // largest band reach of the CTA (FP32 bits)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned long long evals = 0, evals64 = 0, bandc = 0;
 
@@ -363,17 +364,50 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 const float reach = d32 + 2.f * eb;
                 const d3 Pc{cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
                             cell_center(g.corner[2], z, g.h)};
-                for (int64_t base = c0; base < c1; base += kSubThreads) {
-                    const int64_t k = base + tid;
-                    if (k < c1) {
-                        const int t = cand[k];
-                        const float4 hi = tinfo[t], lo = tinfo_lo[t];
-                        s_c[tid] = make_float4((hi.x - chx) + (lo.x - clx), (hi.y - chy) + (lo.y - cly),
-                                               (hi.z - chz) + (lo.z - clz), hi.w);
-                        s_t[tid] = t;
-                    }
+                // the CTA's largest band reach: a triangle passes some band cell's test
+                // below only if its sphere comes within that reach plus the sub-brick
+                // radius of the centre, so the brick list is compacted to those first
+                // (one cooperative pass) instead of every cell testing all of it
+                {
+                    const unsigned rbits = __reduce_max_sync(0xffffffffu, inband ? __float_as_uint(reach) : 0u);
+                    if (tid == 0) s_rmax = 0u;
                     __syncthreads();
-                    const int n = static_cast<int>(c1 - base < kSubThreads ? c1 - base : kSubThreads);
+                    if (lane == 0) atomicMax(&s_rmax, rbits);
+                    __syncthreads();
+                }
+                const float Rb = __uint_as_float(s_rmax);
+                int64_t bcur = c0;
+                while (bcur < c1) {
+                    if (tid == 0) s_n = 0;
+                    __syncthreads();
+                    int n = 0;
+                    while (bcur < c1 && n <= kCap - kSubThreads) {
+                        const int64_t k = bcur + tid;
+                        bool take = false;
+                        float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                        int t = -1;
+                        if (k < c1) {
+                            t = cand[k];
+                            const float4 hi = tinfo[t], lo = tinfo_lo[t];
+                            e = make_float4((hi.x - chx) + (lo.x - clx), (hi.y - chy) + (lo.y - cly),
+                                            (hi.z - chz) + (lo.z - clz), hi.w);
+                            const float limb = ((Rb + e.w) * (1.f + 16.f * kU32) + r4 * (1.f + 17.f * kU32)) *
+                                               (1.f + 8.f * kU32);
+                            take = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z) <= limb;
+                        }
+                        const unsigned m = __ballot_sync(0xffffffffu, take);
+                        int base = 0;
+                        if (lane == 0 && m) base = atomicAdd(&s_n, __popc(m));
+                        base = __shfl_sync(0xffffffffu, base, 0);
+                        if (take) {
+                            const int pos = base + __popc(m & ((1u << lane) - 1u));
+                            s_c[pos] = e;
+                            s_t[pos] = t;
+                        }
+                        bcur += kSubThreads;
+                        __syncthreads();
+                        n = s_n;
+                    }
                     for (int j = 0; j < n; ++j) {
                         const float4 e = s_c[j];
                         const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
