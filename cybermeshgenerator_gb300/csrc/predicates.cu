@@ -7,8 +7,10 @@
 //   EXACT:  the sign of the exact determinant.
 // Three passes, each over a compacted list of the queries the previous pass could
 // not decide, so that divergent work never holds back a full warp:
-//   k_pred_fp32   one thread per query, coordinates streamed from HBM (SoA,
-//                 coalesced), the determinant in FP32 with a rigorous bound that
+//   k_pred_fp32   one thread per query, coordinates streamed from HBM (SoA) into
+//                 shared memory by the TMA engine (bulk copies, mbarrier pipeline;
+//                 per-thread loads for unaligned columns and the tail), the
+//                 determinant in FP32 with a rigorous bound that
 //                 covers the rounding of the inputs to FP32 and of every FP32
 //                 operation, plus the FP64 filter bound of the reference: a sign it
 //                 certifies is the exact sign and also the sign of the FP64 rounded
@@ -182,13 +184,15 @@ __device__ __forceinline__ void push(bool flag, int64_t i, int64_t* list,
     if (flag) list[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
+// Queries [i0, n), one thread each, coordinates loaded per thread.
 template <int NPT>
-__global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t n, int8_t* __restrict__ out,
+__global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t i0, int64_t n,
+                                                        int8_t* __restrict__ out,
                                                         int64_t* __restrict__ list,
                                                         unsigned long long* __restrict__ count) {
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    const int64_t n_round = (n + 31) & ~int64_t(31);  // whole warps in the loop
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
+    const int64_t n_round = i0 + ((n - i0 + 31) & ~int64_t(31));  // whole warps in the loop
+    for (int64_t i = i0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
          i += stride) {
         int sg = 0;
         const bool live = i < n;
@@ -199,6 +203,129 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t n, int8_t
             out[i] = static_cast<int8_t>(sg);
         }
         push(live && sg == 0, i, list, count);
+    }
+}
+
+// ---- the FP32 pass with the columns moved by the TMA engine ----------------------
+// A persistent CTA streams tiles of kTile queries: per tile one bulk copy per
+// coordinate column (cp.async.bulk, global -> shared, completion counted on an
+// mbarrier), kStages tiles in flight, one thread per query computing from shared
+// memory, and one atomic per tile for the undecided list. Every wait is bounded: a
+// wait that runs out (it never should) stops the CTA after draining its copies, and
+// sets `fault`, on which the host reruns the pass with the per-thread loads.
+constexpr int kTile = 256;  // queries per tile: one per thread
+template <int NPT>
+struct Tma {
+    static constexpr int kCols = 3 * NPT;
+    static constexpr int kStages = NPT == 4 ? 4 : 3;
+    static constexpr unsigned kStageBytes = kCols * kTile * 8u;
+    static constexpr size_t kSmem = static_cast<size_t>(kStages) * kStageBytes;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes,
+                                          unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase with the given parity for at most about a second of clocks.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1ll << 31)) return false;
+    return true;
+}
+
+template <int NPT>
+__global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntiles,
+                                                            int8_t* __restrict__ out,
+                                                            int64_t* __restrict__ list,
+                                                            unsigned long long* __restrict__ count,
+                                                            unsigned long long* __restrict__ fault) {
+    using T = Tma<NPT>;
+    constexpr int C = T::kCols, S = T::kStages;
+    extern __shared__ __align__(128) unsigned char smem[];
+    double* buf = reinterpret_cast<double*>(smem);  // [S][C][kTile]
+    __shared__ __align__(8) unsigned long long bar[S];
+    __shared__ int s_wcnt[kThreads / 32];
+    __shared__ unsigned long long s_base;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t K = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    auto issue = [&](int64_t k) {  // thread 0: tile k of this CTA into stage k % S
+        const int st = static_cast<int>(k % S);
+        const int64_t tile = blockIdx.x + k * gridDim.x;
+        mbar_expect_tx(&bar[st], T::kStageBytes);
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            bulk_copy(buf + (static_cast<size_t>(st) * C + c) * kTile, s.c[c] + tile * kTile,
+                      kTile * 8u, &bar[st]);
+    };
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int64_t k = 0; k < S && k < K; ++k) issue(k);
+    for (int64_t k = 0; k < K; ++k) {
+        const int st = static_cast<int>(k % S);
+        const bool ok = mbar_wait(&bar[st], static_cast<unsigned>((k / S) & 1));
+        if (__syncthreads_or(!ok)) {
+            // drain this CTA's copies still in flight (bounded), then stop
+            if (tid == 0) {
+                atomicExch(fault, 1ull);
+                for (int64_t j = k; j < K && j < k + S; ++j)
+                    mbar_wait(&bar[j % S], static_cast<unsigned>((j / S) & 1));
+            }
+            return;
+        }
+        const int64_t i = (blockIdx.x + k * gridDim.x) * kTile + tid;
+        const double* b = buf + static_cast<size_t>(st) * C * kTile;
+        double v[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) v[c] = b[c * kTile + tid];
+        const int sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
+        out[i] = static_cast<int8_t>(sg);
+        const unsigned m = __ballot_sync(0xffffffffu, sg == 0);
+        if (lane == 0) s_wcnt[warp] = __popc(m);
+        __syncthreads();  // the stage is consumed; the warp counts are in
+        if (tid == 0) {
+            int tot = 0;
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const int c = s_wcnt[w];
+                s_wcnt[w] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(count, static_cast<unsigned long long>(tot)) : 0ull;
+            if (k + S < K) {
+                // the next copy into this stage follows the generic reads of it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(k + S);
+            }
+        }
+        __syncthreads();
+        if (sg == 0) list[s_base + s_wcnt[warp] + __popc(m & ((1u << lane) - 1u))] = i;
     }
 }
 
@@ -319,6 +446,7 @@ struct Counters {
     unsigned long long n64;  // left by the FP64 pass
     unsigned long long overflow;
     unsigned long long certified;  // decided in the FP64 pass by an exact evaluation
+    unsigned long long fault;      // a TMA wait of the FP32 pass ran out
 };
 
 }  // namespace
@@ -332,9 +460,43 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
     Counters* c = static_cast<Counters*>(counters);
     CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
     const int grid = 8 * sms;
-    if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, n, d_out, list_a, &c->n32);
-    else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, n, d_out, list_a, &c->n32);
-    CMG_LAUNCH();
+    // the TMA pass takes the whole tiles when every column starts on a 16-byte boundary
+    // (the bulk copies' rule); the rest, and unaligned columns, take the per-thread loads
+    bool aligned = true;
+    for (int k = 0; k < 3 * npt; ++k) aligned = aligned && (reinterpret_cast<uintptr_t>(coords[k]) % 16 == 0);
+    const int64_t ntiles = aligned ? n / kTile : 0;
+    const int64_t i0 = ntiles * kTile;
+    if (ntiles > 0) {
+        if (npt == 4) {
+            CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(Tma<4>::kSmem)));
+            k_pred_fp32_tma<4><<<2 * sms, kThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, list_a,
+                                                                         &c->n32, &c->fault);
+        } else {
+            CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(Tma<5>::kSmem)));
+            k_pred_fp32_tma<5><<<2 * sms, kThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, list_a,
+                                                                         &c->n32, &c->fault);
+        }
+        CMG_LAUNCH();
+    }
+    if (i0 < n) {
+        if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, i0, n, d_out, list_a, &c->n32);
+        else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, i0, n, d_out, list_a, &c->n32);
+        CMG_LAUNCH();
+    }
+    if (ntiles > 0) {
+        // a TMA wait that ran out (it never should) reruns the pass with per-thread loads
+        unsigned long long fault = 0;
+        CMG_CUDA(cudaMemcpyAsync(&fault, &c->fault, sizeof(fault), cudaMemcpyDeviceToHost, st));
+        CMG_CUDA(cudaStreamSynchronize(st));
+        if (fault) {
+            CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
+            if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
+            else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
+            CMG_LAUNCH();
+        }
+    }
     if (npt == 4 && mode == kPredExact)
         k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
                                                                       &c->certified);
