@@ -65,10 +65,11 @@ class WorkModel(ctypes.Structure):
 
 class PredStats(ctypes.Structure):
     _fields_ = [("queries", ctypes.c_int64), ("fp64_queries", ctypes.c_int64),
-                ("exact_queries", ctypes.c_int64), ("expansion_queries", ctypes.c_int64)]
+                ("exact_queries", ctypes.c_int64), ("expansion_queries", ctypes.c_int64),
+                ("fp32_pass_ms", ctypes.c_float)]
 
     def as_dict(self):
-        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+        return {k: (float if k.endswith("_ms") else int)(getattr(self, k)) for k, _ in self._fields_}
 
 
 class SizingStats(ctypes.Structure):

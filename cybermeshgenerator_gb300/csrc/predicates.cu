@@ -433,6 +433,7 @@ __global__ void k_widen(const int8_t* __restrict__ s, int64_t n, int* __restrict
 struct PredWork {
     Arena arena;
     std::mutex mu;
+    cudaEvent_t ev[2] = {nullptr, nullptr};  // around the FP32 pass of the last stream
 };
 PredWork& pred_work() {
     static PredWork w[64];
@@ -454,7 +455,7 @@ struct Counters {
 // Runs the three passes on device-resident SoA coordinates.
 void pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
                         int64_t* list_a, int64_t* list_b, void* counters, cudaStream_t st,
-                        int sms) {
+                        int sms, cudaEvent_t* fp32_events) {
     Soa s{};
     for (int k = 0; k < 3 * npt; ++k) s.c[k] = coords[k];
     Counters* c = static_cast<Counters*>(counters);
@@ -466,6 +467,7 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
     for (int k = 0; k < 3 * npt; ++k) aligned = aligned && (reinterpret_cast<uintptr_t>(coords[k]) % 16 == 0);
     const int64_t ntiles = aligned ? n / kTile : 0;
     const int64_t i0 = ntiles * kTile;
+    if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[0], st));
     if (ntiles > 0) {
         if (npt == 4) {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -485,6 +487,7 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
         else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, i0, n, d_out, list_a, &c->n32);
         CMG_LAUNCH();
     }
+    if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[1], st));
     if (ntiles > 0) {
         // a TMA wait that ran out (it never should) reruns the pass with per-thread loads
         unsigned long long fault = 0;
@@ -572,8 +575,10 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             for (int k = 0; k < 3 * npt; ++k)
                 CMG_CUDA(cudaMemcpyAsync(const_cast<double*>(dc[k]), coords[k], sizeof(double) * n,
                                          cudaMemcpyHostToDevice, st));
+        if (!w.ev[0])
+            for (cudaEvent_t& e : w.ev) CMG_CUDA(cudaEventCreate(&e));
         pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout, la,
-                           lb, cnt, st, sms);
+                           lb, cnt, st, sms, w.ev);
         Counters hc{};
         CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
         if (host) CMG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, st));
@@ -583,6 +588,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             stats->fp64_queries = static_cast<int64_t>(hc.n32);
             stats->exact_queries = static_cast<int64_t>(hc.n64 + hc.certified);
             stats->expansion_queries = static_cast<int64_t>(hc.n64);
+            CMG_CUDA(cudaEventElapsedTime(&stats->fp32_pass_ms, w.ev[0], w.ev[1]));
         }
         if (hc.overflow) {
             set_err(errbuf, len, "insphere: exact expansion exceeded its capacity");
@@ -651,7 +657,7 @@ cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int 
         CMG_LAUNCH();
         const double* cols[12];
         for (int k = 0; k < 12; ++k) cols[k] = soa + k * N;
-        pred_stream_device(4, cols, N, kPredCompat, d8, la, lb, cnt, st, device_sms());
+        pred_stream_device(4, cols, N, kPredCompat, d8, la, lb, cnt, st, device_sms(), nullptr);
         k_widen<<<static_cast<unsigned>((N + 255) / 256), 256, 0, st>>>(d8, N, dsg);
         CMG_LAUNCH();
         CMG_CUDA(cudaMemcpyAsync(out_sign, dsg, sizeof(int) * N, cudaMemcpyDeviceToHost, st));

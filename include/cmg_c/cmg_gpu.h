@@ -272,6 +272,7 @@ typedef struct cmg_pred_stats {
     int64_t exact_queries;     /* resolved in exact arithmetic (an FP64 evaluation in
                                   which no operation rounded, or expansions) */
     int64_t expansion_queries; /* of which needed expansion arithmetic */
+    float fp32_pass_ms;        /* device time of the FP32 certification pass (CUDA events) */
 } cmg_pred_stats;
 
 /* Signs (-1, 0, +1) of n orient3d(a,b,c,d) queries given as 12 SoA coordinate
