@@ -45,6 +45,7 @@ struct Cap {
     static constexpr int value = STAGE ? 256 : 512;
 };
 constexpr int kBatch = 4;  // candidates per thread per probe/filter step (loads in flight)
+constexpr int kProbe = 1024;  // head of the brick list the mixed probe scans (swept: 256-2048)
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only) and its wait.
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -146,14 +147,19 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         //         and the triangle that gives it (the seed of every cell below)
         float tb = FLT_MAX;
         int tseed = INT_MAX;
-        for (int64_t k0 = c0 + tid; k0 < c1; k0 += kBatch * kSubThreads) {
+        // any bound is valid; the brick list runs from the brick centre outwards (large
+        // triangles, then bins ring by ring), so its head holds the centre's nearest. The
+        // mixed path scans only the head (a looser U lengthens the filtered lists a
+        // little, which the cheap FP32 distances absorb); the FP64 path scans it all
+        const int64_t cp = PREC == kPrecMixed && c1 - c0 > kProbe ? c0 + kProbe : c1;
+        for (int64_t k0 = c0 + tid; k0 < cp; k0 += kBatch * kSubThreads) {
             // loads of kBatch candidates in flight before any of them is used
             int tt[kBatch];
             float4 hh[kBatch], ll[kBatch];
 #pragma unroll
             for (int i = 0; i < kBatch; ++i) {
                 const int64_t k = k0 + i * kSubThreads;
-                tt[i] = k < c1 ? cand[k] : -1;
+                tt[i] = k < cp ? cand[k] : -1;
             }
 #pragma unroll
             for (int i = 0; i < kBatch; ++i)
