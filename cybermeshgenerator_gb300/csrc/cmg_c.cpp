@@ -809,30 +809,16 @@ cmg_status cmg_plc_self_intersections(const cmg_plc* plc, cmg_intersections** ou
     if (out) *out = nullptr;
     if (!plc || !out) return CMG_ERR_INVALID_INPUT;
     return guarded(errbuf, len, [&] {
-        // fan triangles in facet order with their facet (src/detect/self_intersection.cpp:153-164)
-        std::vector<int> tris, facet;
-        for (size_t f = 0; f + 1 < plc->foff.size(); ++f) {
-            const int* v = plc->fidx.data() + plc->foff[f];
-            const size_t n = plc->foff[f + 1] - plc->foff[f];
-            for (size_t i = 2; i < n; ++i) {
-                tris.insert(tris.end(), {v[0], v[i - 1], v[i]});
-                facet.push_back(static_cast<int>(f));
-            }
-        }
-        std::vector<std::pair<int, int>> pairs;
+        // fan triangles in facet order with their facet (src/detect/self_intersection.cpp:
+        // 153-164), formed on the device from the facet offsets
+        std::unique_ptr<cmg_intersections> r(new cmg_intersections);
         {
             std::lock_guard<std::mutex> lk(gpu_mutex());
             cmg::gpu::self_intersections(plc->points.data(),
-                                         static_cast<int64_t>(plc->points.size() / 3), tris.data(),
-                                         static_cast<int64_t>(tris.size() / 3), pairs, gpu_stream());
-        }
-        std::unique_ptr<cmg_intersections> r(new cmg_intersections);
-        r->rows.reserve(8 * pairs.size());
-        for (const auto& pq : pairs) {
-            const int i = pq.first, j = pq.second;
-            r->rows.insert(r->rows.end(), {facet[i], facet[j], tris[3 * i], tris[3 * i + 1],
-                                           tris[3 * i + 2], tris[3 * j], tris[3 * j + 1],
-                                           tris[3 * j + 2]});
+                                         static_cast<int64_t>(plc->points.size() / 3),
+                                         plc->fidx.data(), static_cast<int64_t>(plc->fidx.size()),
+                                         plc->foff.data(), static_cast<int64_t>(plc->foff.size()) - 1,
+                                         r->rows, gpu_stream());
         }
         *out = r.release();
     });

@@ -11,12 +11,16 @@
 //      intersection of the two boxes, so each candidate pair is seen exactly once;
 //   2. narrow phase: the same orientation decisions on the device (o3d_fast in the
 //      reference order, the exact sign when it is zero);
-//   3. the crossing pairs are sorted to the reference's (i, j) order on the host.
+//   3. the crossing pairs are sorted to the reference's (i, j) order on the host, and
+//      their rows (facets, corners) gathered on the device.
+// The facets are fanned on the device and the surface's extent reduced there, each
+// stage's buffers sized once its sizes are known (nothing is uploaded twice).
 // The pair set does not depend on the grid, so the result is deterministic.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <cstdint>
 #include <mutex>
 #include <stdexcept>
@@ -201,6 +205,129 @@ __global__ void k_det_pairs(int64_t nentries, const int* __restrict__ list, cons
     }
 }
 
+// ---- fan triangulation of the facets, extent of the surface, result rows ----------
+
+__global__ void k_det_fan_count(const size_t* __restrict__ foff, int64_t nf, int64_t* __restrict__ cnt) {
+    const int64_t f = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int64_t n = static_cast<int64_t>(foff[f + 1] - foff[f]);
+    cnt[f] = n >= 3 ? n - 2 : 0;
+}
+
+// Fan triangles (v0, v[i-1], v[i]) of facet f at toff[f] + i - 2, with their facet.
+__global__ void k_det_fan_emit(const size_t* __restrict__ foff, const int* __restrict__ fidx, int64_t nf,
+                               const int64_t* __restrict__ toff, int* __restrict__ tris,
+                               int* __restrict__ facet) {
+    const int64_t f = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const size_t o = foff[f];
+    const int64_t n = static_cast<int64_t>(foff[f + 1] - o);
+    for (int64_t i = 2; i < n; ++i) {
+        const int64_t t = toff[f] + i - 2;
+        tris[3 * t] = fidx[o];
+        tris[3 * t + 1] = fidx[o + i - 1];
+        tris[3 * t + 2] = fidx[o + i];
+        facet[t] = static_cast<int>(f);
+    }
+}
+
+// Order-preserving integer image of a double (min / max commute with it).
+__device__ __forceinline__ unsigned long long ord_of(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double from_ord(unsigned long long o) {
+    const unsigned long long b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+struct Extent {
+    unsigned long long lo[3], hi[3];  // ord_of images
+    double ext_sum;                   // sum of the valid triangles' largest box extents
+    unsigned long long nvalid;
+    int nonfinite;
+};
+
+// Boxes of the valid triangles (indices inside the points), and the surface's extent.
+__global__ void __launch_bounds__(256) k_det_extent(int64_t ntris, const int* __restrict__ tris,
+                                                    const double* __restrict__ pts, int64_t npts,
+                                                    double* __restrict__ box, int* __restrict__ valid,
+                                                    Extent* __restrict__ ext) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    double es = 0.0;
+    bool ok = false, bad = false;
+    if (t < ntris) {
+        const int i0 = tris[3 * t], i1 = tris[3 * t + 1], i2 = tris[3 * t + 2];
+        ok = i0 >= 0 && i0 < npts && i1 >= 0 && i1 < npts && i2 >= 0 && i2 < npts;
+        valid[t] = ok ? 1 : 0;
+        if (ok) {
+            for (int q = 0; q < 3; ++q) {
+                const double a = pts[3 * static_cast<int64_t>(i0) + q], b = pts[3 * static_cast<int64_t>(i1) + q],
+                             d = pts[3 * static_cast<int64_t>(i2) + q];
+                bad = bad || !isfinite(a) || !isfinite(b) || !isfinite(d);
+                const double l = fmin(a, fmin(b, d)), h = fmax(a, fmax(b, d));
+                box[6 * t + q] = l;
+                box[6 * t + 3 + q] = h;
+                lo[q] = ord_of(l);
+                hi[q] = ord_of(h);
+                es = fmax(es, h - l);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int q = 0; q < 3; ++q) {
+            const unsigned long long l = __shfl_xor_sync(0xffffffffu, lo[q], o);
+            const unsigned long long h = __shfl_xor_sync(0xffffffffu, hi[q], o);
+            lo[q] = l < lo[q] ? l : lo[q];
+            hi[q] = h > hi[q] ? h : hi[q];
+        }
+        es += __shfl_xor_sync(0xffffffffu, es, o);
+    }
+    const unsigned nv = __popc(__ballot_sync(0xffffffffu, ok));
+    const bool anybad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && nv) {
+        for (int q = 0; q < 3; ++q) {
+            atomicMin(&ext->lo[q], lo[q]);
+            atomicMax(&ext->hi[q], hi[q]);
+        }
+        atomicAdd(&ext->ext_sum, es);
+        atomicAdd(&ext->nvalid, static_cast<unsigned long long>(nv));
+        if (anybad) atomicExch(&ext->nonfinite, 1);
+    }
+}
+
+__global__ void k_det_count(int64_t ntris, const int* __restrict__ valid, const double* __restrict__ box,
+                            DetGrid G, int* __restrict__ cnt) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    if (!valid[t]) {
+        cnt[t] = 0;
+        return;
+    }
+    int64_t c = 1;
+    for (int q = 0; q < 3; ++q)
+        c *= cell_of(box[6 * t + 3 + q], G.lo[q], G.cs, G.n[q]) - cell_of(box[6 * t + q], G.lo[q], G.cs, G.n[q]) + 1;
+    cnt[t] = static_cast<int>(c);
+}
+
+// Rows of the sorted pairs: facet_a, facet_b, triangle a's corners, triangle b's.
+__global__ void k_det_rows(int64_t np, const long long* __restrict__ keys, const int* __restrict__ tris,
+                           const int* __restrict__ facet, int* __restrict__ rows) {
+    const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int64_t a = keys[p] >> 32, b = keys[p] & 0xffffffffll;
+    int* r = rows + 8 * p;
+    r[0] = facet[a];
+    r[1] = facet[b];
+    for (int k = 0; k < 3; ++k) {
+        r[2 + k] = tris[3 * a + k];
+        r[5 + k] = tris[3 * b + k];
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -209,38 +336,94 @@ float g_last_ms = 0.f;  // device time of the last call's broad + narrow phase
 
 float self_intersections_last_ms() { return g_last_ms; }
 
-void self_intersections(const double* h_pts, int64_t npts, const int* h_tris, int64_t ntris,
-                        std::vector<std::pair<int, int>>& pairs, cudaStream_t st) {
-    pairs.clear();
+// Sizes one arena for a plan (the plan's pointers are taken again after a growth).
+template <typename Plan>
+void size_arena(Arena& A, Plan&& plan) {
+    A.clear_need();
+    plan();
+    if (A.overflowed()) {
+        A.reserve(A.need());
+        plan();
+    }
+}
+
+void self_intersections(const double* h_pts, int64_t npts, const int* h_fidx, int64_t nidx,
+                        const size_t* h_foff, int64_t nfacets, std::vector<int>& rows,
+                        cudaStream_t st) {
+    rows.clear();
     g_last_ms = 0.f;
+    if (nfacets <= 0 || npts <= 0) return;
+    if (nidx >= (int64_t(1) << 31)) throw std::invalid_argument("self_intersections: too many facet vertices");
+    static std::mutex mu;
+    // one arena per stage, each sized when its sizes are known, so that no earlier
+    // stage's buffers move: inputs, triangles, cells, entries, output, rows
+    static Arena A_in, A_tri, A_cell, A_list, A_out, A_rows;
+    static cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ev[0])
+        for (cudaEvent_t& e : ev) CMG_CUDA(cudaEventCreate(&e));
+    const int64_t nf = nfacets;
+    double* d_pts;
+    int* d_fidx;
+    size_t* d_foff;
+    int64_t *fcnt, *toff, *stmp_f;
+    Extent* ext;
+    size_arena(A_in, [&]() {
+        A_in.reset();
+        d_pts = A_in.take<double>(3 * npts);
+        d_fidx = A_in.take<int>(std::max<int64_t>(nidx, 1));
+        d_foff = A_in.take<size_t>(nf + 1);
+        fcnt = A_in.take<int64_t>(nf);
+        toff = A_in.take<int64_t>(nf + 1);
+        stmp_f = A_in.take<int64_t>(scan_tmp_elems(nf));
+        ext = A_in.take<Extent>(1);
+    });
+    CMG_CUDA(cudaMemcpyAsync(d_pts, h_pts, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
+    if (nidx) CMG_CUDA(cudaMemcpyAsync(d_fidx, h_fidx, sizeof(int) * nidx, cudaMemcpyHostToDevice, st));
+    CMG_CUDA(cudaMemcpyAsync(d_foff, h_foff, sizeof(size_t) * (nf + 1), cudaMemcpyHostToDevice, st));
+    CMG_CUDA(cudaEventRecord(ev[0], st));
+    const unsigned gf = static_cast<unsigned>((nf + 255) / 256);
+    k_det_fan_count<<<gf, 256, 0, st>>>(d_foff, nf, fcnt);
+    CMG_LAUNCH();
+    exclusive_scan(fcnt, toff, nf, stmp_f, st);
+    int64_t ntris = 0;
+    CMG_CUDA(cudaMemcpyAsync(&ntris, toff + nf, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CMG_CUDA(cudaStreamSynchronize(st));
     if (ntris < 2) return;
     if (ntris >= (int64_t(1) << 31)) throw std::invalid_argument("self_intersections: too many triangles");
+
+    int *tris, *facet, *valid, *cnt;
+    double* box;
+    size_arena(A_tri, [&]() {
+        A_tri.reset();
+        tris = A_tri.take<int>(3 * ntris);
+        facet = A_tri.take<int>(ntris);
+        valid = A_tri.take<int>(ntris);
+        cnt = A_tri.take<int>(ntris);
+        box = A_tri.take<double>(6 * ntris);
+    });
+    const unsigned gt = static_cast<unsigned>((ntris + 255) / 256);
+    k_det_fan_emit<<<gf, 256, 0, st>>>(d_foff, d_fidx, nf, toff, tris, facet);
+    CMG_LAUNCH();
+    CMG_CUDA(cudaMemsetAsync(ext, 0, sizeof(Extent), st));
+    CMG_CUDA(cudaMemsetAsync(ext->lo, 0xff, sizeof(ext->lo), st));
+    k_det_extent<<<gt, 256, 0, st>>>(ntris, tris, d_pts, npts, box, valid, ext);
+    CMG_LAUNCH();
+    Extent h{};
+    CMG_CUDA(cudaMemcpyAsync(&h, ext, sizeof(Extent), cudaMemcpyDeviceToHost, st));
+    CMG_CUDA(cudaStreamSynchronize(st));
+    if (h.nvalid < 2) return;
+    if (h.nonfinite) throw std::invalid_argument("self_intersections: non-finite coordinate");
     // grid over the valid triangles' points: cell edge ~ twice the mean box extent
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double ext_sum = 0.0;
-    int64_t nvalid = 0;
-    for (int64_t t = 0; t < ntris; ++t) {
-        const int* T = h_tris + 3 * t;
-        if (T[0] < 0 || T[0] >= npts || T[1] < 0 || T[1] >= npts || T[2] < 0 || T[2] >= npts) continue;
-        double e = 0.0;
-        for (int q = 0; q < 3; ++q) {
-            const double a = h_pts[3 * T[0] + q], b = h_pts[3 * T[1] + q], c = h_pts[3 * T[2] + q];
-            const double l = std::min(a, std::min(b, c)), h = std::max(a, std::max(b, c));
-            lo[q] = std::min(lo[q], l);
-            hi[q] = std::max(hi[q], h);
-            e = std::max(e, h - l);
-        }
-        ext_sum += e;
-        ++nvalid;
+    double lo[3], hi[3];
+    for (int q = 0; q < 3; ++q) {
+        lo[q] = from_ord(h.lo[q]);
+        hi[q] = from_ord(h.hi[q]);
     }
-    if (nvalid < 2) return;
-    for (int q = 0; q < 3; ++q)
-        if (!std::isfinite(lo[q]) || !std::isfinite(hi[q]))
-            throw std::invalid_argument("self_intersections: non-finite coordinate");
     DetGrid G{};
     double span = 0.0;
     for (int q = 0; q < 3; ++q) span = std::max(span, hi[q] - lo[q]);
-    double cs = std::max(2.0 * ext_sum / nvalid, span / 2048.0);
+    double cs = std::max(2.0 * h.ext_sum / static_cast<double>(h.nvalid), span / 2048.0);
     if (!(cs > 0.0)) cs = 1.0;
     for (;;) {
         int64_t total = 1;
@@ -255,94 +438,71 @@ void self_intersections(const double* h_pts, int64_t npts, const int* h_tris, in
     G.cs = cs;
     const int64_t ncell = static_cast<int64_t>(G.n[0]) * G.n[1] * G.n[2];
 
-    static std::mutex mu;
-    static Arena arena;  // grows; the calls are serialised
-    std::lock_guard<std::mutex> lk(mu);
-    Arena& A = arena;
-    double *d_pts, *box;
-    int *d_tris, *cnt, *cellcnt, *list;
+    int* cellcnt;
     int64_t *celloff, *stmp;
-    long long* out;
-    unsigned long long* nout;
-    int64_t nent = 0;
-    unsigned long long cap = 1 << 16;
-    auto plan = [&](int64_t ent) {
-        A.reset();
-        d_pts = A.take<double>(3 * npts);
-        d_tris = A.take<int>(3 * ntris);
-        box = A.take<double>(6 * ntris);
-        cnt = A.take<int>(ntris);
-        cellcnt = A.take<int>(ncell);
-        celloff = A.take<int64_t>(ncell + 1);
-        stmp = A.take<int64_t>(scan_tmp_elems(std::max(ncell, ntris) + 1));
-        list = A.take<int>(std::max<int64_t>(ent, 1));
-        out = A.take<long long>(cap);
-        nout = A.take<unsigned long long>(1);
-    };
-    auto sized = [&](int64_t ent) {
-        A.clear_need();
-        plan(ent);
-        if (A.overflowed()) {
-            A.reserve(A.need());
-            plan(ent);
-        }
-    };
-    sized(0);
-    CMG_CUDA(cudaMemcpyAsync(d_pts, h_pts, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
-    CMG_CUDA(cudaMemcpyAsync(d_tris, h_tris, sizeof(int) * 3 * ntris, cudaMemcpyHostToDevice, st));
-    const unsigned gt = static_cast<unsigned>((ntris + 255) / 256);
-    k_det_boxes<<<gt, 256, 0, st>>>(ntris, d_tris, d_pts, npts, G, box, cnt);
+    size_arena(A_cell, [&]() {
+        A_cell.reset();
+        cellcnt = A_cell.take<int>(ncell);
+        celloff = A_cell.take<int64_t>(ncell + 1);
+        stmp = A_cell.take<int64_t>(scan_tmp_elems(ncell + 1));
+    });
+    k_det_count<<<gt, 256, 0, st>>>(ntris, valid, box, G, cnt);
     CMG_LAUNCH();
     CMG_CUDA(cudaMemsetAsync(cellcnt, 0, sizeof(int) * ncell, st));
     k_det_bin<false><<<gt, 256, 0, st>>>(ntris, cnt, box, G, cellcnt, nullptr, nullptr);
     CMG_LAUNCH();
     exclusive_scan(cellcnt, celloff, ncell, stmp, st);
+    int64_t nent = 0;
     CMG_CUDA(cudaMemcpyAsync(&nent, celloff + ncell, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CMG_CUDA(cudaStreamSynchronize(st));
-    cudaEvent_t e0, e1;
-    CMG_CUDA(cudaEventCreate(&e0));
-    CMG_CUDA(cudaEventCreate(&e1));
-    struct Ev {
-        cudaEvent_t a, b;
-        ~Ev() {
-            cudaEventDestroy(a);
-            cudaEventDestroy(b);
-        }
-    } ev{e0, e1};
+    int* list;
+    size_arena(A_list, [&]() {
+        A_list.reset();
+        list = A_list.take<int>(std::max<int64_t>(nent, 1));
+    });
+    CMG_CUDA(cudaMemsetAsync(cellcnt, 0, sizeof(int) * ncell, st));
+    k_det_bin<true><<<gt, 256, 0, st>>>(ntris, cnt, box, G, cellcnt, celloff, list);
+    CMG_LAUNCH();
+    unsigned long long cap = 1 << 16;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        // the entry list (and, on a second attempt, the output) sized; inputs re-uploaded
-        // because a grown arena moved them
-        sized(nent);
-        CMG_CUDA(cudaMemcpyAsync(d_pts, h_pts, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
-        CMG_CUDA(cudaMemcpyAsync(d_tris, h_tris, sizeof(int) * 3 * ntris, cudaMemcpyHostToDevice, st));
-        CMG_CUDA(cudaEventRecord(e0, st));
-        k_det_boxes<<<gt, 256, 0, st>>>(ntris, d_tris, d_pts, npts, G, box, cnt);
-        CMG_LAUNCH();
-        CMG_CUDA(cudaMemsetAsync(cellcnt, 0, sizeof(int) * ncell, st));
-        k_det_bin<false><<<gt, 256, 0, st>>>(ntris, cnt, box, G, cellcnt, nullptr, nullptr);
-        CMG_LAUNCH();
-        exclusive_scan(cellcnt, celloff, ncell, stmp, st);
-        CMG_CUDA(cudaMemsetAsync(cellcnt, 0, sizeof(int) * ncell, st));
-        k_det_bin<true><<<gt, 256, 0, st>>>(ntris, cnt, box, G, cellcnt, celloff, list);
-        CMG_LAUNCH();
+        long long* out;
+        unsigned long long* nout;
+        size_arena(A_out, [&]() {
+            A_out.reset();
+            out = A_out.take<long long>(cap);
+            nout = A_out.take<unsigned long long>(1);
+        });
         CMG_CUDA(cudaMemsetAsync(nout, 0, sizeof(unsigned long long), st));
         if (nent > 0) {
             k_det_pairs<<<static_cast<unsigned>((nent + 127) / 128), 128, 0, st>>>(
-                nent, list, celloff, ncell, box, G, d_tris, d_pts, out, nout, cap);
+                nent, list, celloff, ncell, box, G, tris, d_pts, out, nout, cap);
             CMG_LAUNCH();
         }
-        CMG_CUDA(cudaEventRecord(e1, st));
+        CMG_CUDA(cudaEventRecord(ev[1], st));
         unsigned long long found = 0;
         CMG_CUDA(cudaMemcpyAsync(&found, nout, sizeof(found), cudaMemcpyDeviceToHost, st));
         CMG_CUDA(cudaStreamSynchronize(st));
-        CMG_CUDA(cudaEventElapsedTime(&g_last_ms, e0, e1));
+        CMG_CUDA(cudaEventElapsedTime(&g_last_ms, ev[0], ev[1]));
         if (found <= cap) {
-            std::vector<long long> h(found);
-            if (found)
-                CMG_CUDA(cudaMemcpy(h.data(), out, sizeof(long long) * found, cudaMemcpyDeviceToHost));
-            std::sort(h.begin(), h.end());
-            pairs.reserve(found);
-            for (long long k : h) pairs.emplace_back(static_cast<int>(k >> 32), static_cast<int>(k & 0xffffffff));
+            if (found == 0) return;
+            // the reference's (i, j) order, then the rows gathered on the device
+            std::vector<long long> keys(found);
+            CMG_CUDA(cudaMemcpy(keys.data(), out, sizeof(long long) * found, cudaMemcpyDeviceToHost));
+            std::sort(keys.begin(), keys.end());
+            long long* dkeys;
+            int* drows;
+            size_arena(A_rows, [&]() {
+                A_rows.reset();
+                dkeys = A_rows.take<long long>(found);
+                drows = A_rows.take<int>(8 * found);
+            });
+            CMG_CUDA(cudaMemcpyAsync(dkeys, keys.data(), sizeof(long long) * found, cudaMemcpyHostToDevice, st));
+            k_det_rows<<<static_cast<unsigned>((found + 255) / 256), 256, 0, st>>>(
+                static_cast<int64_t>(found), dkeys, tris, facet, drows);
+            CMG_LAUNCH();
+            rows.resize(8 * found);
+            CMG_CUDA(cudaMemcpyAsync(rows.data(), drows, sizeof(int) * 8 * found, cudaMemcpyDeviceToHost, st));
+            CMG_CUDA(cudaStreamSynchronize(st));
             return;
         }
         cap = found;  // exact count known: one more pass with room for every pair

@@ -90,11 +90,14 @@ void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vect
 // records (or parsed coordinates), decode + merge kernels, download of the arrays.
 void stl_last_timing(float* upload_ms, float* merge_ms, float* download_ms);
 
-// detect.cu: the pairs (i, j), i < j, of triangles (host arrays; an index outside
-// [0, npts) marks a triangle to skip) that share no vertex index and cross, in (i, j)
-// order, as the reference's self_intersections.
-void self_intersections(const double* pts, int64_t npts, const int* tris, int64_t ntris,
-                        std::vector<std::pair<int, int>>& pairs, cudaStream_t st);
+// detect.cu: the pairs (i, j), i < j, of fan triangles of the facets (host CSR:
+// facet f's polygon is fidx[foff[f] .. foff[f+1]); a triangle with an index outside
+// [0, npts) is skipped) that share no vertex index and cross, in (i, j) order, as the
+// reference's self_intersections; rows gets 8 ints per pair: facet_a, facet_b,
+// triangle a's corners, triangle b's.
+void self_intersections(const double* pts, int64_t npts, const int* fidx, int64_t nidx,
+                        const size_t* foff, int64_t nfacets, std::vector<int>& rows,
+                        cudaStream_t st);
 // Device time (CUDA events) of the last call's boxes, binning and pair tests.
 float self_intersections_last_ms();
 
