@@ -109,7 +109,8 @@ static __device__ __noinline__ bool insphere_certified(const d3& a, const d3& b,
 // determinant of their differences, evaluated in 128-bit integers, is exact; scaling
 // by 2^-L > 0 keeps its sign. B is chosen per predicate so that no intermediate can
 // overflow. Decomposition is on the integer pipe (the FP64 pipe is narrow here).
-__device__ __forceinline__ bool scale_to_ints(const double* v, int n, int B, long long* out) {
+__device__ __forceinline__ bool scale_to_ints(const double* v, int n, int B, long long* out,
+                                              int* scale_exp = nullptr) {
     int lmin = 0x7fffffff, emax = -0x7fffffff;
     for (int i = 0; i < n; ++i) {
         const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v[i]));
@@ -124,9 +125,11 @@ __device__ __forceinline__ bool scale_to_ints(const double* v, int n, int B, lon
     }
     if (lmin == 0x7fffffff) {  // all zero
         for (int i = 0; i < n; ++i) out[i] = 0;
+        if (scale_exp) *scale_exp = 0;
         return true;
     }
     if (emax - lmin + 1 > B) return false;
+    if (scale_exp) *scale_exp = lmin;
     for (int i = 0; i < n; ++i) {
         const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v[i]));
         if ((b << 1) == 0ull) {
@@ -160,6 +163,35 @@ __device__ __forceinline__ bool orient3d_int(const d3& a, const d3& b, const d3&
     return true;
 }
 
+// The sign of orient3d on integer coordinates, and whether the reference's FP64
+// evaluation (any operation order) is exact there: with every difference at most 2^16
+// in the common scale 2^L, products stay below 2^32, minors below 2^33, terms below
+// 2^50 and the determinant below 2^53 (6 D^3), and with -320 <= L, and every
+// coordinate below 2^300, nothing underflows or overflows; the FP64 rounded
+// determinant then equals the exact one.
+__device__ __forceinline__ bool orient3d_int_exact64(const d3& a, const d3& b, const d3& c,
+                                                     const d3& d, int* sign, bool* fp64_exact) {
+    const double v[12] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z};
+    long long X[12];
+    int L = 0;
+    if (!scale_to_ints(v, 12, 40, X, &L)) return false;
+    const long long adx = X[0] - X[9], ady = X[1] - X[10], adz = X[2] - X[11];
+    const long long bdx = X[3] - X[9], bdy = X[4] - X[10], bdz = X[5] - X[11];
+    const long long cdx = X[6] - X[9], cdy = X[7] - X[10], cdz = X[8] - X[11];
+    const __int128 m1 = static_cast<__int128>(bdx) * cdy - static_cast<__int128>(cdx) * bdy;
+    const __int128 m2 = static_cast<__int128>(cdx) * ady - static_cast<__int128>(adx) * cdy;
+    const __int128 m3 = static_cast<__int128>(adx) * bdy - static_cast<__int128>(bdx) * ady;
+    const __int128 det = adz * m1 + bdz * m2 + cdz * m3;
+    *sign = det > 0 ? 1 : (det < 0 ? -1 : 0);
+    long long D = 0;
+    const long long dd[9] = {adx, ady, adz, bdx, bdy, bdz, cdx, cdy, cdz};
+    for (int k = 0; k < 9; ++k) D = max(D, dd[k] < 0 ? -dd[k] : dd[k]);
+    long long M = 0;
+    for (int k = 0; k < 12; ++k) M = max(M, X[k] < 0 ? -X[k] : X[k]);
+    *fp64_exact = D <= (1ll << 16) && L >= -320 && (M == 0 || L + 41 <= 300);
+    return true;
+}
+
 // insphere (lifted 4x4, e as origin) on integers: differences < 2^23, 2x2 minors
 // < 2^47, 3x3 minors < 2^72, lifts < 2^48, terms < 2^120, the sum of four < 2^122.
 __device__ __forceinline__ bool insphere_int(const d3& a, const d3& b, const d3& c, const d3& d,
@@ -190,6 +222,27 @@ __device__ __forceinline__ bool insphere_int(const d3& a, const d3& b, const d3&
     const __int128 det = (dl * abc - cl * dab) + (bl * cda - al * bcd);
     *sign = det > 0 ? 1 : (det < 0 ? -1 : 0);
     return true;
+}
+
+// The same for insphere: differences at most 2^9 keep every intermediate of the
+// lifted evaluation below 2^53 (72 D^5), with -190 <= L and coordinates below 2^180.
+__device__ __forceinline__ bool insphere_int_exact64(const d3& a, const d3& b, const d3& c,
+                                                     const d3& d, const d3& e, int* sign,
+                                                     bool* fp64_exact) {
+    const double v[15] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z,
+                          d.x, d.y, d.z, e.x, e.y, e.z};
+    long long X[15];
+    int L = 0;
+    if (!scale_to_ints(v, 15, 22, X, &L)) return false;
+    long long D = 0;
+    for (int k = 0; k < 12; ++k) {
+        const long long q = X[k] - X[12 + k % 3];
+        D = max(D, q < 0 ? -q : q);
+    }
+    long long M = 0;
+    for (int k = 0; k < 15; ++k) M = max(M, X[k] < 0 ? -X[k] : X[k]);
+    *fp64_exact = D <= (1ll << 9) && L >= -190 && (M == 0 || L + 23 <= 180);
+    return insphere_int(a, b, c, d, e, sign);
 }
 
 // h = e + f: merge by magnitude, then a Two-Sum sweep, zero-eliminated.

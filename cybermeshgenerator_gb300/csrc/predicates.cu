@@ -348,8 +348,24 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
             double v[3 * NPT];
             load_query<NPT>(s, i, v);
             const d3 a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]}, d{v[9], v[10], v[11]};
-            double perm = 0.0, det;
-            if (NPT == 4) {
+            // integer coordinates first (integer pipe): in EXACT mode their sign decides;
+            // in COMPAT mode too when the FP64 evaluation is provably exact there (it then
+            // equals the exact determinant), which spares the narrow FP64 pipe
+            int isg = 0;
+            bool ic = false;
+            {
+                const d3 e5{NPT == 5 ? v[12] : 0.0, NPT == 5 ? v[13] : 0.0, NPT == 5 ? v[14] : 0.0};
+                bool fexact = false;
+                ic = NPT == 4 ? exact::orient3d_int_exact64(a, b, c, d, &isg, &fexact)
+                              : exact::insphere_int_exact64(a, b, c, d, e5, &isg, &fexact);
+                if (ic && (MODE == kPredExact || fexact)) {
+                    out[i] = static_cast<int8_t>(isg);
+                    certified = true;
+                }
+            }
+            double perm = 0.0, det = 0.0;
+            if (certified) {
+            } else if (NPT == 4) {
                 det = o3d_fast(a, b, c, d, MODE == kPredExact ? &perm : nullptr);
                 perm *= kO3dErrA;
             } else {
@@ -357,18 +373,16 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
                 det = isp_fast(a, b, c, d, e, MODE == kPredExact ? &perm : nullptr);
                 perm *= kIspErrA;
             }
-            bool decided = MODE == kPredCompat ? det != 0.0 : (det > perm || -det > perm);
-            if (decided) {
+            bool decided = certified || (MODE == kPredCompat ? det != 0.0 : (det > perm || -det > perm));
+            if (certified) {
+            } else if (decided) {
                 out[i] = static_cast<int8_t>(sgn(det));
             } else {
-                // integer coordinates after a common power-of-two scaling give the
-                // exact determinant on the integer pipe; else an FP64 evaluation in
-                // which no operation rounded is the exact determinant
+                // integer coordinates after a common power-of-two scaling gave the
+                // exact determinant on the integer pipe above; else an FP64 evaluation
+                // in which no operation rounded is the exact determinant
                 const d3 e{NPT == 5 ? v[12] : 0.0, NPT == 5 ? v[13] : 0.0, NPT == 5 ? v[14] : 0.0};
-                int isg;
-                const bool icert = NPT == 4 ? exact::orient3d_int(a, b, c, d, &isg)
-                                            : exact::insphere_int(a, b, c, d, e, &isg);
-                if (icert) {
+                if (ic) {
                     out[i] = static_cast<int8_t>(isg);
                     decided = certified = true;
                 } else {
