@@ -305,6 +305,45 @@ __device__ __forceinline__ float aabb_dist(float cx, float cy, float cz, float4 
     return sqrtf(dx * dx + dy * dy + dz * dz) * (1.f - 8.f * kU32);
 }
 
+// The entries of a group of 32 bins (lane L holds bin L's range [b0, b1)) as one
+// list, in bin order and then entry order: the order of a loop over the bins. The
+// warp takes 32 x R entries per round (R loads in flight per lane, across bin
+// boundaries); f(e, ok) gets the R entry positions of this lane and whether each
+// exists. The trip count is warp-uniform, so f may use warp votes.
+constexpr int kWalkRounds = 4;
+
+template <class F>
+__device__ __forceinline__ void for_group_entries(int64_t b0, int64_t b1, int lane, F&& f) {
+    const int len = static_cast<int>(b1 - b0);
+    int inc = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    const int excl = inc - len;
+    for (int base = 0; base < total; base += 32 * kWalkRounds) {
+        int64_t e[kWalkRounds];
+        bool ok[kWalkRounds];
+#pragma unroll
+        for (int j = 0; j < kWalkRounds; ++j) {
+            const int v = base + 32 * j + lane;
+            // owner bin: the number of bins whose inclusive end is <= v
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, inc, lo + step - 1) <= v) lo += step;
+            const int L = min(lo, 31);
+            const int s0 = __shfl_sync(0xffffffffu, excl, L);
+            const int64_t bb = __shfl_sync(0xffffffffu, b0, L);
+            ok[j] = v < total;
+            e[j] = bb + (v - s0);
+        }
+        f(e, ok);
+    }
+}
+
 // One warp per brick. FILL=false: computes U (stored) and the candidate count;
 // FILL=true: writes the candidates in walk order.
 template <bool FILL>
@@ -341,20 +380,19 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
             for (int k0 = 0; k0 < n; k0 += 32) {
                 int64_t b0 = 0, b1 = 0;
                 shell_bin(s, q, bin_off, r, k0 + lane, n, inside, b0, b1);
-                // the non-empty bins of this group, one at a time, all lanes over its list
-                unsigned m = __ballot_sync(0xffffffffu, b1 > b0);
-                while (m) {
-                    const int src = __ffs(m) - 1;
-                    m &= m - 1;
-                    const int64_t s0 = __shfl_sync(0xffffffffu, b0, src);
-                    const int64_t s1 = __shfl_sync(0xffffffffu, b1, src);
-                    for (int64_t e = s0 + lane; e < s1; e += 32) {
-                        float4 ti = tinfo[bin_list[e]];
+                for_group_entries(b0, b1, lane, [&](const int64_t* e, const bool* ok) {
+                    int t[kWalkRounds];
+#pragma unroll
+                    for (int j = 0; j < kWalkRounds; ++j) t[j] = ok[j] ? bin_list[e[j]] : -1;
+#pragma unroll
+                    for (int j = 0; j < kWalkRounds; ++j) {
+                        if (t[j] < 0) continue;
+                        float4 ti = tinfo[t[j]];
                         float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
                         float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f + 4.f * kU32);
                         U = fminf(U, d + ti.w + tol);
                     }
-                }
+                });
             }
             if (r > 0 && !__any_sync(0xffffffffu, inside)) {
                 U = warp_min(U);
@@ -398,28 +436,27 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         for (int k0 = 0; k0 < n; k0 += 32) {
             int64_t b0 = 0, b1 = 0;
             shell_bin(s, q, bin_off, r, k0 + lane, n, any_inside, b0, b1);
-            unsigned m = __ballot_sync(0xffffffffu, b1 > b0);
-            while (m) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const int64_t s0 = __shfl_sync(0xffffffffu, b0, src);
-                const int64_t s1 = __shfl_sync(0xffffffffu, b1, src);
-                for (int64_t e0 = s0; e0 < s1; e0 += 32) {  // uniform trip count: ballots inside
-                    const int64_t e = e0 + lane;
+            for_group_entries(b0, b1, lane, [&](const int64_t* e, const bool* ok) {
+                int t[kWalkRounds];
+#pragma unroll
+                for (int j = 0; j < kWalkRounds; ++j) t[j] = ok[j] ? bin_list[e[j]] : -1;
+                float4 ti[kWalkRounds];
+#pragma unroll
+                for (int j = 0; j < kWalkRounds; ++j)
+                    if (t[j] >= 0) ti[j] = tinfo[t[j]];
+#pragma unroll
+                for (int j = 0; j < kWalkRounds; ++j) {
                     bool take = false;
-                    int t = 0;
                     float et = 0.f;
-                    if (e < s1) {
-                        t = bin_list[e];
-                        float4 ti = tinfo[t];
-                        float dx2 = ti.x - q.cx, dy2 = ti.y - q.cy, dz2 = ti.z - q.cz;
+                    if (t[j] >= 0) {
+                        float dx2 = ti[j].x - q.cx, dy2 = ti[j].y - q.cy, dz2 = ti[j].z - q.cz;
                         float d = sqrtf(dx2 * dx2 + dy2 * dy2 + dz2 * dz2) * (1.f - 4.f * kU32);
-                        take = d - ti.w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
-                        et = ti.w;
+                        take = d - ti[j].w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
+                        et = ti[j].w;
                     }
-                    emit(take, t, et);
+                    emit(take, t[j], et);
                 }
-            }
+            });
         }
         if (r > 0 && !__any_sync(0xffffffffu, any_inside)) break;
     }
