@@ -6,9 +6,11 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <new>
 #include <tuple>
 
 #include "cmg_util.h"
@@ -21,6 +23,70 @@ std::atomic<long long> g_launches{0};
 }
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches() { return g_launches.load(std::memory_order_relaxed); }
+
+// ------------------------------------------------------------------ host block pool
+namespace {
+
+struct HostPool {
+    static constexpr size_t kCachedCap = size_t{4} << 30;  // idle pinned bytes kept
+    std::mutex mu;
+    std::multimap<size_t, void*> idle;                      // capacity -> block
+    size_t cached = 0;
+};
+
+HostPool& host_pool() {
+    static HostPool* pool = new HostPool;  // never destroyed: blocks outlive static teardown
+    return *pool;
+}
+
+}  // namespace
+
+void* host_block_acquire(size_t bytes, size_t* cap, bool* pinned) {
+    HostPool& P = host_pool();
+    {
+        std::lock_guard<std::mutex> lk(P.mu);
+        auto it = P.idle.lower_bound(bytes);
+        if (it != P.idle.end() && it->first <= 2 * bytes + (size_t{1} << 20)) {
+            void* p = it->second;
+            *cap = it->first;
+            *pinned = true;
+            P.cached -= it->first;
+            P.idle.erase(it);
+            return p;
+        }
+    }
+    const size_t c = (bytes + 65535) & ~size_t{65535};
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, c, cudaHostAllocDefault) == cudaSuccess && p) {
+        *cap = c;
+        *pinned = true;
+        return p;
+    }
+    cudaGetLastError();  // a failed pinning is not an error of the pipeline
+    p = std::malloc(bytes);
+    if (!p) throw std::bad_alloc();
+    *cap = bytes;
+    *pinned = false;
+    return p;
+}
+
+void host_block_release(void* p, size_t cap, bool pinned) {
+    if (!p) return;
+    if (!pinned) {
+        std::free(p);
+        return;
+    }
+    HostPool& P = host_pool();
+    {
+        std::lock_guard<std::mutex> lk(P.mu);
+        if (P.cached + cap <= HostPool::kCachedCap) {
+            P.idle.emplace(cap, p);
+            P.cached += cap;
+            return;
+        }
+    }
+    cudaFreeHost(p);
+}
 
 int device_sms() {
     int dev = 0, sms = 0;

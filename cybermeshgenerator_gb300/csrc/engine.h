@@ -47,26 +47,64 @@ struct HostMesh {
     GridDesc g{};
 };
 
-// Host array filled by a device copy: allocated without value-initialisation.
+// Page-locked host blocks, kept for reuse after release: a device-to-host copy
+// into one runs at the link's rate (no staging through the driver's bounce
+// buffers), and pinning is paid once per block rather than once per call. A block
+// of `bytes` or more is returned with its capacity; when pinning fails the block is
+// ordinary heap memory (*pinned = false). Released blocks beyond the pool's cap of
+// cached bytes are freed. Thread-safe.
+void* host_block_acquire(size_t bytes, size_t* cap, bool* pinned);
+void host_block_release(void* p, size_t cap, bool pinned);
+
+// Host array filled by a device copy: allocated without value-initialisation, from
+// the page-locked block pool.
 template <typename T>
 class HostBuf {
 public:
+    HostBuf() = default;
+    ~HostBuf() { reset(); }
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    HostBuf(HostBuf&& o) noexcept { take(o); }
+    HostBuf& operator=(HostBuf&& o) noexcept {
+        if (this != &o) {
+            reset();
+            take(o);
+        }
+        return *this;
+    }
     void resize(size_t n) {
-        p_.reset(n ? new T[n] : nullptr);
+        if (n * sizeof(T) <= cap_ && n_ != 0) {
+            n_ = n;
+            return;
+        }
+        reset();
+        if (n) p_ = static_cast<T*>(host_block_acquire(n * sizeof(T), &cap_, &pinned_));
         n_ = n;
     }
-    T* data() { return p_.get(); }
-    const T* data() const { return p_.get(); }
+    T* data() { return p_; }
+    const T* data() const { return p_; }
     size_t size() const { return n_; }
     bool empty() const { return n_ == 0; }
     T& operator[](size_t i) { return p_[i]; }
     const T& operator[](size_t i) const { return p_[i]; }
-    const T* begin() const { return p_.get(); }
-    const T* end() const { return p_.get() + n_; }
+    const T* begin() const { return p_; }
+    const T* end() const { return p_ + n_; }
 
 private:
-    std::unique_ptr<T[]> p_;
-    size_t n_ = 0;
+    void reset() {
+        if (p_) host_block_release(p_, cap_, pinned_);
+        p_ = nullptr;
+        n_ = cap_ = 0;
+        pinned_ = false;
+    }
+    void take(HostBuf& o) {
+        p_ = o.p_; n_ = o.n_; cap_ = o.cap_; pinned_ = o.pinned_;
+        o.p_ = nullptr; o.n_ = o.cap_ = 0; o.pinned_ = false;
+    }
+    T* p_ = nullptr;
+    size_t n_ = 0, cap_ = 0;
+    bool pinned_ = false;
 };
 
 struct HostResult {
