@@ -507,6 +507,30 @@ class Batch:
 MEM_HOST, MEM_DEVICE = 0, 1
 
 
+class _HostBlock:
+    """A page-locked block of the library's host pool, returned to the pool when the
+    last array viewing it is collected."""
+
+    def __init__(self, nbytes: int) -> None:
+        self.ptr = _clib.cmg_host_alloc(max(int(nbytes), 1))
+        if not self.ptr:
+            raise MemoryError(f"cmg_host_alloc({nbytes}) failed")
+
+    def __del__(self) -> None:
+        if getattr(self, "ptr", None) and _clib is not None:
+            _clib.cmg_host_free(self.ptr)
+            self.ptr = None
+
+
+def host_empty(n: int, dtype=np.int8) -> np.ndarray:
+    """An uninitialised 1-D array in pooled page-locked host memory (the library
+    writes into it without first-touch page faults; the block is reused after the
+    array is collected)."""
+    dt = np.dtype(dtype)
+    blk = _HostBlock(n * dt.itemsize)
+    return np.asarray(_View(blk, blk.ptr, n, dt))
+
+
 def _stream_call(fn, npt, soa, mode, stream=None):
     """soa: (3*npt, n) float64 NumPy array (host) or a list of device pointers with n."""
     if isinstance(soa, np.ndarray):
@@ -515,7 +539,7 @@ def _stream_call(fn, npt, soa, mode, stream=None):
             raise ValueError(f"expected {3 * npt} coordinate rows")
         n = soa.shape[1]
         rows = (ctypes.c_void_p * (3 * npt))(*[soa[k].ctypes.data for k in range(3 * npt)])
-        out = np.zeros(n, dtype=np.int8)
+        out = host_empty(n, np.int8)
         st = _L.PredStats()
         err = ctypes.create_string_buffer(512)
         _check(fn(rows, n, int(mode), MEM_HOST, out.ctypes.data_as(ctypes.c_void_p),
@@ -593,7 +617,7 @@ def library_path() -> str:
     return _L.library_path()
 
 
-__all__ = ["orient3d_stream", "insphere_stream", "orient3d_signs", "orient3d_batch", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
+__all__ = ["orient3d_stream", "insphere_stream", "host_empty", "orient3d_signs", "orient3d_batch", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
            "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
            "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT",
            "read_plc", "plc_from_stl", "self_intersections", "simplify", "stl_last_timing",

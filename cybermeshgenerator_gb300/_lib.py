@@ -182,6 +182,8 @@ def _bind(lib: ctypes.CDLL) -> None:
         sig(n, I, [ctypes.POINTER(V), ctypes.c_int64, I, I, V, ctypes.POINTER(PredStats), V, S, Z])
     sig("cmg_orient3d_signs", I, [c_double_p, I, c_int_p, I, c_int_p])
     sig("cmg_orient3d_batch", I, [c_double_p, I, c_int_p, I, c_double_p])
+    sig("cmg_host_alloc", V, [Z])
+    sig("cmg_host_free", None, [V])
     sig("cmg_gpu_occupancy_static", I, [V, ctypes.c_int64, V, ctypes.c_int64, c_double_p, D,
                                         c_int_p, I, V, V, S, Z])
     # differentiable signed distance

@@ -23,6 +23,8 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "cmg_util.h"
@@ -306,6 +308,18 @@ cmg_status guarded(char* errbuf, size_t len, F&& f) {
 
 const char* kNotHere = "not part of the GB300 voxelization library (meshing and file I/O stay in the reference)";
 
+}  // namespace
+
+namespace {
+// Blocks handed out by cmg_host_alloc: capacity and whether page-locked.
+struct HostBlocks {
+    std::mutex mu;
+    std::unordered_map<void*, std::pair<size_t, bool>> live;
+};
+HostBlocks& host_blocks() {
+    static HostBlocks* h = new HostBlocks;  // outlives static teardown, like the pool
+    return *h;
+}
 }  // namespace
 
 extern "C" {
@@ -1049,6 +1063,33 @@ cmg_status cmg_orient3d_batch(const double* xyz, int npts, const int* tets, int 
         return CMG_ERR_INTERNAL;
     }
     return CMG_OK;
+}
+
+void* cmg_host_alloc(size_t bytes) {
+    try {
+        size_t cap = 0;
+        bool pinned = false;
+        void* p = cmg::gpu::host_block_acquire(bytes ? bytes : 1, &cap, &pinned);
+        std::lock_guard<std::mutex> lk(host_blocks().mu);
+        host_blocks().live[p] = {cap, pinned};
+        return p;
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void cmg_host_free(void* p) {
+    if (!p) return;
+    HostBlocks& H = host_blocks();
+    std::pair<size_t, bool> b;
+    {
+        std::lock_guard<std::mutex> lk(H.mu);
+        auto it = H.live.find(p);
+        if (it == H.live.end()) return;
+        b = it->second;
+        H.live.erase(it);
+    }
+    cmg::gpu::host_block_release(p, b.first, b.second);
 }
 
 const char* cmg_version(void) { return "0.5.0"; }

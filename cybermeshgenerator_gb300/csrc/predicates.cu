@@ -22,10 +22,13 @@
 //   k_pred_exact  expansion arithmetic (cmg_exact.cuh).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/cmg_c/cmg_gpu.h"
 #include "cmg_device.cuh"
@@ -204,6 +207,50 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t i0, int64
         }
         push(live && sg == 0, i, list, count);
     }
+}
+
+// The FP32 pass over coordinates the device reads straight from host memory (a
+// system whose GPU shares the host's page tables): each query is loaded once over
+// the host link, certified, and its coordinates stored to the device columns `dst`
+// that the FP64 and exact passes read.
+template <int NPT>
+__global__ void __launch_bounds__(kThreads) k_pred_fp32_pull(Soa src, Soa dst, int64_t n,
+                                                             int8_t* __restrict__ out,
+                                                             int64_t* __restrict__ list,
+                                                             unsigned long long* __restrict__ count) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t n_round = (n + 31) & ~int64_t(31);
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
+         i += stride) {
+        int sg = 0;
+        const bool live = i < n;
+        if (live) {
+            double v[3 * NPT];
+#pragma unroll
+            for (int k = 0; k < 3 * NPT; ++k) v[k] = src.c[k][i];
+#pragma unroll
+            for (int k = 0; k < 3 * NPT; ++k) const_cast<double*>(dst.c[k])[i] = v[k];
+            sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
+            out[i] = static_cast<int8_t>(sg);
+        }
+        push(live && sg == 0, i, list, count);
+    }
+}
+
+// Bytes [0, n) of src to dst (host memory written by the device): 16-byte words
+// when dst is 16-byte aligned (src always is), single bytes otherwise and for the
+// tail.
+__global__ void k_put_bytes(const int8_t* __restrict__ src, int8_t* __restrict__ dst, int64_t n) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        const int64_t nw = n / 16;
+        for (int64_t w = t0; w < nw; w += stride)
+            reinterpret_cast<uint4*>(dst)[w] = reinterpret_cast<const uint4*>(src)[w];
+        done = nw * 16;
+    }
+    for (int64_t i = done + t0; i < n; i += stride) dst[i] = src[i];
 }
 
 // ---- the FP32 pass with the columns moved by the TMA engine ----------------------
@@ -448,6 +495,12 @@ struct PredWork {
     Arena arena;
     std::mutex mu;
     cudaEvent_t ev[2] = {nullptr, nullptr};  // around the FP32 pass of the last stream
+    // host-resident streams: the copy stream, buffer-set events and per-chunk FP32
+    // pass events
+    cudaStream_t copy = nullptr;
+    cudaEvent_t in[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> chunk_ev;
+    int pull = -1;  // the device reads pageable host memory (-1: not asked yet)
 };
 PredWork& pred_work() {
     static PredWork w[64];
@@ -464,7 +517,35 @@ struct Counters {
     unsigned long long fault;      // a TMA wait of the FP32 pass ran out
 };
 
+// Queries per chunk of a host-resident stream (two buffer sets of up to 15 columns:
+// at most 1 GB of device memory).
+constexpr int64_t kHostChunk = int64_t{1} << 22;
+// Queries per chunk when the device reads host memory itself (one set of device
+// columns: at most 2 GB).
+constexpr int64_t kPullChunk = int64_t{1} << 24;
+
 }  // namespace
+
+// The FP64 pass over the queries the FP32 pass left, then the exact pass.
+static void pred_stream_finish(int npt, const Soa& s, int mode, int8_t* d_out, int64_t* list_a,
+                               int64_t* list_b, Counters* c, cudaStream_t st, int sms) {
+    if (npt == 4 && mode == kPredExact)
+        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
+    else if (npt == 4)
+        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
+    else if (mode == kPredExact)
+        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
+    else
+        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+                                                                      &c->certified);
+    CMG_LAUNCH();
+    if (npt == 4) k_pred_exact<4><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
+    else k_pred_exact<5><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
+    CMG_LAUNCH();
+}
 
 // Runs the three passes on device-resident SoA coordinates.
 void pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
@@ -514,22 +595,7 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
             CMG_LAUNCH();
         }
     }
-    if (npt == 4 && mode == kPredExact)
-        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
-                                                                      &c->certified);
-    else if (npt == 4)
-        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
-                                                                      &c->certified);
-    else if (mode == kPredExact)
-        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
-                                                                      &c->certified);
-    else
-        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
-                                                                      &c->certified);
-    CMG_LAUNCH();
-    if (npt == 4) k_pred_exact<4><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
-    else k_pred_exact<5><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
-    CMG_LAUNCH();
+    pred_stream_finish(npt, s, mode, d_out, list_a, list_b, c, st, sms);
 }
 
 }  // namespace cmg::gpu
@@ -541,6 +607,22 @@ void set_err(char* buf, size_t len, const std::string& msg) {
         std::strncpy(buf, msg.c_str(), len - 1);
         buf[len - 1] = '\0';
     }
+}
+
+// Whether host-resident streams are read by the device directly: when the device
+// accesses pageable host memory (cudaDevAttrPageableMemoryAccess), unless the
+// environment variable CMG_HOST_STREAM is "copy" (copy calls through two device
+// buffer sets instead; "pull" or unset: direct when supported).
+bool use_pull(cmg::gpu::PredWork& w) {
+    if (w.pull < 0) {
+        int dev = 0, v = 0;
+        CMG_CUDA(cudaGetDevice(&dev));
+        CMG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev));
+        w.pull = v ? 1 : 0;
+    }
+    const char* e = std::getenv("CMG_HOST_STREAM");
+    if (e && std::strcmp(e, "copy") == 0) return false;
+    return w.pull == 1;
 }
 
 cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode, int where,
@@ -575,34 +657,173 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             *lb = a.take<int64_t>(n);
             *cnt = a.take<Counters>(1);
         };
-        const double* dc[15];
-        int8_t* dout;
-        int64_t *la, *lb;
-        void* cnt;
-        w.arena.clear_need();
-        plan(w.arena, dc, &dout, &la, &lb, &cnt);
-        if (w.arena.overflowed()) {
-            w.arena.reserve(w.arena.need());
-            plan(w.arena, dc, &dout, &la, &lb, &cnt);
-        }
-        if (host)
-            for (int k = 0; k < 3 * npt; ++k)
-                CMG_CUDA(cudaMemcpyAsync(const_cast<double*>(dc[k]), coords[k], sizeof(double) * n,
-                                         cudaMemcpyHostToDevice, st));
         if (!w.ev[0])
             for (cudaEvent_t& e : w.ev) CMG_CUDA(cudaEventCreate(&e));
-        pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout, la,
-                           lb, cnt, st, sms, w.ev);
+        const int ncol = 3 * npt;
         Counters hc{};
-        CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-        if (host) CMG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, st));
-        CMG_CUDA(cudaStreamSynchronize(st));
+        if (!host) {
+            const double* dc[15];
+            int8_t* dout;
+            int64_t *la, *lb;
+            void* cnt;
+            w.arena.clear_need();
+            plan(w.arena, dc, &dout, &la, &lb, &cnt);
+            if (w.arena.overflowed()) {
+                w.arena.reserve(w.arena.need());
+                plan(w.arena, dc, &dout, &la, &lb, &cnt);
+            }
+            pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout,
+                               la, lb, cnt, st, sms, w.ev);
+            CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+            CMG_CUDA(cudaStreamSynchronize(st));
+            if (stats) CMG_CUDA(cudaEventElapsedTime(&stats->fp32_pass_ms, w.ev[0], w.ev[1]));
+        } else if (use_pull(w)) {
+            // Host arrays read by the device through the host's page tables (the GPU
+            // and CPU share them over the coherent link): no copy calls. Per chunk the
+            // FP32 pass pulls each query over the link once and stores it to device
+            // columns for the FP64 and exact passes; the device writes the signs back.
+            const int64_t chunk = std::min<int64_t>(n, kPullChunk);
+            const int64_t nch = (n + chunk - 1) / chunk;
+            double* col[15];
+            int8_t* sg;
+            int64_t *la, *lb;
+            Counters* cnt;
+            auto plan_pull = [&](Arena& a) {
+                a.reset();
+                for (int k = 0; k < ncol; ++k) col[k] = a.take<double>(chunk);
+                sg = a.take<int8_t>(chunk);
+                la = a.take<int64_t>(chunk);
+                lb = a.take<int64_t>(chunk);
+                cnt = a.take<Counters>(nch);
+            };
+            w.arena.clear_need();
+            plan_pull(w.arena);
+            if (w.arena.overflowed()) {
+                w.arena.reserve(w.arena.need());
+                plan_pull(w.arena);
+            }
+            while (w.chunk_ev.size() < static_cast<size_t>(2 * nch)) {
+                cudaEvent_t e;
+                CMG_CUDA(cudaEventCreate(&e));
+                w.chunk_ev.push_back(e);
+            }
+            CMG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(Counters) * nch, st));
+            for (int64_t c = 0; c < nch; ++c) {
+                const int64_t i0 = c * chunk, m = std::min(chunk, n - i0);
+                Soa src{}, dst{};
+                for (int k = 0; k < ncol; ++k) {
+                    src.c[k] = coords[k] + i0;
+                    dst.c[k] = col[k];
+                }
+                CMG_CUDA(cudaEventRecord(w.chunk_ev[2 * c], st));
+                if (npt == 4)
+                    k_pred_fp32_pull<4><<<8 * sms, kThreads, 0, st>>>(src, dst, m, sg, la, &cnt[c].n32);
+                else
+                    k_pred_fp32_pull<5><<<8 * sms, kThreads, 0, st>>>(src, dst, m, sg, la, &cnt[c].n32);
+                CMG_LAUNCH();
+                CMG_CUDA(cudaEventRecord(w.chunk_ev[2 * c + 1], st));
+                pred_stream_finish(npt, dst, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, sg, la,
+                                   lb, cnt + c, st, sms);
+                k_put_bytes<<<4 * sms, 256, 0, st>>>(sg, reinterpret_cast<int8_t*>(out) + i0, m);
+                CMG_LAUNCH();
+            }
+            std::vector<Counters> hcs(static_cast<size_t>(nch));
+            CMG_CUDA(cudaMemcpyAsync(hcs.data(), cnt, sizeof(Counters) * nch, cudaMemcpyDeviceToHost, st));
+            CMG_CUDA(cudaStreamSynchronize(st));
+            float total = 0.f;
+            for (int64_t c = 0; c < nch; ++c) {
+                hc.n32 += hcs[c].n32;
+                hc.n64 += hcs[c].n64;
+                hc.certified += hcs[c].certified;
+                hc.overflow |= hcs[c].overflow;
+                float ms = 0.f;
+                CMG_CUDA(cudaEventElapsedTime(&ms, w.chunk_ev[2 * c], w.chunk_ev[2 * c + 1]));
+                total += ms;
+            }
+            if (stats) stats->fp32_pass_ms = total;
+        } else {
+            // Host arrays: chunks through two device buffer sets. The copy stream
+            // uploads chunk c+1 while the launch stream certifies chunk c and
+            // downloads its signs; the link, not the certification, sets the pace.
+            const int64_t chunk = std::min<int64_t>(n, kHostChunk);
+            const int64_t nch = (n + chunk - 1) / chunk;
+            double* col[2][15];
+            int8_t* sg[2];
+            int64_t *la, *lb;
+            Counters* cnt;
+            auto plan_host = [&](Arena& a) {
+                a.reset();
+                for (int b = 0; b < 2; ++b) {
+                    for (int k = 0; k < ncol; ++k) col[b][k] = a.take<double>(chunk);
+                    sg[b] = a.take<int8_t>(chunk);
+                }
+                la = a.take<int64_t>(chunk);
+                lb = a.take<int64_t>(chunk);
+                cnt = a.take<Counters>(nch);
+            };
+            w.arena.clear_need();
+            plan_host(w.arena);
+            if (w.arena.overflowed()) {
+                w.arena.reserve(w.arena.need());
+                plan_host(w.arena);
+            }
+            if (!w.copy) {
+                CMG_CUDA(cudaStreamCreateWithFlags(&w.copy, cudaStreamNonBlocking));
+                for (int b = 0; b < 2; ++b) {
+                    CMG_CUDA(cudaEventCreateWithFlags(&w.in[b], cudaEventDisableTiming));
+                    CMG_CUDA(cudaEventCreateWithFlags(&w.done[b], cudaEventDisableTiming));
+                }
+            }
+            while (w.chunk_ev.size() < static_cast<size_t>(2 * nch)) {
+                cudaEvent_t e;
+                CMG_CUDA(cudaEventCreate(&e));
+                w.chunk_ev.push_back(e);
+            }
+            // the launch stream's earlier work comes before the first upload
+            CMG_CUDA(cudaEventRecord(w.done[1], st));
+            CMG_CUDA(cudaStreamWaitEvent(w.copy, w.done[1], 0));
+            auto upload = [&](int64_t c) {
+                const int b = static_cast<int>(c & 1);
+                const int64_t i0 = c * chunk, m = std::min(chunk, n - i0);
+                if (c >= 2) CMG_CUDA(cudaStreamWaitEvent(w.copy, w.done[b], 0));
+                for (int k = 0; k < ncol; ++k)
+                    CMG_CUDA(cudaMemcpyAsync(col[b][k], coords[k] + i0, sizeof(double) * m,
+                                             cudaMemcpyHostToDevice, w.copy));
+                CMG_CUDA(cudaEventRecord(w.in[b], w.copy));
+            };
+            upload(0);
+            for (int64_t c = 0; c < nch; ++c) {
+                const int b = static_cast<int>(c & 1);
+                const int64_t i0 = c * chunk, m = std::min(chunk, n - i0);
+                CMG_CUDA(cudaStreamWaitEvent(st, w.in[b], 0));
+                if (c + 1 < nch) upload(c + 1);
+                const double* dc[15];
+                for (int k = 0; k < ncol; ++k) dc[k] = col[b][k];
+                pred_stream_device(npt, dc, m, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat,
+                                   sg[b], la, lb, cnt + c, st, sms, &w.chunk_ev[2 * c]);
+                CMG_CUDA(cudaMemcpyAsync(out + i0, sg[b], m, cudaMemcpyDeviceToHost, st));
+                CMG_CUDA(cudaEventRecord(w.done[b], st));
+            }
+            std::vector<Counters> hcs(static_cast<size_t>(nch));
+            CMG_CUDA(cudaMemcpyAsync(hcs.data(), cnt, sizeof(Counters) * nch, cudaMemcpyDeviceToHost, st));
+            CMG_CUDA(cudaStreamSynchronize(st));
+            float total = 0.f;
+            for (int64_t c = 0; c < nch; ++c) {
+                hc.n32 += hcs[c].n32;
+                hc.n64 += hcs[c].n64;
+                hc.certified += hcs[c].certified;
+                hc.overflow |= hcs[c].overflow;
+                float ms = 0.f;
+                CMG_CUDA(cudaEventElapsedTime(&ms, w.chunk_ev[2 * c], w.chunk_ev[2 * c + 1]));
+                total += ms;
+            }
+            if (stats) stats->fp32_pass_ms = total;
+        }
         if (stats) {
             stats->queries = n;
             stats->fp64_queries = static_cast<int64_t>(hc.n32);
             stats->exact_queries = static_cast<int64_t>(hc.n64 + hc.certified);
             stats->expansion_queries = static_cast<int64_t>(hc.n64);
-            CMG_CUDA(cudaEventElapsedTime(&stats->fp32_pass_ms, w.ev[0], w.ev[1]));
         }
         if (hc.overflow) {
             set_err(errbuf, len, "insphere: exact expansion exceeded its capacity");

@@ -301,6 +301,15 @@ cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int 
  * adaptive routine's answer), bit for bit, computed on the GPU. */
 cmg_status cmg_orient3d_batch(const double* xyz, int npts, const int* tets, int n, double* out_value);
 
+/* ---- host memory ------------------------------------------------------------ */
+/* No counterpart in the reference. Page-locked host memory from the library's pool
+ * of reused blocks: outputs (stream signs, grids) written there skip the page
+ * faults of freshly mapped memory and the copy engine's staging. At least `bytes`
+ * bytes, or NULL when no memory is left. cmg_host_free returns a block to the pool
+ * (NULL is ignored). */
+void* cmg_host_alloc(size_t bytes);
+void cmg_host_free(void* p);
+
 /* ---- occupancy without allocation ----------------------------------------- */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc (a host
  * framework that owns device memory through its own pool, a loop that may not

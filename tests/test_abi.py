@@ -194,3 +194,18 @@ def test_bulk_triangles_equal_single_facets(lib):
     assert len(a.triangles) == len(b.triangles) == len(tris) + 2
     assert np.array_equal(a.triangles, b.triangles)
     assert np.array_equal(b.triangles[2:], tris)
+
+
+def test_host_blocks_without_gpu(lib):
+    """cmg_host_alloc hands out ordinary heap memory where nothing can be page-locked
+    (no GPU here): the array over it is writable, and its block goes back to the
+    library when the array is collected; a NULL free is ignored."""
+    import gc
+    import cybermeshgenerator_gb300 as cm
+    for _ in range(3):
+        a = cm.host_empty(1 << 20, np.float32)
+        a[:] = 1.5
+        assert a.dtype == np.float32 and a.shape == (1 << 20,) and float(a.sum()) == 1.5 * (1 << 20)
+        del a
+        gc.collect()
+    lib.cmg_host_free(None)

@@ -49,6 +49,49 @@ def test_stream_device_memory(cm):
     assert np.array_equal(out.cpu().numpy(), host)
 
 
+_STREAMS = {}
+
+
+def _stream_case(kind, n):
+    from cybermeshgenerator_gb300 import workloads as W
+    if (kind, n) not in _STREAMS:
+        _STREAMS.clear()
+        _STREAMS[(kind, n)] = W.predicate_stream(n, kind, degenerate=0.1, near=0.1, seed=33)
+    return _STREAMS[(kind, n)]
+
+
+@pytest.mark.parametrize("path", ["pull", "copy"])
+@pytest.mark.parametrize("kind,n", [("orient3d", (1 << 24) + 123_457), ("insphere", (1 << 22) + 1001)])
+def test_host_stream_chunks_match_device_and_oracle(cm, orc, kind, n, path, monkeypatch):
+    """Host arrays, both ways: read by the device through the host's page tables in
+    chunks of 2^24 queries ("pull", where the device supports it), or copied in chunks
+    of 2^22 with the next chunk's upload overlapping this one's certification
+    ("copy"). Signs and counts equal those of one device-resident call; the chunk
+    seams and the ragged tail equal the oracle."""
+    torch = pytest.importorskip("torch")
+    import oracle as O
+    monkeypatch.setenv("CMG_HOST_STREAM", path)
+    S = _stream_case(kind, n)
+    fn = cm.orient3d_stream if kind == "orient3d" else cm.insphere_stream
+    ncol = S.shape[0]
+    d = torch.tensor(S, device="cuda")
+    out = torch.zeros(n, dtype=torch.int8, device="cuda")
+    ptrs = [d[k].data_ptr() for k in range(ncol)]
+    seams = [k << 22 for k in range(1, (n >> 22) + 1)] + [n]
+    idx = np.unique(np.concatenate([np.arange(max(0, b - 3000), min(n, b + 3000)) for b in seams]
+                                   + [np.arange(0, 3000)]))
+    for mode in (cm.PRED_COMPAT, cm.PRED_EXACT):
+        host, st = fn(S, mode)
+        _, dst = fn((ptrs, n, out.data_ptr()), mode, stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), host)
+        for k in ("queries", "fp64_queries", "exact_queries", "expansion_queries"):
+            assert st[k] == dst[k], k
+        want = orc.stream(kind, np.ascontiguousarray(S[:, idx]), O.COMPAT if mode == cm.PRED_COMPAT else O.EXACT)
+        assert np.array_equal(host[idx], want)
+    del d
+
+
 def _lcg_cloud(n, s):
     # the point cloud of tests/test_backend.cpp:14-18 (LCG, 24-bit fractions)
     pts = []
