@@ -1045,11 +1045,18 @@ def run_simplify(args):
                        "d2h_bytes_per_step": int(24 * nrep + 12 * nkept),
                        "call": "cmg_plc_simplify (PLC handle -> PLC handle)"}
         # a fine grid keeps most triangles: the dedupe table and output dominate
-        t0 = time.perf_counter()
+        # (1 warm-up call, then the mean of 3)
         fine = cm.simplify(plc, 512)
-        tf = time.perf_counter() - t0
-        line["grid512"] = {"device_triangles_per_s": T / (cm.simplify_last_timing()["cluster_ms"] * 1e-3),
-                           "e2e_triangles_per_s": T / tf, "representatives": int(fine.num_points),
+        tf, cl = [], []
+        for _ in range(3):
+            del fine
+            t0 = time.perf_counter()
+            fine = cm.simplify(plc, 512)
+            tf.append(time.perf_counter() - t0)
+            cl.append(cm.simplify_last_timing()["cluster_ms"])
+        line["grid512"] = {"device_triangles_per_s": T / (sum(cl) / len(cl) * 1e-3),
+                           "e2e_triangles_per_s": T / (sum(tf) / len(tf)),
+                           "representatives": int(fine.num_points),
                            "kept": int(len(fine.triangles))}
         if not args.no_cpu:
             v = _simplify_cpu(pts, tris, grid, args.cpu_seconds)

@@ -41,15 +41,17 @@ struct Region {
 
 }  // namespace
 
+// Large arrays in pooled page-locked host memory (cmg::gpu::HostVec): the device
+// reads and fills them without staging or first-touch faults.
 struct cmg_plc {
-    std::vector<double> points;            // 3 per point
-    std::vector<int> fidx;                 // facet polygons, concatenated
-    std::vector<size_t> foff{0};           // facet f is fidx[foff[f] .. foff[f+1])
-    std::vector<int> markers;
+    cmg::gpu::HostVec<double> points;      // 3 per point
+    cmg::gpu::HostVec<int> fidx;           // facet polygons, concatenated
+    cmg::gpu::HostVec<size_t> foff{0};     // facet f is fidx[foff[f] .. foff[f+1])
+    cmg::gpu::HostVec<int> markers;
     std::vector<double> holes;
     std::vector<Region> regions;
-    std::vector<double> pts_cache;
-    std::vector<int> tri_cache;
+    cmg::gpu::HostVec<double> pts_cache;
+    cmg::gpu::HostVec<int> tri_cache;
 };
 
 struct cmg_options {
@@ -128,23 +130,35 @@ cudaStream_t gpu_stream() {
 
 // Fan triangulation (v0, v[i-1], v[i]) of every facet polygon
 // (src/voxelize/voxelize.cpp:29-38).
-std::vector<int> fan(const cmg_plc& p) {
-    std::vector<int> t;
-    t.reserve(3 * (p.fidx.size() - 2 * (p.foff.size() - 1)));
-    for (size_t f = 0; f + 1 < p.foff.size(); ++f) {
+cmg::gpu::HostVec<int> fan(const cmg_plc& p) {
+    const size_t nf = p.foff.size() - 1;
+    size_t total = 0;
+    bool all3 = true;
+    for (size_t f = 0; f < nf; ++f) {
+        const size_t n = p.foff[f + 1] - p.foff[f];
+        total += n >= 3 ? 3 * (n - 2) : 0;
+        all3 = all3 && n == 3;
+    }
+    cmg::gpu::HostVec<int> t(total);
+    if (all3 && total == p.fidx.size()) {  // every facet a triangle: as stored
+        std::memcpy(t.data(), p.fidx.data(), sizeof(int) * total);
+        return t;
+    }
+    size_t o = 0;
+    for (size_t f = 0; f < nf; ++f) {
         const int* v = p.fidx.data() + p.foff[f];
         const size_t n = p.foff[f + 1] - p.foff[f];
         for (size_t i = 2; i < n; ++i) {
-            t.push_back(v[0]);
-            t.push_back(v[i - 1]);
-            t.push_back(v[i]);
+            t[o++] = v[0];
+            t[o++] = v[i - 1];
+            t[o++] = v[i];
         }
     }
     return t;
 }
 
 // make_grid (src/voxelize/voxelize.cpp:52-74), same operations in the same order.
-bool make_grid(const std::vector<double>& pts, int resolution, int pad, GridDesc& g) {
+bool make_grid(const cmg::gpu::HostVec<double>& pts, int resolution, int pad, GridDesc& g) {
     const size_t n = pts.size() / 3;
     double lo[3] = {pts[0], pts[1], pts[2]}, hi[3] = {pts[0], pts[1], pts[2]};
     for (size_t i = 0; i < n; ++i)
@@ -177,9 +191,9 @@ struct CoreError {
 // Validation of voxelize (src/voxelize/voxelize.cpp:362-379) plus index checks
 // (an out-of-range facet index is undefined behaviour in the reference; here it
 // is an InvalidInput error, since the GPU must never read outside its inputs).
-std::vector<int> checked_triangles(const cmg_plc& p) {
+cmg::gpu::HostVec<int> checked_triangles(const cmg_plc& p) {
     if (p.points.empty()) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no points"};
-    std::vector<int> t = fan(p);
+    cmg::gpu::HostVec<int> t = fan(p);
     if (t.empty())
         throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no boundary triangles"};
     const int64_t np = static_cast<int64_t>(p.points.size() / 3);
@@ -250,7 +264,7 @@ void set_geometry(cmg_voxels* v, const GridDesc& g) {
 cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
     if (!o.explicit_grid && o.resolution < 1)
         throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
-    std::vector<int> tris = checked_triangles(p);
+    cmg::gpu::HostVec<int> tris = checked_triangles(p);
     GridDesc g{};
     if (o.explicit_grid) {
         for (int a = 0; a < 3; ++a) g.corner[a] = o.corner[a];
@@ -498,7 +512,7 @@ cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, 
     if (!plcs || !opts || !out || n < 1) return CMG_ERR_INVALID_INPUT;
     if (!opts->explicit_grid && (!resolutions || !pads)) return CMG_ERR_INVALID_INPUT;
     return guarded(errbuf, len, [&] {
-        std::vector<std::vector<int>> tris(static_cast<size_t>(n));
+        std::vector<cmg::gpu::HostVec<int>> tris(static_cast<size_t>(n));
         std::vector<cmg::gpu::HostMesh> meshes(static_cast<size_t>(n));
         std::unique_ptr<cmg_batch> b(new cmg_batch);
         for (int i = 0; i < n; ++i) {
@@ -856,8 +870,8 @@ std::string lower_ext(const std::string& path) {
 }
 
 cmg_plc* plc_from_stl(const char* bytes, size_t n) {
-    std::vector<double> pts;
-    std::vector<int> tris;
+    cmg::gpu::HostVec<double> pts;
+    cmg::gpu::HostVec<int> tris;
     {
         std::lock_guard<std::mutex> lk(gpu_mutex());
         cmg::gpu::stl_read(bytes, n, pts, tris, gpu_stream());
@@ -945,8 +959,8 @@ cmg_status cmg_plc_simplify(const cmg_plc* in, int grid, cmg_plc** out, char* er
         // simplify.cpp:49-54, answered before any device is touched
         if (in->points.empty()) throw CoreError{CMG_ERR_INVALID_INPUT, "simplify: PLC has no points"};
         if (grid < 1) throw CoreError{CMG_ERR_INVALID_INPUT, "simplify: grid must be >= 1"};
-        std::vector<double> pts;
-        std::vector<int> tris;
+        cmg::gpu::HostVec<double> pts;
+        cmg::gpu::HostVec<int> tris;
         {
             std::lock_guard<std::mutex> lk(gpu_mutex());
             cmg::gpu::simplify(in->points.data(), static_cast<int64_t>(in->points.size() / 3),

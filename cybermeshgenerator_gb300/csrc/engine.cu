@@ -88,6 +88,51 @@ void host_block_release(void* p, size_t cap, bool pinned) {
     cudaFreeHost(p);
 }
 
+namespace {
+constexpr size_t kLargeHost = size_t{1} << 20;
+struct LargeBlocks {
+    std::mutex mu;
+    std::map<void*, std::pair<size_t, bool>> live;  // block -> capacity, page-locked
+};
+LargeBlocks& large_blocks() {
+    static LargeBlocks* b = new LargeBlocks;  // never destroyed, like the pool
+    return *b;
+}
+}  // namespace
+
+void* host_large_alloc(size_t bytes) {
+    if (bytes < kLargeHost) {
+        void* p = std::malloc(bytes ? bytes : 1);
+        if (!p) throw std::bad_alloc();
+        return p;
+    }
+    size_t cap = 0;
+    bool pinned = false;
+    void* p = host_block_acquire(bytes, &cap, &pinned);
+    LargeBlocks& L = large_blocks();
+    std::lock_guard<std::mutex> lk(L.mu);
+    L.live[p] = {cap, pinned};
+    return p;
+}
+
+void host_large_free(void* p, size_t bytes) noexcept {
+    if (!p) return;
+    if (bytes < kLargeHost) {
+        std::free(p);
+        return;
+    }
+    std::pair<size_t, bool> b{0, false};
+    {
+        LargeBlocks& L = large_blocks();
+        std::lock_guard<std::mutex> lk(L.mu);
+        auto it = L.live.find(p);
+        if (it == L.live.end()) return;
+        b = it->second;
+        L.live.erase(it);
+    }
+    host_block_release(p, b.first, b.second);
+}
+
 int device_sms() {
     int dev = 0, sms = 0;
     CMG_CUDA(cudaGetDevice(&dev));

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "cmg_types.h"
+#include "host_mem.h"
 
 namespace cmg::gpu {
 
@@ -46,15 +47,6 @@ struct HostMesh {
     int64_t ntris = 0;
     GridDesc g{};
 };
-
-// Page-locked host blocks, kept for reuse after release: a device-to-host copy
-// into one runs at the link's rate (no staging through the driver's bounce
-// buffers), and pinning is paid once per block rather than once per call. A block
-// of `bytes` or more is returned with its capacity; when pinning fails the block is
-// ordinary heap memory (*pinned = false). Released blocks beyond the pool's cap of
-// cached bytes are freed. Thread-safe.
-void* host_block_acquire(size_t bytes, size_t* cap, bool* pinned);
-void host_block_release(void* p, size_t cap, bool pinned);
 
 // Host array filled by a device copy: allocated without value-initialisation, from
 // the page-locked block pool.

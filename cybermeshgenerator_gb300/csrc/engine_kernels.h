@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "cmg_types.h"
+#include "host_mem.h"
 
 namespace cmg::gpu {
 
@@ -84,7 +85,7 @@ void adjoint_backward(int precision, const GridDesc& g, int64_t ncell, const dou
 // stl.cu: an STL image (host bytes) -> merged points (3 doubles each, first-occurrence
 // order) and triangles (3 indices each), as the reference's read_stl; throws
 // std::invalid_argument with its messages.
-void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vector<int>& tris,
+void stl_read(const char* bytes, size_t len, HostVec<double>& pts, HostVec<int>& tris,
               cudaStream_t st);
 // Phase times of the last stl_read on this device (CUDA events): upload of the
 // records (or parsed coordinates), decode + merge kernels, download of the arrays.
@@ -106,7 +107,7 @@ float self_intersections_last_ms();
 // offsets), as the reference's cmg::simplify::simplify. Throws std::invalid_argument
 // with the reference's message on invalid input.
 void simplify(const double* pts, int64_t npts, const int* fidx, int64_t nidx, const size_t* foff,
-              int64_t nfacets, int grid, std::vector<double>& out_pts, std::vector<int>& out_tris,
+              int64_t nfacets, int grid, HostVec<double>& out_pts, HostVec<int>& out_tris,
               cudaStream_t st);
 // Device times of the last simplify: host-to-device copy, clustering, device-to-host copy.
 void simplify_last_timing(float* upload_ms, float* cluster_ms, float* download_ms);

@@ -359,7 +359,7 @@ SimplifyWork& simplify_work() {
 }  // namespace
 
 void simplify(const double* pts, int64_t npts, const int* fidx, int64_t nidx, const size_t* foff,
-              int64_t nfacets, int grid, std::vector<double>& out_pts, std::vector<int>& out_tris,
+              int64_t nfacets, int grid, HostVec<double>& out_pts, HostVec<int>& out_tris,
               cudaStream_t st) {
     if (npts <= 0) throw std::invalid_argument("simplify: PLC has no points");
     if (grid < 1) throw std::invalid_argument("simplify: grid must be >= 1");

@@ -231,7 +231,7 @@ void parse_ascii(const char* b, size_t len, std::vector<double>& v) {
 
 }  // namespace
 
-void stl_read(const char* bytes, size_t len, std::vector<double>& pts, std::vector<int>& tris,
+void stl_read(const char* bytes, size_t len, HostVec<double>& pts, HostVec<int>& tris,
               cudaStream_t st) {
     bool binary = false;
     uint32_t n = 0;
