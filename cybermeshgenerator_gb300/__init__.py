@@ -232,8 +232,9 @@ class SizingField:
                                                 w.data_ptr() if which else None, st, err, 256), err)
             return (out, w) if which else out
         q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 3)
-        out = np.empty(len(q))
-        w = np.empty(len(q), dtype=np.int32) if which else None
+        alloc = host_empty if len(q) >= 65536 else (lambda n, dt: np.empty(n, dtype=dt))
+        out = alloc(len(q), np.float64)
+        w = alloc(len(q), np.int32) if which else None
         _check(_clib.cmg_sizing_eval(self._h, q.ctypes.data_as(_L.c_double_p), len(q),
                                      out.ctypes.data_as(_L.c_double_p),
                                      w.ctypes.data_as(_L.c_int_p) if which else None, err, 256), err)
@@ -539,7 +540,7 @@ def _stream_call(fn, npt, soa, mode, stream=None):
             raise ValueError(f"expected {3 * npt} coordinate rows")
         n = soa.shape[1]
         rows = (ctypes.c_void_p * (3 * npt))(*[soa[k].ctypes.data for k in range(3 * npt)])
-        out = host_empty(n, np.int8)
+        out = host_empty(n, np.int8) if n >= 65536 else np.zeros(n, dtype=np.int8)
         st = _L.PredStats()
         err = ctypes.create_string_buffer(512)
         _check(fn(rows, n, int(mode), MEM_HOST, out.ctypes.data_as(ctypes.c_void_p),

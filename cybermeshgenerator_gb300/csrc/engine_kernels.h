@@ -12,6 +12,9 @@
 
 namespace cmg::gpu {
 
+// engine.cu: multiprocessors of the current device.
+int device_sms();
+
 // occupancy.cu
 void launch_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* pts,
                      const int* tris, double* soup, int4* xybox, int64_t* pairs, cudaStream_t st);

@@ -9,7 +9,7 @@
 //                    c_t in the brick grid; triangles larger than two bricks (or
 //                    degenerate) go to a per-mesh "always considered" list
 //   k_bin_fill       bin -> triangle CSR
-//   k_brick_walk     one warp per brick: a ring walk over bins gives an upper bound
+//   k_brick_walk     one CTA per brick: a ring walk over bins gives an upper bound
 //                    U on the distance from the brick centre to the surface, then
 //                    the candidate list = every triangle whose lower bound
 //                    |c - c_t| - e_t - r_B can be <= U + r_B (r_B = brick radius),
@@ -28,6 +28,7 @@
 
 #include <cfloat>
 #include <climits>
+#include <type_traits>
 
 #include "cmg_device.cuh"
 #include "cmg_sdf.cuh"
@@ -344,10 +345,20 @@ __device__ __forceinline__ void for_group_entries(int64_t b0, int64_t b1, int la
     }
 }
 
-// One warp per brick. FILL=false: computes U (stored) and the candidate count;
-// FILL=true: writes the candidates in walk order.
-template <bool FILL>
-__global__ void __launch_bounds__(128)
+// W warps per brick, 4 / W bricks per CTA of 128 threads. With few bricks the walks of
+// the bricks deep inside a closed surface set the kernel's time (tens of thousands of
+// candidates each: every triangle within U + 2 r_B), and W = 4 splits them; with
+// many bricks the GPU is full anyway and W = 1 walks each with one warp. Each
+// shell's 32-bin groups are split into contiguous ranges, one per warp, range w
+// before range w + 1, so the walk order is that of a single walker; the bound U, the
+// stopping rules and the counts are reduced over the brick's warps after each shell
+// (a named barrier per brick). FILL=false: computes U (stored) and the candidate
+// count. FILL=true: per shell each warp counts its candidates, the brick's warps take
+// prefix sums, and each writes its own at its offset, in walk order.
+constexpr int kWalkThreads = 128;
+
+template <bool FILL, int W>
+__global__ void __launch_bounds__(kWalkThreads)
 k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
              const double* __restrict__ soup, const float4* __restrict__ tinfo,
              const float4* __restrict__ tlo, const float4* __restrict__ thi,
@@ -356,9 +367,19 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
              int* __restrict__ cand_cnt, const int64_t* __restrict__ cand_off,
              int* __restrict__ cand, float* __restrict__ brick_emax,
              Stats* __restrict__ st) {
-    const int lane = threadIdx.x & 31;
-    const int64_t gb = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
-    if (gb >= nbricks) return;
+    constexpr int kWarps = kWalkThreads / 32;
+    __shared__ float s_f[kWarps];
+    __shared__ int s_i[kWarps];
+    __shared__ int s_c[kWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int slot = wid / W, sub = wid % W;  // brick within the CTA, warp within the brick
+    const int first = slot * W;               // the brick's first warp
+    const int64_t gb = static_cast<int64_t>(blockIdx.x) * (kWarps / W) + slot;
+    if (gb >= nbricks) return;  // uniform over the brick's warps
+    auto brick_sync = [&]() {
+        if (W == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(32 * W) : "memory");
+    };
     const int si = find_seg<&MeshSeg::brick_begin>(segs, nseg, gb);
     const MeshSeg& s = segs[si];
     const BrickGeo q = brick_geo(s, gb - s.brick_begin);
@@ -366,20 +387,52 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
     const float tol = 8.f * kU32 * s.scale + 1e-30f;
     const float emax = s.emax;
     const int rmax = max(s.bnx, max(s.bny, s.bnz));
+    // reductions over the brick's warps (each of its threads calls them, at points
+    // uniform over the brick)
+    auto cta_min = [&](float v) {
+        v = warp_min(v);
+        if (W == 1) return v;
+        if (lane == 0) s_f[wid] = v;
+        brick_sync();
+        float m = s_f[first];
+#pragma unroll
+        for (int w = 1; w < W; ++w) m = fminf(m, s_f[first + w]);
+        brick_sync();
+        return m;
+    };
+    auto cta_any = [&](bool v) {
+        const bool wv = __any_sync(0xffffffffu, v);
+        if (W == 1) return wv;
+        if (lane == 0) s_i[wid] = wv ? 1 : 0;
+        brick_sync();
+        int a = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) a |= s_i[first + w];
+        brick_sync();
+        return a != 0;
+    };
+    // this warp's contiguous range [g0, g1) of the 32-bin groups of a shell of n bins
+    auto range = [&](int n, int& g0, int& g1) {
+        const int ng = (n + 31) / 32;
+        g0 = static_cast<int>(static_cast<int64_t>(ng) * sub / W);
+        g1 = static_cast<int>(static_cast<int64_t>(ng) * (sub + 1) / W);
+    };
     float U;
     if (!FILL) {
         // ---- upper bound on the distance from the brick centre to the surface
         U = FLT_MAX;
-        for (int64_t e = s.large_begin + lane; e < s.large_end; e += 32)
+        for (int64_t e = s.large_begin + 32 * sub + lane; e < s.large_end; e += 32 * W)
             U = fminf(U, large_upper(soup, large_list[e], s.g.corner, q.cx, q.cy, q.cz, tol));
         for (int r = 0; r <= rmax; ++r) {
-            U = warp_min(U);
+            U = cta_min(U);
             if (r > 0 && (r - 1) * bw > U) break;  // farther bins cannot lower U
             const int n = shell_count(r);
+            int g0, g1;
+            range(n, g0, g1);
             bool inside = false;
-            for (int k0 = 0; k0 < n; k0 += 32) {
+            for (int g = g0; g < g1; ++g) {
                 int64_t b0 = 0, b1 = 0;
-                shell_bin(s, q, bin_off, r, k0 + lane, n, inside, b0, b1);
+                shell_bin(s, q, bin_off, r, 32 * g + lane, n, inside, b0, b1);
                 for_group_entries(b0, b1, lane, [&](const int64_t* e, const bool* ok) {
                     int t[kWalkRounds];
 #pragma unroll
@@ -394,48 +447,27 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
                     }
                 });
             }
-            if (r > 0 && !__any_sync(0xffffffffu, inside)) {
-                U = warp_min(U);
+            if (r > 0 && !cta_any(inside)) {
+                U = cta_min(U);
                 break;
             }
         }
-        U = warp_min(U);
-        if (lane == 0) bound[gb] = U;
+        U = cta_min(U);
+        if (sub == 0 && lane == 0) bound[gb] = U;
     } else {
         U = bound[gb];
     }
     // ---- candidates: lower bound <= U + 2 r_B (+ margins)
     const float lim = (U + 2.f * q.rb) * (1.f + 1e-5f) + 2.f * tol;
-    int count = 0;
-    int64_t out = FILL ? cand_off[gb] : 0;
+    const int64_t out = FILL ? cand_off[gb] : 0;
+    const unsigned below = (1u << lane) - 1u;
     float bemax = 0.f;
-    auto emit = [&](bool take, int t, float et) {
-        unsigned m = __ballot_sync(0xffffffffu, take);
-        if (FILL && take) cand[out + count + __popc(m & ((1u << lane) - 1u))] = t;
-        if (take) bemax = fmaxf(bemax, et);
-        count += __popc(m);
-    };
-    for (int64_t e0 = s.large_begin; e0 < s.large_end; e0 += 32) {
-        int64_t e = e0 + lane;
-        bool take = false;
-        int t = 0;
-        float et = 0.f;
-        if (e < s.large_end) {
-            t = large_list[e];
-            float4 lo = tlo[t], hi = thi[t];
-            float d = aabb_dist(q.cx, q.cy, q.cz, lo, hi);
-            take = d <= lim;  // d(v,t) >= d - r_B must reach U + r_B
-            et = tinfo[t].w;
-        }
-        emit(take, t, et);
-    }
-    for (int r = 0; r <= rmax; ++r) {
-        if (r > 0 && (r - 1) * bw - emax > lim) break;
-        const int n = shell_count(r);
-        bool any_inside = false;
-        for (int k0 = 0; k0 < n; k0 += 32) {
+    // walks this warp's groups of shell r; f(take, t, e_t) per entry, in walk order,
+    // called by the whole warp
+    auto walk = [&](int r, int n, int g0, int g1, bool& inside, auto&& f) {
+        for (int g = g0; g < g1; ++g) {
             int64_t b0 = 0, b1 = 0;
-            shell_bin(s, q, bin_off, r, k0 + lane, n, any_inside, b0, b1);
+            shell_bin(s, q, bin_off, r, 32 * g + lane, n, inside, b0, b1);
             for_group_entries(b0, b1, lane, [&](const int64_t* e, const bool* ok) {
                 int t[kWalkRounds];
 #pragma unroll
@@ -454,19 +486,100 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
                         take = d - ti[j].w <= lim;  // |v - c_t| - e_t >= d - r_B - e_t
                         et = ti[j].w;
                     }
-                    emit(take, t[j], et);
+                    f(take, t[j], et);
                 }
             });
         }
-        if (r > 0 && !__any_sync(0xffffffffu, any_inside)) break;
+    };
+    // the always-considered large triangles first, by the brick's first warp
+    if (sub == 0) {
+        int c = 0;
+        for (int64_t e0 = s.large_begin; e0 < s.large_end; e0 += 32) {
+            const int64_t e = e0 + lane;
+            bool take = false;
+            int t = 0;
+            float et = 0.f;
+            if (e < s.large_end) {
+                t = large_list[e];
+                float4 lo = tlo[t], hi = thi[t];
+                float d = aabb_dist(q.cx, q.cy, q.cz, lo, hi);
+                take = d <= lim;  // d(v,t) >= d - r_B must reach U + r_B
+                et = tinfo[t].w;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (FILL && take) cand[out + c + __popc(m & below)] = t;
+            if (take) bemax = fmaxf(bemax, et);
+            c += __popc(m);
+        }
+        if (lane == 0) s_c[first] = c;
     }
-    if (!FILL && lane == 0) {
-        cand_cnt[gb] = count;
-        atomicAdd(&st->candidates, static_cast<unsigned long long>(count));
+    brick_sync();
+    int64_t base = s_c[first];  // entries before the current shell
+    brick_sync();
+    int mine = 0;           // count pass: this warp's entries over all shells
+    for (int r = 0; r <= rmax; ++r) {
+        if (r > 0 && (r - 1) * bw - emax > lim) break;
+        const int n = shell_count(r);
+        int g0, g1;
+        range(n, g0, g1);
+        bool any_inside = false;
+        int c = 0;
+        if (FILL && W == 1) {
+            // one warp per brick: written in the one walk, at a running offset
+            walk(r, n, g0, g1, any_inside, [&](bool take, int t, float et) {
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                if (take) {
+                    cand[out + base + c + __popc(m & below)] = t;
+                    bemax = fmaxf(bemax, et);
+                }
+                c += __popc(m);
+            });
+            base += c;
+        } else {
+            walk(r, n, g0, g1, any_inside,
+                 [&](bool take, int, float) { c += __popc(__ballot_sync(0xffffffffu, take)); });
+        }
+        if (FILL && W > 1) {
+            // several warps: prefix sums of this shell's counts, then the writing walk
+            if (lane == 0) s_c[wid] = c;
+            brick_sync();
+            int64_t off = base;
+            int tot = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                if (w < sub) off += s_c[first + w];
+                tot += s_c[first + w];
+            }
+            brick_sync();
+            int k = 0;
+            bool again = false;
+            walk(r, n, g0, g1, again, [&](bool take, int t, float et) {
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                if (take) {
+                    cand[out + off + k + __popc(m & below)] = t;
+                    bemax = fmaxf(bemax, et);
+                }
+                k += __popc(m);
+            });
+            base += tot;
+        } else if (!FILL) {
+            mine += c;
+        }
+        if (r > 0 && !cta_any(any_inside)) break;
     }
-    if (FILL) {
-        bemax = warp_min(-bemax);
-        if (lane == 0) brick_emax[gb] = -bemax;
+    if (!FILL) {
+        if (lane == 0) s_c[wid] = mine;
+        brick_sync();
+        if (sub == 0 && lane == 0) {
+            int64_t total = base;
+#pragma unroll
+            for (int w = 0; w < W; ++w) total += s_c[first + w];
+            cand_cnt[gb] = static_cast<int>(total);
+            atomicAdd(&st->candidates, static_cast<unsigned long long>(total));
+        }
+    } else {
+        bemax = -cta_min(-bemax);
+        if (sub == 0 && lane == 0) brick_emax[gb] = bemax;
     }
 }
 
@@ -955,15 +1068,32 @@ void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks
                        float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
                        float* brick_emax, Stats* stats, cudaStream_t st) {
     if (nbricks == 0) return;
-    unsigned grid = static_cast<unsigned>((nbricks + 3) / 4);
-    if (fill)
-        k_brick_walk<true><<<grid, 128, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi, bin_off,
-                                                 bin_list, large_list, bound, cand_cnt, cand_off,
-                                                 cand, brick_emax, stats);
-    else
-        k_brick_walk<false><<<grid, 128, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi,
-                                                  bin_off, bin_list, large_list, bound, cand_cnt,
-                                                  cand_off, cand, brick_emax, stats);
+    // warps per brick: 4 while 4-warp bricks fit about twice in the GPU's warp slots
+    // (a few heavy bricks set the time), 2 up to twice that, then 1
+    const int64_t sms = device_sms();
+    const int W = nbricks <= 32 * sms ? 4 : (nbricks <= 64 * sms ? 2 : 1);
+    const unsigned grid = static_cast<unsigned>((nbricks * W + 3) / 4);
+    auto go = [&](auto fill_tag, auto w_tag) {
+        constexpr bool F = decltype(fill_tag)::value;
+        constexpr int WW = decltype(w_tag)::value;
+        k_brick_walk<F, WW><<<grid, kWalkThreads, 0, st>>>(segs, nseg, nbricks, soup, tinfo, tlo, thi,
+                                                           bin_off, bin_list, large_list, bound,
+                                                           cand_cnt, cand_off, cand, brick_emax, stats);
+    };
+    using T = std::true_type;
+    using Fa = std::false_type;
+    using W1 = std::integral_constant<int, 1>;
+    using W2 = std::integral_constant<int, 2>;
+    using W4 = std::integral_constant<int, 4>;
+    if (fill) {
+        if (W == 4) go(T{}, W4{});
+        else if (W == 2) go(T{}, W2{});
+        else go(T{}, W1{});
+    } else {
+        if (W == 4) go(Fa{}, W4{});
+        else if (W == 2) go(Fa{}, W2{});
+        else go(Fa{}, W1{});
+    }
     CMG_LAUNCH();
 }
 
