@@ -280,9 +280,13 @@ typedef struct cmg_pred_stats {
  * reference's robust::orient3d as initialised: the rounded determinant's sign
  * unless it is exactly zero, src/predicates/robust.cpp:36-42) or CMG_PRED_EXACT.
  * where: CMG_MEM_HOST (arrays and out in host memory) or CMG_MEM_DEVICE (device
- * memory; stream is the cudaStream_t to use, NULL for the default). The call
- * returns when the signs are written. stats may be NULL. No counterpart in the
- * reference beyond the scalar predicate it applies per query. */
+ * memory; stream is the cudaStream_t to use, NULL for the default). Host arrays are
+ * read by the device directly where it accesses pageable host memory
+ * (cudaDevAttrPageableMemoryAccess), in chunks of 2^24 queries, and otherwise copied
+ * in chunks of 2^22 through two device buffer sets (the environment variable
+ * CMG_HOST_STREAM=copy forces the copies). The call returns when the signs are
+ * written. stats may be NULL (fp32_pass_ms: summed over the chunks). No counterpart
+ * in the reference beyond the scalar predicate it applies per query. */
 cmg_status cmg_orient3d_stream(const double* const* coords, int64_t n, int mode, int where,
                                signed char* out, cmg_pred_stats* stats, void* stream,
                                char* errbuf, size_t errbuf_len);
