@@ -61,6 +61,31 @@ def test_scale_fp64_sampled_bit_exact(cm, orc, c5):
     assert np.array_equal(np.abs(r.sdf64[vox]), np.sqrt(d2))
 
 
+def test_two_warps_per_brick_walk(cm, orc, c5):
+    """The same surface at 320^3: 8000 candidate bricks, between 32 and 64 per SM, so the
+    brick walk runs with two warps per brick (the headline grid takes four, the 512^3
+    grid one). Plain FP64 distances bit for bit and mixed ones within 1e-6 of the
+    diagonal on sampled cells, occupancy bit for bit."""
+    torch = pytest.importorskip("torch")
+    import oracle as O
+    g = orc.make_grid(c5["pts"], 318, 1)
+    nb = -(-g.nx // 16) * -(-g.ny // 16) * -(-g.nz // 16)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert 32 * sms < nb <= 64 * sms, (nb, sms)
+    occ, _ = orc.occupancy(c5["pts"], c5["tris"], g, O.COMPAT)
+    rng = np.random.default_rng(53)
+    plain = cm.voxelize_ex(c5["plc"], resolution=318, pad=1,
+                           outputs=cm.OUT_OCCUPANCY | cm.OUT_SDF_F64, precision=cm.PREC_FP64)
+    mixed = cm.voxelize_ex(c5["plc"], resolution=318, pad=1,
+                           outputs=cm.OUT_OCCUPANCY | cm.OUT_SDF_F32, precision=cm.PREC_MIXED)
+    assert np.array_equal(plain.occupancy, occ) and np.array_equal(mixed.occupancy, occ)
+    vox = _samples(g, plain.sdf64, rng)
+    d2, _ = orc.dist2_points(c5["pts"], c5["tris"], _centres(g, vox))
+    assert np.array_equal(np.abs(plain.sdf64[vox]), np.sqrt(d2))
+    want = np.where(occ[vox] != 0, -1.0, 1.0) * np.sqrt(d2)
+    assert np.abs(mixed.sdf32[vox].astype(np.float64) - want).max() <= 1e-6 * c5["diag"]
+
+
 def test_scale_adjoint_matches_host_gradient(cm, orc, c5):
     torch = pytest.importorskip("torch")
     from cybermeshgenerator_gb300 import torch_sdf as TS
