@@ -209,3 +209,20 @@ def test_host_blocks_without_gpu(lib):
         del a
         gc.collect()
     lib.cmg_host_free(None)
+
+
+def test_large_triangle_plc_readback(lib):
+    """A PLC of triangles only, with arrays above the 1 MiB pool threshold: points and
+    fan triangles read back as given (the fan of a triangle is itself, copied as
+    stored), and an appended quad switches the readback to the general fan."""
+    import cybermeshgenerator_gb300 as cm
+    rng = np.random.default_rng(7)
+    pts = rng.random((200_000, 3))
+    tris = rng.integers(0, len(pts), size=(400_000, 3)).astype(np.int32)
+    plc = cm.PLC.from_arrays(pts, tris)
+    assert np.array_equal(plc.points, pts)
+    assert np.array_equal(plc.triangles, tris)
+    plc.add_facet([0, 1, 2, 3])
+    t = plc.triangles
+    assert len(t) == len(tris) + 2 and np.array_equal(t[:-2], tris)
+    assert t[-2:].tolist() == [[0, 1, 2], [0, 2, 3]]
