@@ -637,7 +637,7 @@ def run_stream(args):
     if rank == 0 or world == 1:
         B.build()
     barrier(world)
-    n = STREAM_N
+    n = args.stream_n
     dev, outs, host = {}, {}, {}
     for kind, seed in (("orient3d", 1000), ("insphere", 2000)):
         host[kind] = _stream_soa(kind, n, seed)
@@ -692,7 +692,7 @@ def run_stream(args):
         line["sample_parity"] = {"queries": 400_000, "equal": ok}
         # the harder mix: the same plus 10 % of queries within a few ulps of a tie
         # (the first 2e7 of each kind, replaced in place and restored afterwards)
-        m = 2 * STREAM_CHUNK
+        m = min(2 * STREAM_CHUNK, n)
         hard_stats, hard_ms = {}, 0.0
         for kind, fn, seed in (("orient3d", cm.orient3d_stream, 3000),
                                ("insphere", cm.insphere_stream, 4000)):
@@ -1276,6 +1276,8 @@ def main():
     ap.add_argument("--stage", type=int, default=-1,
                     help="mixed record access: 0 L1/L2, 1 staged in shared memory, -1 default")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--stream-n", type=int, default=STREAM_N,
+                    help="queries per kind of the stream workload (smaller for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="sdf",
                     choices=["sdf", "batch", "scale", "stream", "stl", "detect", "simplify",
