@@ -194,6 +194,21 @@ def traffic_from_profile():
     return None
 
 
+def stream_traffic_per_query():
+    """DRAM bytes per query of the FP32 stream passes (orient3d, insphere) from the
+    committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_pred_fp32_tma_stream2e7.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_query:"):
+                    w = line.split(":", 1)[1].split()
+                    return float(w[w.index("orient3d") + 1]), float(w[w.index("insphere") + 1])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
 def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None, probe=2000):
     """The oracle (CPU restatement of the reference algorithm) on this host: full
     occupancy plus the ring-search SDF on a uniform sample of cells, scaled to
@@ -716,7 +731,11 @@ def run_stream(args):
         line["roofline"] = {"bound": "hbm", "kernel": "k_pred_fp32_tma<orient3d> + <insphere> "
                                                       "(certification passes, TMA-staged)",
                             "achieved": byts / t_fp32 / 1e9, "peak": hbm, "unit": "GB/s",
-                            "frac": byts / t_fp32 / 1e9 / hbm, "traffic": None,
+                            "frac": byts / t_fp32 / 1e9 / hbm,
+                            "traffic": (lambda q: q and n * (q[0] + q[1]))(stream_traffic_per_query()),
+                            "traffic_basis": "DRAM bytes of both FP32 launches of a step: the ncu "
+                                             "bytes per query of a 2e7-query capture (the "
+                                             "traffic grows with the queries) times the queries",
                             "kernel_ms": t_fp32 * 1e3,
                             "step_achieved": byts / t_step / 1e9,
                             "work": "97 B per orient3d + 121 B per insphere query (coordinates read "
