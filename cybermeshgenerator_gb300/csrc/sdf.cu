@@ -389,7 +389,7 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
     const int rmax = max(s.bnx, max(s.bny, s.bnz));
     // reductions over the brick's warps (each of its threads calls them, at points
     // uniform over the brick)
-    auto cta_min = [&](float v) {
+    auto brick_min = [&](float v) {
         v = warp_min(v);
         if (W == 1) return v;
         if (lane == 0) s_f[wid] = v;
@@ -400,7 +400,7 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         brick_sync();
         return m;
     };
-    auto cta_any = [&](bool v) {
+    auto brick_any = [&](bool v) {
         const bool wv = __any_sync(0xffffffffu, v);
         if (W == 1) return wv;
         if (lane == 0) s_i[wid] = wv ? 1 : 0;
@@ -424,7 +424,7 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         for (int64_t e = s.large_begin + 32 * sub + lane; e < s.large_end; e += 32 * W)
             U = fminf(U, large_upper(soup, large_list[e], s.g.corner, q.cx, q.cy, q.cz, tol));
         for (int r = 0; r <= rmax; ++r) {
-            U = cta_min(U);
+            U = brick_min(U);
             if (r > 0 && (r - 1) * bw > U) break;  // farther bins cannot lower U
             const int n = shell_count(r);
             int g0, g1;
@@ -447,12 +447,12 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
                     }
                 });
             }
-            if (r > 0 && !cta_any(inside)) {
-                U = cta_min(U);
+            if (r > 0 && !brick_any(inside)) {
+                U = brick_min(U);
                 break;
             }
         }
-        U = cta_min(U);
+        U = brick_min(U);
         if (sub == 0 && lane == 0) bound[gb] = U;
     } else {
         U = bound[gb];
@@ -565,7 +565,7 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         } else if (!FILL) {
             mine += c;
         }
-        if (r > 0 && !cta_any(any_inside)) break;
+        if (r > 0 && !brick_any(any_inside)) break;
     }
     if (!FILL) {
         if (lane == 0) s_c[wid] = mine;
@@ -578,7 +578,7 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
             atomicAdd(&st->candidates, static_cast<unsigned long long>(total));
         }
     } else {
-        bemax = -cta_min(-bemax);
+        bemax = -brick_min(-bemax);
         if (sub == 0 && lane == 0) brick_emax[gb] = bemax;
     }
 }
