@@ -140,6 +140,7 @@ cmg::gpu::HostVec<int> fan(const cmg_plc& p) {
         all3 = all3 && n == 3;
     }
     cmg::gpu::HostVec<int> t(total);
+    if (total == 0) return t;
     if (all3 && total == p.fidx.size()) {  // every facet a triangle: as stored
         std::memcpy(t.data(), p.fidx.data(), sizeof(int) * total);
         return t;
