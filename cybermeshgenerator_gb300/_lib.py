@@ -66,7 +66,7 @@ class WorkModel(ctypes.Structure):
 class PredStats(ctypes.Structure):
     _fields_ = [("queries", ctypes.c_int64), ("fp64_queries", ctypes.c_int64),
                 ("exact_queries", ctypes.c_int64), ("expansion_queries", ctypes.c_int64),
-                ("fp32_pass_ms", ctypes.c_float)]
+                ("fp32_pass_ms", ctypes.c_float), ("tma_reruns", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: (float if k.endswith("_ms") else int)(getattr(self, k)) for k, _ in self._fields_}

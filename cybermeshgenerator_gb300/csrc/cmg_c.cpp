@@ -22,6 +22,7 @@
 #include <fstream>
 #include <memory>
 #include <mutex>
+#include <stdexcept>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -114,18 +115,18 @@ std::mutex& gpu_mutex() {
     return m;
 }
 
+// The library's own stream on the current device, created on first use and kept
+// for the life of the process (one per device ordinal).
 cudaStream_t gpu_stream() {
+    constexpr int kMaxDevices = 64;
     static std::mutex mu;
-    static int dev_of_stream = -1;
-    static cudaStream_t st = nullptr;
+    static cudaStream_t streams[kMaxDevices] = {};
     int dev = 0;
     CMG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("device ordinal out of range");
     std::lock_guard<std::mutex> g(mu);
-    if (!st || dev != dev_of_stream) {
-        CMG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        dev_of_stream = dev;
-    }
-    return st;
+    if (!streams[dev]) CMG_CUDA(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+    return streams[dev];
 }
 
 // Fan triangulation (v0, v[i-1], v[i]) of every facet polygon

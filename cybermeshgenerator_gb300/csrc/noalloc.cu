@@ -12,9 +12,11 @@
 //
 // Set-up: the first call on a device resolves the array's device address with
 // cudaGetSymbolAddress, with that device current; make that first call before any
-// stream capture. Calls share the array and it keeps the last call's contents, so
-// each call clears what must start at zero; calls that overlap on the GPU (two
-// streams, or two host threads) race on it and must be serialised by the caller.
+// stream capture. Every call reads two sizes back from the device and waits for
+// `stream` to finish before it returns (it synchronises the stream). Calls share the
+// array and it keeps the last call's contents, so each call clears what must start at
+// zero; calls that overlap on the GPU (two streams, or two host threads) race on it
+// and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,7 +102,10 @@ extern "C" cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t n
                                                unsigned char* d_occupancy, void* stream,
                                                char* errbuf, size_t errbuf_len) {
     using namespace cmg::gpu;
-    if (!d_points || !d_triangles || !corner || !dims || !d_occupancy) return CMG_ERR_INVALID_INPUT;
+    if (!d_points || !d_triangles || !corner || !dims || !d_occupancy) {
+        set_err(errbuf, errbuf_len, "cmg_gpu_occupancy_static: null pointer argument");
+        return CMG_ERR_INVALID_INPUT;
+    }
     if (npoints < 1 || ntriangles < 1) {
         set_err(errbuf, errbuf_len, "cmg_gpu_occupancy_static: no points or no triangles");
         return CMG_ERR_INVALID_INPUT;

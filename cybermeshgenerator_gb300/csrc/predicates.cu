@@ -27,6 +27,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -259,7 +260,10 @@ __global__ void k_put_bytes(const int8_t* __restrict__ src, int8_t* __restrict__
 // mbarrier), kStages tiles in flight, one thread per query computing from shared
 // memory, and one atomic per tile for the undecided list. Every wait is bounded: a
 // wait that runs out (it never should) stops the CTA after draining its copies, and
-// sets `fault`, on which the host reruns the pass with the per-thread loads.
+// sets `fault`, on which the host reruns the pass with the per-thread loads. When the
+// drain's own bounded waits run out as well, the CTA sets `drain_fault` too: copies
+// may still have been writing its shared memory, and the host reports an error
+// instead of rerunning.
 constexpr int kTile = 256;  // queries per tile: one per thread
 template <int NPT>
 struct Tma {
@@ -309,7 +313,8 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
                                                             int8_t* __restrict__ out,
                                                             int64_t* __restrict__ list,
                                                             unsigned long long* __restrict__ count,
-                                                            unsigned long long* __restrict__ fault) {
+                                                            unsigned long long* __restrict__ fault,
+                                                            unsigned long long* __restrict__ drain_fault) {
     using T = Tma<NPT>;
     constexpr int C = T::kCols, S = T::kStages;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -342,8 +347,10 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
             // drain this CTA's copies still in flight (bounded), then stop
             if (tid == 0) {
                 atomicExch(fault, 1ull);
+                bool drained = true;
                 for (int64_t j = k; j < K && j < k + S; ++j)
-                    mbar_wait(&bar[j % S], static_cast<unsigned>((j / S) & 1));
+                    drained = mbar_wait(&bar[j % S], static_cast<unsigned>((j / S) & 1)) && drained;
+                if (!drained) atomicExch(drain_fault, 1ull);
             }
             return;
         }
@@ -515,6 +522,7 @@ struct Counters {
     unsigned long long overflow;
     unsigned long long certified;  // decided in the FP64 pass by an exact evaluation
     unsigned long long fault;      // a TMA wait of the FP32 pass ran out
+    unsigned long long drain_fault;  // ... and so did the drain of the copies in flight
 };
 
 // Queries per chunk of a host-resident stream (two buffer sets of up to 15 columns:
@@ -547,8 +555,10 @@ static void pred_stream_finish(int npt, const Soa& s, int mode, int8_t* d_out, i
     CMG_LAUNCH();
 }
 
-// Runs the three passes on device-resident SoA coordinates.
-void pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
+// Runs the three passes on device-resident SoA coordinates. Returns the number of
+// times the FP32 pass was rerun with per-thread loads after a TMA wait ran out (0 or
+// 1); throws when copies may have outlived their CTA.
+int pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
                         int64_t* list_a, int64_t* list_b, void* counters, cudaStream_t st,
                         int sms, cudaEvent_t* fp32_events) {
     Soa s{};
@@ -568,12 +578,14 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<4>::kSmem)));
             k_pred_fp32_tma<4><<<2 * sms, kThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, list_a,
-                                                                         &c->n32, &c->fault);
+                                                                         &c->n32, &c->fault,
+                                                                         &c->drain_fault);
         } else {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<5>::kSmem)));
             k_pred_fp32_tma<5><<<2 * sms, kThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, list_a,
-                                                                         &c->n32, &c->fault);
+                                                                         &c->n32, &c->fault,
+                                                                         &c->drain_fault);
         }
         CMG_LAUNCH();
     }
@@ -583,19 +595,26 @@ void pred_stream_device(int npt, const double* const* coords, int64_t n, int mod
         CMG_LAUNCH();
     }
     if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[1], st));
+    int reruns = 0;
     if (ntiles > 0) {
-        // a TMA wait that ran out (it never should) reruns the pass with per-thread loads
-        unsigned long long fault = 0;
-        CMG_CUDA(cudaMemcpyAsync(&fault, &c->fault, sizeof(fault), cudaMemcpyDeviceToHost, st));
+        // a TMA wait that ran out (it never should) reruns the pass with per-thread loads,
+        // unless the copies in flight could not be drained either
+        unsigned long long fault[2] = {0, 0};
+        CMG_CUDA(cudaMemcpyAsync(fault, &c->fault, sizeof(fault), cudaMemcpyDeviceToHost, st));
         CMG_CUDA(cudaStreamSynchronize(st));
-        if (fault) {
+        if (fault[1])
+            throw std::runtime_error(
+                "predicate stream: a bulk copy of the FP32 pass did not complete within its wait");
+        if (fault[0]) {
             CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
             if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
             else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
             CMG_LAUNCH();
+            reruns = 1;
         }
     }
     pred_stream_finish(npt, s, mode, d_out, list_a, list_b, c, st, sms);
+    return reruns;
 }
 
 }  // namespace cmg::gpu
@@ -661,6 +680,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             for (cudaEvent_t& e : w.ev) CMG_CUDA(cudaEventCreate(&e));
         const int ncol = 3 * npt;
         Counters hc{};
+        int reruns = 0;
         if (!host) {
             const double* dc[15];
             int8_t* dout;
@@ -672,7 +692,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
                 w.arena.reserve(w.arena.need());
                 plan(w.arena, dc, &dout, &la, &lb, &cnt);
             }
-            pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout,
+            reruns += pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout,
                                la, lb, cnt, st, sms, w.ev);
             CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
             CMG_CUDA(cudaStreamSynchronize(st));
@@ -799,7 +819,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
                 if (c + 1 < nch) upload(c + 1);
                 const double* dc[15];
                 for (int k = 0; k < ncol; ++k) dc[k] = col[b][k];
-                pred_stream_device(npt, dc, m, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat,
+                reruns += pred_stream_device(npt, dc, m, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat,
                                    sg[b], la, lb, cnt + c, st, sms, &w.chunk_ev[2 * c]);
                 CMG_CUDA(cudaMemcpyAsync(out + i0, sg[b], m, cudaMemcpyDeviceToHost, st));
                 CMG_CUDA(cudaEventRecord(w.done[b], st));
@@ -824,6 +844,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             stats->fp64_queries = static_cast<int64_t>(hc.n32);
             stats->exact_queries = static_cast<int64_t>(hc.n64 + hc.certified);
             stats->expansion_queries = static_cast<int64_t>(hc.n64);
+            stats->tma_reruns = reruns;
         }
         if (hc.overflow) {
             set_err(errbuf, len, "insphere: exact expansion exceeded its capacity");

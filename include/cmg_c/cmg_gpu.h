@@ -273,6 +273,8 @@ typedef struct cmg_pred_stats {
                                   which no operation rounded, or expansions) */
     int64_t expansion_queries; /* of which needed expansion arithmetic */
     float fp32_pass_ms;        /* device time of the FP32 certification pass (CUDA events) */
+    int32_t tma_reruns;        /* FP32 passes rerun with per-thread loads after a bulk-copy
+                                  wait ran out (expected 0) */
 } cmg_pred_stats;
 
 /* Signs (-1, 0, +1) of n orient3d(a,b,c,d) queries given as 12 SoA coordinate
@@ -326,8 +328,9 @@ void cmg_host_free(void* p);
  * are rejected with CMG_ERR_INVALID_INPUT and a message. The first call on a device
  * resolves the array's address (make it before any stream capture); calls share
  * the array, so calls that overlap on the GPU race and must be serialised.
- * `stream` is a cudaStream_t (NULL for the default stream); the call returns
- * after the work on it has finished. predicates: CMG_PRED_COMPAT or
+ * `stream` is a cudaStream_t (NULL for the default stream); the call reads two
+ * sizes back from the device and synchronises `stream`, so it returns after the
+ * work on it has finished. predicates: CMG_PRED_COMPAT or
  * CMG_PRED_EXACT. The result equals cmg_plc_voxelize_ex's occupancy. */
 cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t npoints,
                                     const int* d_triangles, int64_t ntriangles,

@@ -63,7 +63,10 @@ def build(ref: bool = False) -> None:
         if r.returncode != 0:
             raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
     if ref:
-        r = subprocess.run(["make", "-C", _HERE, "ref"], capture_output=True, text=True)
+        root = os.environ.get("CMG_REFERENCE_ROOT")
+        if not root:
+            raise RuntimeError("the reference harness needs CMG_REFERENCE_ROOT (the reference source tree)")
+        r = subprocess.run(["make", "-C", _HERE, "ref", "REF_ROOT=" + root], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("reference harness build failed:\n" + r.stdout + r.stderr)
 

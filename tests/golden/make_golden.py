@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference's own code.
 
-Run where the reference sources are available (it builds oracle/_ref from them):
+Run where the reference sources are available (it builds oracle/_ref from them;
+CMG_REFERENCE_ROOT names the reference source tree):
 
-    python tests/golden/make_golden.py [case ...]   # all cases, or only those named
+    CMG_REFERENCE_ROOT=<tree> python tests/golden/make_golden.py [case ...]
 
 Every fixture stores its input mesh as raw float64/int32 bits (so hosts whose
 libm differs still see identical inputs) and the reference's outputs:
