@@ -56,9 +56,28 @@ PZ_FLOPS = 22      # flops of one plane_z
 L2_FLUSH_BYTES = 256 << 20
 
 
+PINNED_MESH = os.path.join(ROOT, "tests", "golden", "shsphere256.npz")
+
+
 def workload():
+    """The headline mesh as serialised float64 bits (the input the full-size parity
+    tests check against the reference's outputs), else regenerated."""
+    if os.path.exists(PINNED_MESH):
+        with np.load(PINNED_MESH) as z:
+            return np.array(z["points"]), np.array(z["triangles"])
     from cybermeshgenerator_gb300 import workloads as W
     return W.sh_sphere(nlon=256, nlat=128, seed=3)
+
+
+def kernel_source_sha(files=("sdf_sub.cu", "cmg_sdf.cuh")):
+    """SHA-256 (16 hex digits) of the evaluation kernel's sources, recorded in its ncu
+    summary so that the bench line takes DRAM traffic only from a capture of this code."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(ROOT, "cybermeshgenerator_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def workload_desc(dims, ntris):
@@ -181,17 +200,26 @@ def fraction_of_peak(work_flops, ms, peak):
     return achieved, achieved / peak
 
 
+TRAFFIC_PROFILE = os.path.join("profiles", "k_sdf_sub_mixed_shsphere256.md")
+
+
 def traffic_from_profile():
-    """DRAM bytes per launch of the evaluation kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_sdf_sub_mixed_shsphere256.md")
+    """DRAM bytes per launch of the evaluation kernel from the committed ncu summary,
+    when that capture was of the current kernel source: (bytes or None, note)."""
+    path = os.path.join(ROOT, TRAFFIC_PROFILE)
+    vals = {}
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_launch:"):
-                    return float(line.split(":", 1)[1].split()[0])
+                for key in ("dram_bytes_per_launch:", "kernel_source_sha:"):
+                    if line.startswith(key):
+                        vals[key] = line.split(":", 1)[1].split()[0]
     except OSError:
-        pass
-    return None
+        return None, "no ncu summary"
+    sha = kernel_source_sha()
+    if vals.get("kernel_source_sha:") != sha:
+        return None, f"{TRAFFIC_PROFILE} was captured from other kernel sources (now {sha})"
+    return float(vals["dram_bytes_per_launch:"]), f"{TRAFFIC_PROFILE}, ncu capture of kernel sources {sha}"
 
 
 def stream_traffic_per_query():
@@ -212,7 +240,7 @@ def stream_traffic_per_query():
 def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None, probe=2000):
     """The oracle (CPU restatement of the reference algorithm) on this host: full
     occupancy plus the ring-search SDF on a uniform sample of cells, scaled to
-    the grid."""
+    the grid. threads=None: every host core."""
     import oracle
     orc = oracle.Oracle()
     threads = threads or os.cpu_count() or 1
@@ -234,7 +262,18 @@ def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None, probe=2000):
     t_full = t_occ + t_build + t_q / m * n
     return {"value": n / t_full, "unit": UNIT, "cores": int(threads), "kind": "port",
             "sample": f"occupancy on all {n} cells; ring-search SDF on {m} uniformly sampled cells "
-                      f"+ the 3-D bucket build, scaled to {n} cells (extrapolated)"}
+                      f"({100.0 * m / n:.3g} % of the grid) + the 3-D bucket build, scaled to {n} "
+                      f"cells (extrapolated)",
+            "sample_fraction": m / n, "seconds": time.perf_counter() - t0}
+
+
+def cpu_baselines(pts, tris, dims_grid, seconds):
+    """The single-threaded figure (the reference voxelizer runs on one thread), with
+    the all-cores figure of the same port beside it."""
+    one = cpu_baseline(pts, tris, dims_grid, seconds=seconds, threads=1, probe=300)
+    allc = cpu_baseline(pts, tris, dims_grid, seconds=seconds)
+    one["all_cores"] = {k: allc[k] for k in ("value", "cores", "sample", "sample_fraction")}
+    return one
 
 
 def run_ours(args):
@@ -272,6 +311,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
             "config": dict(workload_desc(dims, len(tris)), parallelism=f"replicas x{world}"),
             "gpu_launches": int(launches)}
+    line["config"]["mesh"] = "serialised float64 bits (tests/golden/shsphere256.npz)" \
+        if os.path.exists(PINNED_MESH) else "regenerated"
     clocks = clk.summary()
     line["clocks"] = clocks
 
@@ -300,10 +341,11 @@ def run_ours(args):
         w_sdf = wm["sum_k"] * PT_FLOPS
         ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
         ach64, frac64 = fraction_of_peak(w_sdf, tp["eval_ms"], p64)
+        traffic, traffic_note = traffic_from_profile()
         line["roofline"] = {
             "bound": "fp32", "kernel": "k_sdf_sub<mixed> (distance evaluation)",
             "achieved": ach / 1e12, "peak": p32 / 1e12, "unit": "TFLOP/s", "frac": frac,
-            "traffic": traffic_from_profile(),
+            "traffic": traffic, "traffic_source": traffic_note,
             "work": f"sum_v K(v) * {PT_FLOPS} = {w_sdf:.4g} flops per launch; K(v) = triangles whose "
                     f"bounding sphere reaches the cell's distance sphere",
             "peak_source": "measured FFMA microbenchmark on this GPU (no FP32 entry in MEASURED_PEAKS.json)",
@@ -334,8 +376,8 @@ def run_ours(args):
                        "d2h_bytes_per_step": int(cells * (1 + 4)),
                        "call": "cmg_plc_voxelize_ex (mixed, occupancy + float SDF), host buffers"}
         if not args.no_cpu:
-            line["cpu_baseline"] = cpu_baseline(pts, tris, (r0.corner, r0.spacing, r0.dims),
-                                                seconds=args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baselines(pts, tris, (r0.corner, r0.spacing, r0.dims),
+                                                 seconds=args.cpu_seconds)
         print(json.dumps(line), flush=True)
     barrier(world)
     if world > 1:
@@ -368,7 +410,9 @@ def run_reference(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": g.ncell / value * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-            "config": dict(workload_desc(g.dims, len(tris)), parallelism="cpu threads"),
+            "config": dict(workload_desc(g.dims, len(tris)), parallelism=f"replicas x{world}",
+                           mesh="serialised float64 bits (tests/golden/shsphere256.npz)"
+                           if os.path.exists(PINNED_MESH) else "regenerated"),
             "cpu_baseline": base,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -26,7 +26,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["scan.cu", "occupancy.cu", "sdf.cu", "sdf_sub.cu", "engine.cu", "peak.cu", "noalloc.cu", "predicates.cu", "adjoint.cu", "stl.cu", "detect.cu", "simplify.cu", "sizing.cu"]
 # per-file flags: sizing.cu rounds every product and sum separately, as the reference does
 CU_FLAGS = {"sizing.cu": ["-fmad=false"]}
-CXX_SOURCES = ["cmg_c.cpp"]
+CXX_SOURCES = ["cmg_c.cpp", "cmg_cpp.cpp"]
+# per-file language standard: the C++ surface (cmg::voxelize::voxelize) is built as
+# C++20, as the reference is, so cmg::expected has the same layout on both sides
+CXX_STD = {"cmg_cpp.cpp": "-std=c++20"}
 
 
 def _nvcc() -> str:
@@ -59,8 +62,9 @@ def build(jobs: int | None = None, verbose: bool = False) -> str:
     nvcc = _nvcc()
     inc = os.path.join(_cuda_home(nvcc), "include")
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers += [os.path.join(ROOT, "include", "cmg_c", f)
-                for f in os.listdir(os.path.join(ROOT, "include", "cmg_c"))]
+    for sub in ("cmg_c", os.path.join("cmg", "core"), os.path.join("cmg", "voxelize")):
+        d = os.path.join(ROOT, "include", sub)
+        headers += [os.path.join(d, f) for f in os.listdir(d)]
     steps, objs = [], []
     for src in CU_SOURCES:
         s, o = os.path.join(CSRC, src), os.path.join(BUILD, src + ".o")
@@ -72,8 +76,9 @@ def build(jobs: int | None = None, verbose: bool = False) -> str:
         s, o = os.path.join(CSRC, src), os.path.join(BUILD, src + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
-            steps.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
-                          "-fvisibility=default", "-I" + inc, "-c", s, "-o", o])
+            steps.append(["g++", "-O2", CXX_STD.get(src, "-std=c++17"), "-fPIC", "-ffp-contract=off",
+                          "-fvisibility=default", "-I" + inc, "-I" + os.path.join(ROOT, "include"),
+                          "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         for log in ex.map(_run, steps):
             if verbose and log.strip():

@@ -159,9 +159,9 @@ cmg::gpu::HostVec<int> fan(const cmg_plc& p) {
     return t;
 }
 
-// make_grid (src/voxelize/voxelize.cpp:52-74), same operations in the same order.
-bool make_grid(const cmg::gpu::HostVec<double>& pts, int resolution, int pad, GridDesc& g) {
-    const size_t n = pts.size() / 3;
+// make_grid (src/voxelize/voxelize.cpp:52-74), same operations in the same order;
+// pts holds n points of 3 coordinates (n >= 1).
+bool make_grid(const double* pts, size_t n, int resolution, int pad, GridDesc& g) {
     double lo[3] = {pts[0], pts[1], pts[2]}, hi[3] = {pts[0], pts[1], pts[2]};
     for (size_t i = 0; i < n; ++i)
         for (int a = 0; a < 3; ++a) {
@@ -193,15 +193,19 @@ struct CoreError {
 // Validation of voxelize (src/voxelize/voxelize.cpp:362-379) plus index checks
 // (an out-of-range facet index is undefined behaviour in the reference; here it
 // is an InvalidInput error, since the GPU must never read outside its inputs).
+void check_mesh(int64_t npts, const int* tris, int64_t ntris) {
+    if (npts == 0) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no points"};
+    if (ntris == 0)
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no boundary triangles"};
+    for (int64_t i = 0; i < 3 * ntris; ++i)
+        if (tris[i] < 0 || tris[i] >= npts)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: facet vertex index out of range"};
+}
+
 cmg::gpu::HostVec<int> checked_triangles(const cmg_plc& p) {
     if (p.points.empty()) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no points"};
     cmg::gpu::HostVec<int> t = fan(p);
-    if (t.empty())
-        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no boundary triangles"};
-    const int64_t np = static_cast<int64_t>(p.points.size() / 3);
-    for (int v : t)
-        if (v < 0 || v >= np)
-            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: facet vertex index out of range"};
+    check_mesh(static_cast<int64_t>(p.points.size() / 3), t.data(), static_cast<int64_t>(t.size() / 3));
     return t;
 }
 
@@ -263,10 +267,10 @@ void set_geometry(cmg_voxels* v, const GridDesc& g) {
     v->nz = g.nz;
 }
 
-cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
-    if (!o.explicit_grid && o.resolution < 1)
-        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
-    cmg::gpu::HostVec<int> tris = checked_triangles(p);
+// One voxelization of host arrays: pts (npts points of 3 coordinates), tris (ntris
+// triangles of 3 indices, already fanned and checked).
+cmg_voxels* voxelize_arrays(const double* pts, int64_t npts, const int* tris, int64_t ntris,
+                            const cmg_voxel_opts& o) {
     GridDesc g{};
     if (o.explicit_grid) {
         for (int a = 0; a < 3; ++a) g.corner[a] = o.corner[a];
@@ -275,17 +279,17 @@ cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
         g.ny = o.dims[1];
         g.nz = o.dims[2];
         if (!(g.h > 0)) throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: spacing must be > 0"};
-    } else if (!make_grid(p.points, o.resolution, o.pad, g)) {
+    } else if (!make_grid(pts, static_cast<size_t>(npts), o.resolution, o.pad, g)) {
         throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
     }
     check_grid_size(g);
     const int outputs = effective_outputs(o);
     cmg::gpu::VoxOpts vo = to_vox(o, outputs);
     cmg::gpu::HostMesh m;
-    m.pts = p.points.data();
-    m.npts = static_cast<int64_t>(p.points.size() / 3);
-    m.tris = tris.data();
-    m.ntris = static_cast<int64_t>(tris.size() / 3);
+    m.pts = pts;
+    m.npts = npts;
+    m.tris = tris;
+    m.ntris = ntris;
     m.g = g;
     std::lock_guard<std::mutex> lk(gpu_mutex());
     cudaStream_t st = gpu_stream();
@@ -300,6 +304,14 @@ cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
     v->r = std::move(res[0]);
     fill_stats(v.get(), ri);
     return v.release();
+}
+
+cmg_voxels* voxelize_one(const cmg_plc& p, const cmg_voxel_opts& o) {
+    if (!o.explicit_grid && o.resolution < 1)
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
+    cmg::gpu::HostVec<int> tris = checked_triangles(p);
+    return voxelize_arrays(p.points.data(), static_cast<int64_t>(p.points.size() / 3), tris.data(),
+                           static_cast<int64_t>(tris.size() / 3), o);
 }
 
 template <typename F>
@@ -325,6 +337,33 @@ cmg_status guarded(char* errbuf, size_t len, F&& f) {
 const char* kNotHere = "not part of the GB300 voxelization library (meshing and file I/O stay in the reference)";
 
 }  // namespace
+
+namespace cmg::gpu {
+
+// The core of cmg_plc_voxelize on host arrays, for the C++ surface (cmg_cpp.cpp):
+// validation in the reference's order and with its messages, then the GPU pipeline.
+// pts: npts points of 3 coordinates; tris: ntris fanned triangles. Returns the
+// status; on success *out holds the grid, otherwise *msg the error text.
+cmg_status voxelize_host(const double* pts, int64_t npts, const int* tris, int64_t ntris,
+                         int resolution, int pad, int mode, cmg_voxels** out, std::string* msg) {
+    *out = nullptr;
+    char buf[512] = {0};
+    const cmg_status st = guarded(buf, sizeof(buf), [&] {
+        if (resolution < 1)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
+        check_mesh(npts, tris, ntris);
+        cmg_voxel_opts o;
+        cmg_voxel_opts_init(&o);
+        o.resolution = resolution;
+        o.pad = pad;
+        o.mode = mode == 1 ? 1 : 0;
+        *out = voxelize_arrays(pts, npts, tris, ntris, o);
+    });
+    if (st != CMG_OK) *msg = buf;
+    return st;
+}
+
+}  // namespace cmg::gpu
 
 namespace {
 // Blocks handed out by cmg_host_alloc: capacity and whether page-locked.
@@ -531,7 +570,7 @@ cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, 
             } else {
                 if (resolutions[i] < 1)
                     throw CoreError{CMG_ERR_INVALID_INPUT, "resolution must be >= 1"};
-                if (!make_grid(p.points, resolutions[i], pads[i], g))
+                if (!make_grid(p.points.data(), p.points.size() / 3, resolutions[i], pads[i], g))
                     throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
             }
             check_grid_size(g);

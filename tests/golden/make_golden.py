@@ -74,6 +74,40 @@ def grid_case(ref, name, pts, tris, corner, spacing, dims, nsample=512, seed=0):
     return occ
 
 
+def full_case(ref, name, pts, tris, grids, nsample=2048, seed=0):
+    """A full-size configuration: the mesh as raw bits and, per grid, the reference's
+    occupancy (public voxelize for ("api", resolution, pad), classify_occupancy for
+    ("grid", corner, spacing, dims)) as a SHA-256 and bit-packed, plus FP64 squared
+    distances (brute-force point_tri_dist2) at sampled cells."""
+    out = dict(points=pts, triangles=tris.astype(np.int32), grids=np.array([g[0] for g in grids]))
+    facets = [list(t) for t in tris]
+    for gname, g in grids:
+        if g[0] == "api":
+            _, resolution, pad = g
+            st, origin, sp, dims, occ = ref.voxelize(pts, facets, resolution, pad, 0)
+            assert st == 0, (name, gname, st)
+            rc, corner, sp2, dims2 = ref.make_grid(pts, resolution, pad)
+            assert dims2 == dims and sp2 == sp
+            out[gname + "_resolution"] = np.int32(resolution)
+            out[gname + "_pad"] = np.int32(pad)
+        else:
+            _, corner, sp, dims = g
+            occ = ref.occupancy_grid(pts, tris, corner, sp, dims)
+        n = int(np.prod(dims))
+        rng = np.random.default_rng(seed)
+        vox = np.sort(rng.choice(n, size=min(nsample, n), replace=False)).astype(np.int64)
+        out[gname + "_dims"] = np.array(dims, np.int32)
+        out[gname + "_corner"] = np.asarray(corner, np.float64)
+        out[gname + "_spacing"] = np.float64(sp)
+        out[gname + "_occ_sha"] = np.array(sha(occ))
+        out[gname + "_occ_bits"] = np.packbits(occ)
+        out[gname + "_sample_vox"] = vox
+        out[gname + "_sample_d2"] = ref.dist2_brute(pts, tris, corner, sp, dims, vox)
+    out["grid_names"] = np.array([g for g, _ in grids])
+    del out["grids"]
+    save(name, **out)
+
+
 def pred_case(ref, name, n, seed):
     out = {}
     for kind, npt in (("orient3d", 4), ("insphere", 5)):
@@ -372,6 +406,19 @@ def main():
         api_case(ref, "cube4_r16p1", pts, tris, 16, 1)
     manifest["cube4_r16p1"] = "reference test fixture subdivided_cube(4); resolution 16, pad 1 (exact 16^3 block)"
 
+    # the same cube with a zero-area facet (three collinear dyadic points at z = 0.5)
+    # inserted halfway through its triangle list: every column whose bucket holds it
+    # grazes on all six nudges, and the reference keeps the last attempt's crossings
+    # of the triangles before it (voxelize.cpp:158-165), which changes 720 cells
+    k = len(pts)
+    pts_d = np.vstack([pts, [[0.25, 0.25, 0.5], [0.5, 0.5, 0.5], [0.75, 0.75, 0.5]]])
+    tris_d = np.insert(tris, len(tris) // 2, [k, k + 1, k + 2], axis=0)
+    if want("cube4deg_r16p1"):
+        api_case(ref, "cube4deg_r16p1", pts_d, tris_d, 16, 1)
+    manifest["cube4deg_r16p1"] = ("subdivided_cube(4) with a zero-area facet (0.25,0.25,0.5)-(0.5,0.5,0.5)-"
+                                  "(0.75,0.75,0.5) inserted at triangle 96; resolution 16, pad 1 "
+                                  "(81 columns exhaust every nudge)")
+
     pts, tris = W.uv_sphere(1.0, 16, 16)
     if want("uvsphere16_r20p1"):
         api_case(ref, "uvsphere16_r20p1", pts, tris, 20, 1)
@@ -401,6 +448,24 @@ def main():
     if want("cube3_facegrid"):
         grid_case(ref, "cube3_facegrid", pts, tris, [-4.5 / 12, -4.5 / 12, -4.5 / 12], 1.0 / 12, (20, 20, 20))
     manifest["cube3_facegrid"] = "subdivided_cube(3) on a 20^3 grid, h=1/12, centres on faces and shared edges"
+
+    # full-size configurations: the headline SH surface (65,024 triangles) at 128 and
+    # 256 cells on its long axis, and the 262,156-triangle box + torus on the exact-face
+    # 256^3 grid and through the API
+    pts, tris = W.sh_sphere(nlon=256, nlat=128, seed=3)
+    if want("shsphere256"):
+        full_case(ref, "shsphere256", pts, tris,
+                  [("r126p1", ("api", 126, 1)), ("r254p1", ("api", 254, 1))])
+    manifest["shsphere256"] = ("SH star surface on a 256x128-band UV sphere (seed 3, 65,024 triangles); "
+                               "resolution 126 pad 1 (128^3) and resolution 254 pad 1 (231x247x256)")
+    pts, tris = W.box_and_torus(512, 256)
+    h = 2.0 ** -7
+    if want("boxtorus512"):
+        full_case(ref, "boxtorus512", pts, tris,
+                  [("facegrid", ("grid", [-64.5 * h, -64.5 * h, -43.5 * h], h, (256, 256, 256))),
+                   ("r254p1", ("api", 254, 1))])
+    manifest["boxtorus512"] = ("unit box + torus(R .35, r .12, 512x256 quads; 262,156 triangles) on the "
+                               "exact-face 256^3 grid (h=2^-7) and through the API at resolution 254, pad 1")
 
     if want("predicates"):
         pred_case(ref, "predicates", 4096, seed=21)

@@ -12,8 +12,8 @@ from conftest import unpack_occ
 
 pytestmark = pytest.mark.gpu
 
-API_CASES = ["icosphere_s3_r58p3", "cube4_r16p1", "uvsphere16_r20p1", "brick312_r20p1",
-             "shsphere64_r30p1", "boxtorus64_r62p1"]
+API_CASES = ["icosphere_s3_r58p3", "cube4_r16p1", "cube4deg_r16p1", "uvsphere16_r20p1",
+             "brick312_r20p1", "shsphere64_r30p1", "boxtorus64_r62p1"]
 GRID_CASES = ["boxtorus64_facegrid", "cube3_facegrid"]
 ALL = API_CASES + GRID_CASES
 
@@ -64,6 +64,21 @@ def test_nudge_statistics_match_oracle(cm, golden, orc):
     _, st = orc.occupancy(g["points"], g["triangles"], grid)
     assert r.stats["nudged_columns"] == st["nudged_columns"] > 0
     assert r.stats["exhausted_columns"] == st["exhausted_columns"]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_exhausted_nudges_keep_last_partial(cm, golden, orc, mode):
+    """A zero-area facet halfway through the triangle list: 81 columns graze on all six
+    nudges and keep the crossings of the triangles before it (voxelize.cpp:158-165)."""
+    g = golden("cube4deg_r16p1")
+    r = _run(cm, g, "cube4deg_r16p1", outputs=cm.OUT_OCCUPANCY | cm.OUT_SDF_F32, predicates=mode)
+    grid = orc.grid(r.corner, r.spacing, r.dims)
+    occ, st = orc.occupancy(g["points"], g["triangles"], grid, mode)
+    assert r.stats["exhausted_columns"] == st["exhausted_columns"] == 81
+    assert r.stats["nudged_columns"] == st["nudged_columns"]
+    assert np.array_equal(r.occupancy, occ)
+    assert np.array_equal(r.occupancy, unpack_occ(g))
+    assert _sha(r.sdf32) == str(g["sdf32_sha"])
 
 
 @pytest.mark.parametrize("name", [c for c in API_CASES if c != "boxtorus64_r62p1"])

@@ -7,8 +7,11 @@ import pytest
 
 from conftest import unpack_occ
 
-API_CASES = ["icosphere_s3_r58p3", "cube4_r16p1", "uvsphere16_r20p1", "brick312_r20p1",
-             "shsphere64_r30p1", "boxtorus64_r62p1"]
+API_CASES = ["icosphere_s3_r58p3", "cube4_r16p1", "cube4deg_r16p1", "uvsphere16_r20p1",
+             "brick312_r20p1", "shsphere64_r30p1", "boxtorus64_r62p1"]
+# full-size configurations: (fixture, grid) pairs
+FULL_CASES = [("shsphere256", "r126p1"), ("shsphere256", "r254p1"), ("boxtorus512", "facegrid"),
+              ("boxtorus512", "r254p1")]
 GRID_CASES = ["boxtorus64_facegrid", "cube3_facegrid"]
 
 
@@ -60,8 +63,8 @@ def test_known_answer_cube_block(golden):
     assert np.array_equal(occ, block)
 
 
-@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "cube4_r16p1", "uvsphere16_r20p1",
-                                  "brick312_r20p1", "shsphere64_r30p1"])
+@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "cube4_r16p1", "cube4deg_r16p1",
+                                  "uvsphere16_r20p1", "brick312_r20p1", "shsphere64_r30p1"])
 def test_sdf_float_bits(orc, golden, name):
     g = golden(name)
     grid = orc.make_grid(g["points"], int(g["resolution"]), int(g["pad"]))
@@ -242,3 +245,52 @@ def test_sizing_reference_properties(orc):
     full, _ = orc.sizing(P, T, np.full(len(P), 0.4), 1.0, [[0.5, 0.5, 0.5]])
     half, _ = orc.sizing(P, T, np.full(len(P), 0.4), 0.5, [[0.5, 0.5, 0.5]])
     assert abs(half[0] - 0.5 * full[0]) < 1e-9 and abs(full[0] - 0.4) < 1e-6
+
+
+def test_exhausted_nudges_keep_partial_heights(orc, golden):
+    """A zero-area facet makes every nudge of 81 columns graze; the reference keeps the
+    crossings of the triangles before it in bucket order (voxelize.cpp:158-165), which
+    differs from the plain cube's occupancy."""
+    g = golden("cube4deg_r16p1")
+    grid = orc.make_grid(g["points"], int(g["resolution"]), int(g["pad"]))
+    for mode in (0, 1):
+        occ, st = orc.occupancy(g["points"], g["triangles"], grid, mode)
+        assert st["exhausted_columns"] == 81 and st["nudged_columns"] == 131
+        assert np.array_equal(occ, unpack_occ(g))
+    plain = golden("cube4_r16p1")
+    assert int((unpack_occ(plain) != unpack_occ(g)).sum()) == 720
+
+
+def _full(golden, name, gname):
+    z = golden(name)
+    return z, {k[len(gname) + 1:]: v for k, v in z.items() if k.startswith(gname + "_")}
+
+
+@pytest.mark.parametrize("name,gname", FULL_CASES)
+def test_full_size_occupancy(orc, golden, name, gname):
+    z, g = _full(golden, name, gname)
+    if "resolution" in g:
+        grid = orc.make_grid(z["points"], int(g["resolution"]), int(g["pad"]))
+        assert grid.dims == tuple(int(d) for d in g["dims"])
+        assert np.array_equal(np.array(grid.corner), g["corner"])
+    else:
+        grid = orc.grid(g["corner"], g["spacing"], g["dims"])
+    occ, st = orc.occupancy(z["points"], z["triangles"], grid)
+    assert _sha(occ) == str(g["occ_sha"])
+    assert np.array_equal(occ, np.unpackbits(g["occ_bits"])[:grid.ncell])
+    if name == "boxtorus512":
+        assert st["nudged_columns"] > 0 and st["exact_calls"] > 0
+    d2, _, _ = orc.sdf_brute(z["points"], z["triangles"], grid, g["sample_vox"])
+    assert np.array_equal(d2.view(np.uint64), g["sample_d2"].view(np.uint64))
+
+
+def test_full_size_meshes_match_generators(golden):
+    """The serialised meshes are the generators' (triangle indices exactly; point
+    coordinates to the last bits, which transcendental functions may round
+    differently on another host)."""
+    from cybermeshgenerator_gb300 import workloads as W
+    for name, (p, t) in (("shsphere256", W.sh_sphere(256, 128, seed=3)),
+                         ("boxtorus512", W.box_and_torus(512, 256))):
+        z = golden(name)
+        assert np.array_equal(z["triangles"], t)
+        assert np.allclose(z["points"], p, rtol=0, atol=1e-13)
