@@ -276,6 +276,19 @@ def cpu_baselines(pts, tris, dims_grid, seconds):
     return one
 
 
+def tunables(args):
+    """Options of the SDF pipeline: the library's autotuner (brick edge, queue grab,
+    walk warps, probe head, evaluation CTAs per SM, timed on this input) unless a
+    brick edge or a tunable is given on the command line or --no-autotune is set."""
+    fixed = {k: v for k, v in (("brick", args.brick), ("walk_warps", args.walk_warps),
+                                ("probe", args.probe), ("ctas", args.ctas)) if v}
+    return dict(fixed, autotune=not fixed and not args.no_autotune)
+
+
+def chosen(stats):
+    return {k: int(stats[k]) for k in ("brick", "grab", "walk_warps", "probe", "ctas")}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup(args.gpus)
@@ -288,8 +301,9 @@ def run_ours(args):
     pts, tris = workload()
     plc = cm.PLC.from_arrays(pts, tris)
     outs = cm.OUT_OCCUPANCY | cm.OUT_SDF_F32
+    tune = tunables(args)
     mixed = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_MIXED, band=1.0,
-                     brick=args.brick, stage=args.stage)
+                     stage=args.stage, **tune)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     mixed.run().sync()  # sizing pass
     cells = mixed.cells
@@ -323,8 +337,8 @@ def run_ours(args):
         tm = mixed.timing()
         wm = mixed.work_model()
         st = mixed.stats()
-        plain = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64,
-                         brick=args.brick)
+        line["config"]["tuning"] = dict(chosen(st), autotuned=bool(tune["autotune"]))
+        plain = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64, **tune)
         plain.run().sync()
         p_ms = time_batch(cm, torch, plain, max(1, min(3, args.steps)), 1, flush)
         plain.set_timing(True)
@@ -352,6 +366,7 @@ def run_ours(args):
             "eval_ms": tm["eval_ms"], "phase_ms": tm,
             "fp64_kernel": {"kernel": "k_sdf_sub<fp64>", "achieved": ach64 / 1e12, "peak": p64 / 1e12,
                             "frac": frac64, "eval_ms": tp["eval_ms"], "phase_ms": tp,
+                            "tuning": chosen(plain.stats()),
                             "peak_source": "measured DFMA microbenchmark (FMA = 2 flops)"}}
         line["mixed_vs_fp64"] = {"fp64_value": p_value, "speedup": value / world / p_value,
                                  "max_abs_err": float(err.max()), "rms_err": float(np.sqrt((err ** 2).mean())),
@@ -367,8 +382,7 @@ def run_ours(args):
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             r = cm.voxelize_ex(plc, resolution=RESOLUTION, pad=PAD, outputs=outs,
-                               precision=cm.PREC_MIXED, band=1.0, brick=args.brick,
-                               stage=args.stage)
+                               precision=cm.PREC_MIXED, band=1.0, stage=args.stage, **tune)
             if i >= args.warmup:
                 e2e_t.append(time.perf_counter() - t0)
         line["e2e"] = {"value": cells / (sum(e2e_t) / len(e2e_t)), "unit": UNIT,
@@ -493,7 +507,7 @@ def run_batch(args):
                           f"segments, scale 0.5-2, random rotation), {ntris} triangles, "
                           f"resolutions 32-192 pad 1, {cells} cells: occupancy + mixed SDF",
               "meshes": len(items), "triangles": int(ntris), "cells": int(cells),
-              "autotuned": {"brick": int(st["brick"]), "grab": int(st["grab"])},
+              "autotuned": chosen(st),
               "replay": "CUDA graph", "l2": "inputs and outputs larger than L2",
               "parallelism": f"replicas x{world}"}
     line = _base_line(BATCH_METRIC, UNIT, value, world, args, total_ms, "fp32+fp64", config,
@@ -503,6 +517,7 @@ def run_batch(args):
         bt.run().sync()
         tm = bt.timing()
         wm = bt.work_model()
+        line["config"]["autotuned"] = chosen(bt.stats())
         p32 = cm.peak_flops(False)
         w_sdf = wm["sum_k"] * PT_FLOPS
         ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
@@ -569,7 +584,7 @@ def run_scale(args):
     pts, tris = _scale_workload()
     g = oracle.Oracle().make_grid(pts, 510, 1)
     grid = TS.grid_of(list(g.corner), g.spacing, (g.nx, g.ny, g.nz))
-    plan = TS.SDFPlan(pts, tris, grid, precision=cm.PREC_MIXED)
+    plan = TS.SDFPlan(pts, tris, grid, precision=cm.PREC_MIXED, autotune=True)
     v = torch.tensor(pts, device="cuda")
     sdf, occ, tri, reg = plan.forward(v)  # sizing
     rng = np.random.default_rng(53)
@@ -614,12 +629,13 @@ def run_scale(args):
         # the dominant kernel of the step is the forward's evaluation: its cost model
         # on a batch over the same grid (phase timing and K(v) counting pass)
         bt = cm.Batch([cm.PLC.from_arrays(pts, tris)], outputs=cm.OUT_OCCUPANCY | cm.OUT_SDF_F32,
-                      precision=cm.PREC_MIXED, grid=grid)
+                      precision=cm.PREC_MIXED, grid=grid, autotune=True)
         bt.run().sync()
         bt.set_timing(True)
         bt.run().sync()
         tm = bt.timing()
         wm = bt.work_model()
+        line["config"]["autotuned"] = chosen(bt.stats())
         p32 = cm.peak_flops(False)
         w_sdf = wm["sum_k"] * PT_FLOPS
         ach, frac = fraction_of_peak(w_sdf, tm["eval_ms"], p32)
@@ -1338,6 +1354,13 @@ def main():
     ap.add_argument("--brick", type=int, default=0)
     ap.add_argument("--stage", type=int, default=-1,
                     help="mixed record access: 0 L1/L2, 1 staged in shared memory, -1 default")
+    ap.add_argument("--walk-warps", type=int, default=0,
+                    help="warps per brick of the candidate walk (1, 2, 4); 0 = autotuned")
+    ap.add_argument("--probe", type=int, default=0, help="mixed probe head; 0 = autotuned")
+    ap.add_argument("--ctas", type=int, default=0,
+                    help="evaluation CTAs per SM (12, 16); 0 = autotuned")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="library defaults for every tunable not given")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--stream-n", type=int, default=STREAM_N,
                     help="queries per kind of the stream workload (smaller for profiler captures)")

@@ -351,13 +351,15 @@ class VoxelResult:
 def make_opts(resolution: int = 64, pad: int = 1, outputs: int = OUT_OCCUPANCY,
               precision: int = PREC_FP64, predicates: int = PRED_COMPAT, grid=None,
               band: float = 1.0, brick: int = 0, autotune: bool = False, grab: int = 0,
-              stage: int = -1) -> _L.VoxelOpts:
+              stage: int = -1, walk_warps: int = 0, probe: int = 0,
+              ctas: int = 0) -> _L.VoxelOpts:
     o = _L.VoxelOpts()
     _clib.cmg_voxel_opts_init(ctypes.byref(o))
     o.resolution, o.pad, o.outputs = int(resolution), int(pad), int(outputs)
     o.precision, o.predicates = int(precision), int(predicates)
     o.band, o.brick, o.autotune = float(band), int(brick), int(bool(autotune))
     o.grab, o.stage = int(grab), int(stage)
+    o.walk_warps, o.probe, o.ctas = int(walk_warps), int(probe), int(ctas)
     if grid is not None:
         corner, spacing, dims = grid
         o.explicit_grid = 1

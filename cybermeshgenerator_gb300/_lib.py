@@ -29,7 +29,8 @@ class VoxelOpts(ctypes.Structure):
                 ("predicates", ctypes.c_int), ("explicit_grid", ctypes.c_int),
                 ("corner", ctypes.c_double * 3), ("spacing", ctypes.c_double),
                 ("dims", ctypes.c_int * 3), ("band", ctypes.c_double), ("brick", ctypes.c_int),
-                ("autotune", ctypes.c_int), ("grab", ctypes.c_int), ("stage", ctypes.c_int)]
+                ("autotune", ctypes.c_int), ("grab", ctypes.c_int), ("stage", ctypes.c_int),
+                ("walk_warps", ctypes.c_int), ("probe", ctypes.c_int), ("ctas", ctypes.c_int)]
 
 
 class VoxelStats(ctypes.Structure):
@@ -40,7 +41,8 @@ class VoxelStats(ctypes.Structure):
                 ("candidates", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("fp64_evaluations", ctypes.c_int64), ("band_cells", ctypes.c_int64),
                 ("filtered", ctypes.c_int64), ("brick", ctypes.c_int), ("grab", ctypes.c_int),
-                ("max_error_bound", ctypes.c_double)]
+                ("max_error_bound", ctypes.c_double), ("walk_warps", ctypes.c_int),
+                ("probe", ctypes.c_int), ("ctas", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

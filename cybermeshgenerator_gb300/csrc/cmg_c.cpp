@@ -228,6 +228,9 @@ cmg::gpu::VoxOpts to_vox(const cmg_voxel_opts& o, int outputs) {
     v.autotune = o.autotune != 0;
     v.grab = o.grab;
     v.stage = o.stage;
+    v.walk_warps = o.walk_warps;
+    v.probe = o.probe;
+    v.ctas = o.ctas;
     return v;
 }
 
@@ -251,6 +254,9 @@ void fill_stats(cmg_voxels* v, const cmg::gpu::RunInfo& ri) {
     s.filtered = static_cast<int64_t>(ri.stats.filtered);
     s.brick = ri.brick;
     s.grab = ri.grab;
+    s.walk_warps = ri.walk_warps;
+    s.probe = ri.probe;
+    s.ctas = ri.ctas;
     double m = 0;
     for (float e : v->r.err) m = std::max(m, static_cast<double>(e));
     s.max_error_bound = m;

@@ -78,8 +78,9 @@ __device__ __forceinline__ void load_soup(const double* __restrict__ soup, int64
 // ------------------------------------------------------------------ FP32 record
 // Translation-invariant FP32 data of a triangle, computed once from FP64: vertex
 // offsets from the centroid, edges (v1-v0, v2-v1, v0-v2), unit normal, in-plane
-// inward edge normals (n x e_k), 1/|e_k|^2 (0 for a degenerate edge), and a flag
-// that allows the plane branch (nonzero area).
+// inward edge normals (n x e_k), 1/|e_k|^2 (0 for a degenerate edge), a flag
+// that allows the plane branch (nonzero area), and a bound on the distance of the
+// FP32 unit normal from the exact one (0 for a degenerate triangle).
 struct alignas(16) TriRec {
     float o0[3], o1[3], o2[3];
     float e0[3], e1[3], e2[3];
@@ -87,7 +88,8 @@ struct alignas(16) TriRec {
     float m0[3], m1[3], m2[3];
     float inv[3];
     float ok;
-    float pad_[2];
+    float nerr;
+    float pad_;
 };
 static_assert(sizeof(TriRec) == 144, "record layout");
 
@@ -99,47 +101,66 @@ __device__ __forceinline__ void load_rec(const TriRec* __restrict__ recs, int t,
 }
 
 // Squared FP32 distance from a point to the triangle, given (dx,dy,dz) = point -
-// centroid; region numbered as the FP64 Ericson regions. When the point does not
-// project inside, its nearest point lies on an edge whose edge function is
-// negative (at most two such edges; their shared vertex belongs to both), so only
-// those segments are measured (all three for a degenerate triangle).
-__device__ __forceinline__ void seg2(float px, float py, float pz, const float* e, float inv,
-                                     float& d, float& t) {
-    t = __saturatef((px * e[0] + py * e[1] + pz * e[2]) * inv);
-    const float qx = px - t * e[0], qy = py - t * e[1], qz = pz - t * e[2];
-    d = qx * qx + qy * qy + qz * qz;
+// centroid; region numbered as the FP64 Ericson regions. A point that projects inside
+// a non-degenerate triangle (every in-plane edge function >= 0) is at its plane
+// distance; otherwise its nearest point lies on the boundary, and the distance is the
+// smallest of the three segment distances (the segment of a satisfied edge is never
+// nearer than the triangle, so the minimum is the boundary distance up to rounding,
+// within the same bound as each segment distance). Every lane measures all three
+// segments: no branch splits a warp whose cells lie in different regions.
+// Explicit intrinsics fix the operation sequence, so the value does not depend on
+// whether the region is wanted (REG) or on the inlining context.
+__device__ __forceinline__ float dot3f(float ax, float ay, float az, const float* b) {
+    return fmaf(ax, b[0], fmaf(ay, b[1], __fmul_rn(az, b[2])));
 }
 
-__device__ __forceinline__ float dist_rec(const TriRec& r, float dx, float dy, float dz, int* reg) {
-    const float pax = dx - r.o0[0], pay = dy - r.o0[1], paz = dz - r.o0[2];
-    const float pbx = dx - r.o1[0], pby = dy - r.o1[1], pbz = dz - r.o1[2];
-    const float pcx = dx - r.o2[0], pcy = dy - r.o2[1], pcz = dz - r.o2[2];
-    const float s0 = r.m0[0] * pax + r.m0[1] * pay + r.m0[2] * paz;
-    const float s1 = r.m1[0] * pbx + r.m1[1] * pby + r.m1[2] * pbz;
-    const float s2 = r.m2[0] * pcx + r.m2[1] * pcy + r.m2[2] * pcz;
-    const bool flat = r.ok > 0.f;
-    if (flat && s0 >= 0.f && s1 >= 0.f && s2 >= 0.f) {
-        const float dp = r.nn[0] * pax + r.nn[1] * pay + r.nn[2] * paz;
-        *reg = 6;
-        return dp * dp;
-    }
-    float d = FLT_MAX, dd, t;
+__device__ __forceinline__ void seg2(float px, float py, float pz, const float* e, float inv,
+                                     float& d, float& t) {
+    t = __saturatef(__fmul_rn(dot3f(px, py, pz, e), inv));
+    const float qx = fmaf(-t, e[0], px), qy = fmaf(-t, e[1], py), qz = fmaf(-t, e[2], pz);
+    d = fmaf(qx, qx, fmaf(qy, qy, __fmul_rn(qz, qz)));
+}
+
+template <bool REG>
+__device__ __forceinline__ float dist_rec_t(const TriRec& r, float dx, float dy, float dz, int* reg) {
+    const float pax = __fsub_rn(dx, r.o0[0]), pay = __fsub_rn(dy, r.o0[1]), paz = __fsub_rn(dz, r.o0[2]);
+    const float pbx = __fsub_rn(dx, r.o1[0]), pby = __fsub_rn(dy, r.o1[1]), pbz = __fsub_rn(dz, r.o1[2]);
+    const float pcx = __fsub_rn(dx, r.o2[0]), pcy = __fsub_rn(dy, r.o2[1]), pcz = __fsub_rn(dz, r.o2[2]);
+    const float s0 = dot3f(pax, pay, paz, r.m0);
+    const float s1 = dot3f(pbx, pby, pbz, r.m1);
+    const float s2 = dot3f(pcx, pcy, pcz, r.m2);
+    const float dp = dot3f(pax, pay, paz, r.nn);
+    float d0, t0, d1, t1, d2, t2;
+    seg2(pax, pay, paz, r.e0, r.inv[0], d0, t0);
+    seg2(pbx, pby, pbz, r.e1, r.inv[1], d1, t1);
+    seg2(pcx, pcy, pcz, r.e2, r.inv[2], d2, t2);
+    const bool face = r.ok > 0.f && s0 >= 0.f && s1 >= 0.f && s2 >= 0.f;
+    float d = d0;
     int g = 0;
-    if (!flat || s0 < 0.f) {
-        seg2(pax, pay, paz, r.e0, r.inv[0], dd, t);
-        d = dd;
-        g = t <= 0.f ? 0 : (t >= 1.f ? 1 : 2);
+    if (REG) g = t0 <= 0.f ? 0 : (t0 >= 1.f ? 1 : 2);
+    if (d1 < d) {
+        d = d1;
+        if (REG) g = t1 <= 0.f ? 1 : (t1 >= 1.f ? 3 : 5);
     }
-    if (!flat || s1 < 0.f) {
-        seg2(pbx, pby, pbz, r.e1, r.inv[1], dd, t);
-        if (dd < d) { d = dd; g = t <= 0.f ? 1 : (t >= 1.f ? 3 : 5); }
+    if (d2 < d) {
+        d = d2;
+        if (REG) g = t2 <= 0.f ? 3 : (t2 >= 1.f ? 0 : 4);
     }
-    if (!flat || s2 < 0.f) {
-        seg2(pcx, pcy, pcz, r.e2, r.inv[2], dd, t);
-        if (dd < d) { d = dd; g = t <= 0.f ? 3 : (t >= 1.f ? 0 : 4); }
+    if (face) {
+        d = __fmul_rn(dp, dp);
+        g = 6;
     }
-    *reg = g;
+    if (REG) *reg = g;
     return d;
+}
+
+// The distance and its region.
+__device__ __forceinline__ float dist_rec(const TriRec& r, float dx, float dy, float dz, int* reg) {
+    return dist_rec_t<true>(r, dx, dy, dz, reg);
+}
+// The distance alone (the same value as dist_rec).
+__device__ __forceinline__ float dist_rec_val(const TriRec& r, float dx, float dy, float dz) {
+    return dist_rec_t<false>(r, dx, dy, dz, nullptr);
 }
 
 // ------------------------------------------------------------------ outputs

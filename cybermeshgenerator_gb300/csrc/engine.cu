@@ -355,7 +355,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
     // persistent evaluation grid: resident CTAs per SM for the chosen kernel
     if (opts_.grab <= 0) opts_.grab = 1;
     if (opts_.stage < 0) opts_.stage = 0;
-    if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(opts_.precision, opts_.stage != 0) : sms;
+    if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(opts_.precision, opts_.stage != 0, opts_.ctas) : sms;
     else impl_->grid_eval = (brick == 4 ? 8 : 3) * sms;
 }
 
@@ -489,7 +489,7 @@ void Batch::run_impl(bool sizing) {
                     I.large_cnt + nseg, I.large_list, st);
     launch_brick_walk(false, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
                       I.bin_list, I.large_list, I.bound, I.cand_cnt, nullptr, nullptr, nullptr,
-                      stats_, st);
+                      stats_, opts_.walk_warps, st);
     exclusive_scan(I.cand_cnt, I.cand_off, nbrick_, I.scan_tmp, st);
     if (sizing) {
         int64_t C = 0;
@@ -510,15 +510,15 @@ void Batch::run_impl(bool sizing) {
     }
     launch_brick_walk(true, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
                       I.bin_list, I.large_list, I.bound, I.cand_cnt, I.cand_off, I.cand,
-                      I.brick_emax, stats_, st);
+                      I.brick_emax, stats_, opts_.walk_warps, st);
     if (opts_.brick == 16) launch_sub_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
     else launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
     radix_sort_pairs(I.work_keys, I.work, nwork_, 32, I.sort_tmp, st);
     CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
     if (timed) CMG_CUDA(cudaEventRecord(ev_[2], st));
     if (opts_.brick == 16)
-        launch_sdf_sub(opts_.precision, opts_.stage != 0, opts_.grab, dsegs_, nseg, I.work, nwork_,
-                       queue_, I.soup, I.tinfo,
+        launch_sdf_sub(opts_.precision, opts_.stage != 0, opts_.grab, opts_.probe, opts_.ctas, dsegs_,
+                       nseg, I.work, nwork_, queue_, I.soup, I.tinfo,
                        I.tinfo_lo, I.trec, I.tnorm, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
                        sdf32_, sdf64_, near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
     else
@@ -577,6 +577,9 @@ RunInfo Batch::info() {
     CMG_CUDA(cudaStreamSynchronize(stream_));
     r.brick = opts_.brick;
     r.grab = opts_.brick == 16 ? opts_.grab : 0;
+    r.walk_warps = brick_walk_warps(nbrick_, opts_.walk_warps);
+    r.probe = opts_.precision == kPrecMixed ? (opts_.probe > 0 ? opts_.probe : 1024) : 0;
+    r.ctas = opts_.brick == 16 ? sdf_sub_minb(opts_.ctas) : 0;
     r.cells = nvox_;
     r.pairs = pairs_cap_;
     r.candidates = cand_cap_;
@@ -608,9 +611,26 @@ void Batch::download(std::vector<HostResult>& out, RunInfo* info) {
 }
 
 // ------------------------------------------------------------------ autotuner
+// A coordinate search on the device, each candidate timed as a whole pipeline run
+// (the better of two runs after the sizing run), in this order:
+//   1. candidate brick edge and queue grab: 16^3 bricks evaluated by 4^3 sub-bricks
+//      taken 1 or 2 per grab, or 8^3 bricks with one evaluation CTA each;
+//   2. warps per brick of the candidate walk: 1, 2, 4 (the heaviest bricks' walks set
+//      the SDF preparation time when the bricks are few);
+//   3. mixed precision, 16^3 bricks: the probe head, 512 / 1024 / 2048 entries (a
+//      longer head gives a tighter bound and shorter filtered lists for more loads);
+//   4. 16^3 bricks: evaluation CTAs per SM, 12 (80 registers) or 16 (64 registers).
+// Each step keeps the fastest value and moves on; the result is cached per process by
+// workload shape.
+namespace {
+struct Tuned {
+    int brick, grab, walk_warps, probe, ctas;
+};
+}  // namespace
+
 void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t stream) {
     static std::mutex mu;
-    static std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> cache;
+    static std::map<std::tuple<int, int, int, int, int>, Tuned> cache;
     int64_t tris = 0, cells = 0;
     for (const HostMesh& m : meshes) {
         tris += m.ntris;
@@ -622,50 +642,82 @@ void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t s
     auto key = std::make_tuple(opts.precision, lg(tris), lg(cells),
                                static_cast<int>(std::min<size_t>(meshes.size(), 4)),
                                static_cast<int>(opts.want_sdf64));
+    auto apply = [&](const Tuned& t) {
+        opts.brick = t.brick;
+        opts.grab = t.grab;
+        opts.walk_warps = t.walk_warps;
+        opts.probe = t.probe;
+        opts.ctas = t.ctas;
+    };
     {
         std::lock_guard<std::mutex> g(mu);
         auto it = cache.find(key);
         if (it != cache.end()) {
-            opts.brick = it->second.first;
-            opts.grab = it->second.second;
+            apply(it->second);
             return;
         }
     }
-    // candidates: 16^3 candidate bricks evaluated by 4^3 sub-bricks taken 1 or 2 per
-    // queue grab, or 8^3 bricks with one evaluation CTA each
-    const std::pair<int, int> cand[] = {{16, 1}, {16, 2}, {8, 1}};
-    float best_ms = 0.f;
-    std::pair<int, int> best = cand[0];
     cudaEvent_t e0, e1;
     CMG_CUDA(cudaEventCreate(&e0));
     CMG_CUDA(cudaEventCreate(&e1));
-    bool first = true;
-    for (const auto& c : cand) {
+    auto time_one = [&](const Tuned& t) {
         VoxOpts o = opts;
-        o.brick = c.first;
-        o.grab = c.second;
+        o.brick = t.brick;
+        o.grab = t.grab;
+        o.walk_warps = t.walk_warps;
+        o.probe = t.probe;
+        o.ctas = t.ctas;
         o.autotune = false;
         Batch bt(meshes, o, stream);
         bt.run();  // sizing run (warms up as well)
         bt.synchronize();
-        CMG_CUDA(cudaEventRecord(e0, stream));
-        bt.run();
-        CMG_CUDA(cudaEventRecord(e1, stream));
-        CMG_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (first || ms < best_ms) {
-            best_ms = ms;
-            best = c;
-            first = false;
+        float best = 0.f;
+        for (int r = 0; r < 2; ++r) {
+            CMG_CUDA(cudaEventRecord(e0, stream));
+            bt.run();
+            CMG_CUDA(cudaEventRecord(e1, stream));
+            CMG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (r == 0 || ms < best) best = ms;
         }
+        return best;
+    };
+    Tuned cur{16, 1, 0, 0, 0};
+    float cur_ms = time_one(cur);
+    auto try_set = [&](Tuned t) {
+        const float ms = time_one(t);
+        if (ms < cur_ms) {
+            cur = t;
+            cur_ms = ms;
+        }
+    };
+    try_set({16, 2, 0, 0, 0});
+    try_set({8, 1, 0, 0, 0});
+    const Tuned step1 = cur;
+    for (int w : {1, 2, 4}) {
+        Tuned t = step1;
+        t.walk_warps = w;
+        try_set(t);
+    }
+    if (cur.brick == 16) {
+        if (opts.precision == kPrecMixed) {
+            const Tuned step2 = cur;
+            for (int pr : {512, 2048}) {
+                Tuned t = step2;
+                t.probe = pr;
+                try_set(t);
+            }
+        }
+        Tuned t = cur;
+        t.ctas = 16;
+        try_set(t);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> g(mu);
-    cache[key] = best;
-    opts.brick = best.first;
-    opts.grab = best.second;
+    cache[key] = cur;
+    apply(cur);
 }
 
 }  // namespace cmg::gpu

@@ -38,6 +38,10 @@ struct VoxOpts {
     int grab = 0;                  // sub-bricks per queue grab (1, 2, 4, 8); 0 = default
     int stage = -1;                // mixed: stage candidate records in shared memory
                                    // (1) or read them from L1/L2 (0); -1 = default
+    int walk_warps = 0;            // warps per brick in the candidate walk (1, 2, 4); 0 =
+                                   // by the brick count
+    int probe = 0;                 // mixed: brick-list head the probe scans; 0 = default
+    int ctas = 0;                  // evaluation CTAs per SM (12 or 16); 0 = default (12)
 };
 
 struct HostMesh {
@@ -129,6 +133,9 @@ struct RunInfo {
     Stats stats{};
     int brick = 0;
     int grab = 0;
+    int walk_warps = 0;  // warps per brick of the candidate walk
+    int probe = 0;       // probe head (mixed)
+    int ctas = 0;        // evaluation CTAs per SM
     int64_t cells = 0;
     int64_t pairs = 0;       // (triangle, column) bucket entries
     int64_t candidates = 0;  // (brick, triangle) candidate entries
@@ -222,10 +229,10 @@ private:
     void sized_run();
 };
 
-// Sets opts.brick and opts.grab for a workload by timing the candidates (16^3
-// bricks with 1 or 2 sub-bricks per queue grab, 8^3 bricks) on the device; the
-// choice is cached per process by workload shape (precision, log2 of triangle and
-// cell counts, number of meshes).
+// Sets opts.brick, grab, walk_warps, probe and ctas for a workload by timing the
+// candidates on the device (see engine.cu); the choice is cached per process by
+// workload shape (precision, log2 of triangle and cell counts, number of meshes,
+// whether FP64 distances are kept).
 void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t stream);
 
 // Number of SMs of the current device.

@@ -46,7 +46,10 @@ void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks
                        const float4* tinfo, const float4* tlo, const float4* thi,
                        const int64_t* bin_off, const int* bin_list, const int* large_list,
                        float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
-                       float* brick_emax, Stats* stats, cudaStream_t st);
+                       float* brick_emax, Stats* stats, int walk_warps, cudaStream_t st);
+// Warps per brick the walk uses: walk_warps when it is 1, 2 or 4, else by the brick
+// count (4 while 4-warp bricks fit about twice in the GPU, 2 up to twice that, then 1).
+int brick_walk_warps(int64_t nbricks, int walk_warps);
 void launch_count_K(int brick, const MeshSeg* segs, int nseg, int64_t nbricks, const float4* tinfo,
                     const int64_t* cand_off, const int* cand, const double* sdf64,
                     const float* sdf32, float band_cells, unsigned long long* out,
@@ -63,10 +66,13 @@ void launch_sdf_eval(int precision, int brick, const MeshSeg* segs, int nseg, co
 // sdf_sub.cu: evaluation by 4^3 sub-bricks of 16^3 candidate bricks.
 void launch_sub_work_keys(const int* cand_cnt, int64_t nbricks, uint32_t* keys, uint32_t* vals,
                           cudaStream_t st);
-int sdf_sub_grid(int precision, bool stage);
-void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, int nseg,
-                    const uint32_t* work, int64_t nwork, unsigned long long* queue, const double* soup,
-                    const float4* tinfo, const float4* tinfo_lo, const void* trec,
+// ctas: resident CTAs per SM of the evaluation kernel (16, or 12 for any other value);
+// probe: brick-list head scanned by the mixed probe (<= 0: the default).
+int sdf_sub_minb(int ctas);
+int sdf_sub_grid(int precision, bool stage, int ctas);
+void launch_sdf_sub(int precision, bool stage, int grab, int probe, int ctas, const MeshSeg* segs,
+                    int nseg, const uint32_t* work, int64_t nwork, unsigned long long* queue,
+                    const double* soup, const float4* tinfo, const float4* tinfo_lo, const void* trec,
                     const float4* tnorm, const int64_t* cand_off, const int* cand, const float* brick_emax,
                     float band_cells, const uint8_t* occ, float* sdf32, double* sdf64,
                     int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats, int grid,

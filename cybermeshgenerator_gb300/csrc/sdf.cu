@@ -124,13 +124,14 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         // product of rounded edges errs by at most 21 u |u| |v| (as a vector), which
         // turns its direction by at most twice that over |u x v|; then the
         // normalisation and the FP32 rounding of the components
-        if (tnorm) {
-            const double lu = sqrt(ux * ux + uy * uy + uz * uz), lv = sqrt(vx * vx + vy * vy + vz * vz);
-            const double en = nl > 0.0 ? 50.0 * kU64 * lu * lv / nl + 1.2e-7 : 0.0;
+        const double lu = sqrt(ux * ux + uy * uy + uz * uz), lv = sqrt(vx * vx + vy * vy + vz * vz);
+        const double en = nl > 0.0 ? 50.0 * kU64 * lu * lv / nl + 1.2e-7 : 0.0;
+        if (tnorm)
             tnorm[t] = make_float4(static_cast<float>(n3[0]), static_cast<float>(n3[1]),
                                    static_cast<float>(n3[2]), round_up_f(en));
-        }
-        r.pad_[0] = r.pad_[1] = 0.f;
+        // the record carries the same bound (nerr) for the plane test of the mixed path
+        r.nerr = round_up_f(en);
+        r.pad_ = 0.f;
         trec[t] = r;
     }
     // the mesh's coordinate scale max |v - K| (rounded up), per segment, for the
@@ -1062,16 +1063,21 @@ void launch_seg_finish(MeshSeg* segs, int nseg, const int64_t* large_off, const 
     CMG_LAUNCH();
 }
 
+int brick_walk_warps(int64_t nbricks, int walk_warps) {
+    if (walk_warps == 1 || walk_warps == 2 || walk_warps == 4) return walk_warps;
+    // 4 while 4-warp bricks fit about twice in the GPU's warp slots (a few heavy bricks
+    // set the time), 2 up to twice that, then 1
+    const int64_t sms = device_sms();
+    return nbricks <= 32 * sms ? 4 : (nbricks <= 64 * sms ? 2 : 1);
+}
+
 void launch_brick_walk(bool fill, const MeshSeg* segs, int nseg, int64_t nbricks, const double* soup,
                        const float4* tinfo, const float4* tlo, const float4* thi,
                        const int64_t* bin_off, const int* bin_list, const int* large_list,
                        float* bound, int* cand_cnt, const int64_t* cand_off, int* cand,
-                       float* brick_emax, Stats* stats, cudaStream_t st) {
+                       float* brick_emax, Stats* stats, int walk_warps, cudaStream_t st) {
     if (nbricks == 0) return;
-    // warps per brick: 4 while 4-warp bricks fit about twice in the GPU's warp slots
-    // (a few heavy bricks set the time), 2 up to twice that, then 1
-    const int64_t sms = device_sms();
-    const int W = nbricks <= 32 * sms ? 4 : (nbricks <= 64 * sms ? 2 : 1);
+    const int W = brick_walk_warps(nbricks, walk_warps);
     const unsigned grid = static_cast<unsigned>((nbricks * W + 3) / 4);
     auto go = [&](auto fill_tag, auto w_tag) {
         constexpr bool F = decltype(fill_tag)::value;

@@ -42,10 +42,51 @@ constexpr int kSubThreads = 64;  // one cell per thread
 // filtered candidates per round in shared memory (STAGE: their records as well)
 template <bool STAGE>
 struct Cap {
-    static constexpr int value = STAGE ? 256 : 512;
+    static constexpr int value = STAGE ? 256 : 384;
 };
+// mixed path: filtered entries per need-mask chunk (one bit per entry); the records a
+// warp needs in a chunk are staged in its own shared-memory slots
+constexpr int kChunk = 32;
 constexpr int kBatch = 4;  // candidates per thread per probe/filter step (loads in flight)
-constexpr int kProbe = 1024;  // head of the brick list the mixed probe scans (swept: 256-2048)
+constexpr int kProbe = 1024;  // default head of the brick list the mixed probe scans
+
+// Reach of a cell's sphere test against one filtered triangle (mixed path): the cell
+// may need the triangle when |cell - centroid| <= lim, lim = (b + w)(1 + 16u) + 16u r
+// (b the cell's bound, w the triangle's radius, r the sub-brick radius; the margins
+// cover the FP32 rounding of the centroids, cell offsets and bound). Evaluated as
+//   reach_term(w, r) = RU(w (1 + 20u) + RU(17u r))     once per triangle, and
+//   reach(b, term)   = RU(b (1 + 20u) + term)           per cell,
+// which is at least (b + w)(1 + 20u) + 17u r. The same expression rounded to nearest
+// step by step is at most (b + w)(1 + 16u)(1 + u)^3 + 16u r (1 + u)^2, which is smaller,
+// so this test admits every triangle the step-by-step form admits.
+__device__ __forceinline__ float reach_term(float w, float r) {
+    return __fmaf_ru(w, 1.f + 20.f * kU32, __fmul_ru(17.f * kU32, r));
+}
+__device__ __forceinline__ float reach(float b, float term) {
+    return __fmaf_ru(b, 1.f + 20.f * kU32, term);
+}
+
+// A cell's bound in the mixed path, from its smallest FP32 squared distance so far, d2:
+// sqrt(d2) rounded (1 + 8u) plus the stated FP32 error of a distance of that size,
+// 48u (d + 2 e + 2 r) with d <= sqrt(d2) + the error itself (kap = 98u (e + r)). A
+// triangle whose FP32 distance can still be at most the current minimum lies within
+// this bound, so its sphere test passes whatever order the candidates come in: the
+// cell ends with the exact (FP32 distance, triangle id) minimum over all triangles,
+// independent of the order of the filtered list (which the warps' scheduling sets).
+__device__ __forceinline__ float cell_bound(float d2, float kap) {
+    return __fmaf_ru(sqrtf(d2), 1.f + 58.f * kU32, kap);
+}
+
+// Largest computed plane distance |n . (cell - a)| of a triangle that can still reach
+// the cell's FP32 minimum, for a cell bound b (cell_bound): such a triangle is within b
+// of the cell, so |cell - a| <= b + 2e (a a vertex, e the brick's largest
+// centroid-to-vertex distance), and the FP32 plane distance errs by at most
+// nerr |cell - a| (nerr bounds the FP32 unit normal's error, TriRec::nerr) plus the
+// rounding of the recentred offsets and the dot product, all within
+// (nerr + 64u)(b + 4e + 4r) (ebr4 = 4(e + r), rounded up).
+__device__ __forceinline__ float plane_reach(float b, float nerr, float ebr4) {
+    return __fmaf_ru(__fadd_ru(b, ebr4), __fadd_ru(nerr, 64.f * kU32), b);
+}
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only) and its wait.
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -80,12 +121,14 @@ __device__ __forceinline__ SubGeo sub_geo(const MeshSeg& s, int64_t lb, int sub)
 
 // PREC: kPrecMixed or kPrecFP64. STAGE (mixed only): copy the records of the
 // filtered candidates into shared memory (cp.async) instead of reading them
-// from L1/L2 at evaluation time. grab: consecutive sub-bricks taken from the queue
-// at once (a divisor of 64: they share one brick list).
-template <int PREC, bool STAGE>
-__global__ void __launch_bounds__(kSubThreads, 12)
+// from L1/L2 at evaluation time. MINB: resident CTAs per SM the registers are
+// budgeted for (12: 80 registers; 16: 64). grab: consecutive sub-bricks taken from
+// the queue at once (a divisor of 64: they share one brick list). probe_n: entries
+// of the brick list head the mixed probe scans.
+template <int PREC, bool STAGE, int MINB>
+__global__ void __launch_bounds__(kSubThreads, MINB)
 k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict__ work,
-          int64_t nwork, int grab_n, unsigned long long* __restrict__ queue,
+          int64_t nwork, int grab_n, int probe_n, unsigned long long* __restrict__ queue,
           const double* __restrict__ soup,
           const float4* __restrict__ tinfo, const float4* __restrict__ tinfo_lo,
           const TriRec* __restrict__ trec, const float4* __restrict__ tnorm,
@@ -100,6 +143,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
     __shared__ float s_pe[PREC == kPrecFP64 ? kCap : 1];
     __shared__ int s_t[kCap];
     __shared__ TriRec s_rec[STAGE ? kCap : 1];
+    __shared__ TriRec s_wrec[PREC == kPrecMixed && !STAGE ? (kSubThreads / 32) * kChunk : 1];
     __shared__ int s_n;
     __shared__ long long s_item;
     __shared__ unsigned long long s_red[kSubThreads / 32];
@@ -151,7 +195,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         // triangles, then bins ring by ring), so its head holds the centre's nearest. The
         // mixed path scans only the head (a looser U lengthens the filtered lists a
         // little, which the cheap FP32 distances absorb); the FP64 path scans it all
-        const int64_t cp = PREC == kPrecMixed && c1 - c0 > kProbe ? c0 + kProbe : c1;
+        const int64_t cp = PREC == kPrecMixed && c1 - c0 > probe_n ? c0 + probe_n : c1;
         for (int64_t k0 = c0 + tid; k0 < cp; k0 += kBatch * kSubThreads) {
             // loads of kBatch candidates in flight before any of them is used
             int tt[kBatch];
@@ -178,8 +222,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 if (dc - hi.w < tb) {
                     TriRec r;
                     load_rec(trec, t, r);
-                    int reg;
-                    const float d = sqrtf(dist_rec(r, -rx, -ry, -rz, &reg));
+                    const float d = sqrtf(dist_rec_val(r, -rx, -ry, -rz));
                     const float ub = d * (1.f + 32.f * kU32) + 32.f * kU32 * (dc + 2.f * hi.w);
                     if (ub < tb || (ub == tb && t < tseed)) { tb = ub; tseed = t; }
                 }
@@ -189,8 +232,8 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         unsigned long long key =
             (static_cast<unsigned long long>(__float_as_uint(tb)) << 32) | static_cast<unsigned>(tseed);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, sh);
             key = k2 < key ? k2 : key;
         }
         if (lane == 0) s_red[warp] = key;
@@ -200,8 +243,16 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         for (int i = 1; i < kSubThreads / 32; ++i) kmin = s_red[i] < kmin ? s_red[i] : kmin;
         const float U = __uint_as_float(static_cast<unsigned>(kmin >> 32));
         const int seed = static_cast<int>(static_cast<unsigned>(kmin & 0xffffffffull));
-        // a triangle can be nearest to a cell only if its sphere reaches U + 2 r
-        const float limf = (U + 2.f * r4) * (1.f + 32.f * kU32) + 32.f * kU32 * (U + r4);
+        // mixed: the stated FP32 error of a distance near d is 48u (d + 2 e + 2 r) (e the
+        // brick's largest centroid-to-vertex distance); kap carries its constant part
+        const float kap = PREC == kPrecMixed ? __fmul_ru(98.f * kU32, brick_emax[gb] + r4) : 0.f;
+        const float ebr4 = PREC == kPrecMixed ? __fmul_ru(4.f, __fadd_ru(brick_emax[gb], r4)) : 0.f;
+        // a triangle can be nearest to a cell only if its sphere reaches U + 2 r; in the
+        // mixed path, also any triangle whose FP32 distance can undercut the nearest
+        // one's (two stated errors more), so the filtered list holds every triangle the
+        // FP32 minimum can come from
+        const float limf = (U + 2.f * r4) * (1.f + 32.f * kU32) + 32.f * kU32 * (U + r4) +
+                           (PREC == kPrecMixed ? __fmaf_ru(100.f * kU32, U + 4.f * r4, 2.f * kap) : 0.f);
 
         // ---- 2+3. rounds: filter into shared memory, then evaluate the cells
         float best = FLT_MAX, bestd = FLT_MAX;  // FP32 path
@@ -225,7 +276,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 ++evals;
                 bt = seed;
                 br = reg;
-                bestd = sqrtf(best) * (1.f + 8.f * kU32);
+                bestd = cell_bound(best, kap);
             } else {
                 d3 a, b, c;
                 load_soup(soup, seed, a, b, c);
@@ -287,6 +338,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     base = __shfl_sync(0xffffffffu, base, 0);
                     if (take) {
                         const int pos = base + __popc(m & ((1u << lane) - 1u));
+                        if (PREC == kPrecMixed && !STAGE) e.w = reach_term(e.w, r4);
                         s_c[pos] = e;
                         if (PREC == kPrecFP64) {
                             s_nrm[pos] = nv;
@@ -307,6 +359,82 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 n = s_n;
             }
             if (tid == 0 && n) atomicAdd(&st->filtered, static_cast<unsigned long long>(n));
+            if (PREC == kPrecMixed && !STAGE) {
+                // In chunks of kChunk entries: each lane marks the entries its cell may
+                // need under its bound at the start of the chunk (s_c[].w holds the
+                // radius term of the reach, see reach_term); the warp stages the records
+                // of the union into its shared slots (lane k loads entry k's record:
+                // every load of the chunk in flight at once) and evaluates every marked
+                // entry. The bound only shrinks and the test admits at least what the
+                // one-by-one test with the running bound admits, so every triangle that
+                // can be nearest is evaluated; the running minimum is of (distance,
+                // triangle id) pairs, so the extra evaluations change nothing.
+                TriRec* wrec = s_wrec + warp * kChunk;
+                for (int j0 = 0; j0 < n; j0 += kChunk) {
+                    const int cnt = min(kChunk, n - j0);
+                    unsigned mine = 0;
+                    if (valid) {
+                        const float bl = bestd;
+                        if (cnt == kChunk) {
+#pragma unroll
+                            for (int k = 0; k < kChunk; ++k) {
+                                const float4 e = s_c[j0 + k];
+                                const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                                const float lim = reach(bl, e.w);
+                                if (dx * dx + dy * dy + dz * dz <= lim * lim) mine |= 1u << k;
+                            }
+                        } else {
+                            for (int k = 0; k < cnt; ++k) {
+                                const float4 e = s_c[j0 + k];
+                                const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                                const float lim = reach(bl, e.w);
+                                if (dx * dx + dy * dy + dz * dz <= lim * lim) mine |= 1u << k;
+                            }
+                        }
+                    }
+                    const unsigned any = __reduce_or_sync(0xffffffffu, mine);
+                    if (!any) continue;
+                    if ((any >> lane) & 1u) {
+                        const int slot = __popc(any & ((1u << lane) - 1u));
+                        const float4* src = reinterpret_cast<const float4*>(trec + s_t[j0 + lane]);
+                        float4* dst = reinterpret_cast<float4*>(wrec + slot);
+                        float4 v[9];
+#pragma unroll
+                        for (int q2 = 0; q2 < 9; ++q2) v[q2] = __ldg(src + q2);
+#pragma unroll
+                        for (int q2 = 0; q2 < 9; ++q2) dst[q2] = v[q2];
+                    }
+                    __syncwarp();
+                    unsigned m = any;
+                    for (int slot = 0; m; ++slot) {
+                        const int k = __ffs(m) - 1;
+                        m &= m - 1u;
+                        const float4 e = s_c[j0 + k];
+                        const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                        // the plane: a triangle is no nearer than its plane, so a marked
+                        // triangle whose plane lies beyond every lane's bound is skipped
+                        // (see plane_reach; a degenerate triangle has a zero normal and
+                        // is never skipped)
+                        const TriRec& R = wrec[slot];
+                        const float dp = dot3f(__fsub_rn(dx, R.o0[0]), __fsub_rn(dy, R.o0[1]),
+                                               __fsub_rn(dz, R.o0[2]), R.nn);
+                        if (!__any_sync(0xffffffffu, valid && fabsf(dp) <= plane_reach(bestd, R.nerr, ebr4)))
+                            continue;
+                        if (valid) {
+                            const float d2 = dist_rec_val(wrec[slot], dx, dy, dz);
+                            ++evals;
+                            const int t = s_t[j0 + k];
+                            if (d2 < best || (d2 == best && t < bt)) {
+                                best = d2;
+                                bt = t;
+                                br = -1;  // the region of the final triangle is found below
+                                bestd = cell_bound(d2, kap);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            } else
             for (int j = 0; j < n; ++j) {
                 const float4 e = s_c[j];
                 const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
@@ -333,7 +461,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                             best = d2;
                             bt = t;
                             br = reg;
-                            bestd = sqrtf(d2) * (1.f + 8.f * kU32);
+                            bestd = cell_bound(d2, kap);
                         }
                     }
                 } else {
@@ -424,8 +552,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                         TriRec r;
                         load_rec(trec, t, r);
                         if (!need) continue;
-                        int reg;
-                        const float d = sqrtf(dist_rec(r, dx, dy, dz, &reg));
+                        const float d = sqrtf(dist_rec_val(r, dx, dy, dz));
                         if (d > reach * (1.f + 1e-6f)) continue;
                         d3 a, b, c;
                         load_soup(soup, t, a, b, c);
@@ -451,6 +578,17 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 write_cell(o, idx, __dsqrt_rn(best_band), bt64, br64);
                 if (o.errbound) o.errbound[idx] = 0.f;
             } else {
+                if (PREC == kPrecMixed && !STAGE && br < 0 && o.near_reg) {
+                    // the region of the nearest triangle: its distance again, recentred
+                    // exactly as the filter recentred it (the same value, now with the
+                    // region)
+                    const float4 hi = tinfo[bt], lo = tinfo_lo[bt];
+                    const float ex = (hi.x - chx) + (lo.x - clx), ey = (hi.y - chy) + (lo.y - cly),
+                                ez = (hi.z - chz) + (lo.z - clz);
+                    TriRec r;
+                    load_rec(trec, bt, r);
+                    dist_rec(r, px - ex, py - ey, pz - ez, &br);
+                }
                 write_cell(o, idx, static_cast<double>(sqrtf(best)), bt, br);
                 if (o.errbound) o.errbound[idx] = eb;
             }
@@ -489,25 +627,33 @@ void launch_sub_work_keys(const int* cand_cnt, int64_t nbricks, uint32_t* keys, 
     CMG_LAUNCH();
 }
 
-int sdf_sub_grid(int precision, bool stage) {
-    int dev = 0, sms = 0, per = 0;
-    CMG_CUDA(cudaGetDevice(&dev));
-    CMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (precision == kPrecMixed && stage)
-        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecMixed, true>,
-                                                               kSubThreads, 0));
-    else if (precision == kPrecMixed)
-        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecMixed, false>,
-                                                               kSubThreads, 0));
-    else
-        CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<kPrecFP64, false>,
-                                                               kSubThreads, 0));
-    return sms * (per > 0 ? per : 1);
+namespace {
+template <int PREC, bool STAGE, int MINB>
+int resident_ctas() {
+    int per = 0;
+    CMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sdf_sub<PREC, STAGE, MINB>,
+                                                           kSubThreads, 0));
+    return per > 0 ? per : 1;
+}
+}  // namespace
+
+// Resident CTAs per SM targeted by the evaluation kernel: 16 when asked for, else 12.
+int sdf_sub_minb(int ctas) { return ctas == 16 ? 16 : 12; }
+
+int sdf_sub_grid(int precision, bool stage, int ctas) {
+    const int sms = device_sms();
+    const bool hi = sdf_sub_minb(ctas) == 16;
+    int per;
+    if (precision == kPrecMixed && stage) per = resident_ctas<kPrecMixed, true, 12>();
+    else if (precision == kPrecMixed) per = hi ? resident_ctas<kPrecMixed, false, 16>()
+                                               : resident_ctas<kPrecMixed, false, 12>();
+    else per = hi ? resident_ctas<kPrecFP64, false, 16>() : resident_ctas<kPrecFP64, false, 12>();
+    return sms * per;
 }
 
-void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, int nseg,
-                    const uint32_t* work, int64_t nwork, unsigned long long* queue, const double* soup,
-                    const float4* tinfo, const float4* tinfo_lo, const void* trec,
+void launch_sdf_sub(int precision, bool stage, int grab, int probe, int ctas, const MeshSeg* segs,
+                    int nseg, const uint32_t* work, int64_t nwork, unsigned long long* queue,
+                    const double* soup, const float4* tinfo, const float4* tinfo_lo, const void* trec,
                     const float4* tnorm, const int64_t* cand_off, const int* cand, const float* brick_emax,
                     float band_cells, const uint8_t* occ, float* sdf32, double* sdf64,
                     int* near_tri, uint8_t* near_reg, float* errbound, Stats* stats, int grid,
@@ -516,18 +662,16 @@ void launch_sdf_sub(int precision, bool stage, int grab, const MeshSeg* segs, in
     Out o{occ, sdf32, sdf64, near_tri, near_reg, errbound};
     const TriRec* r = static_cast<const TriRec*>(trec);
     if (grab != 1 && grab != 2 && grab != 4 && grab != 8) grab = 1;
-    if (precision == kPrecMixed && stage)
-        k_sdf_sub<kPrecMixed, true><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
-            brick_emax, band_cells, o, stats);
-    else if (precision == kPrecMixed)
-        k_sdf_sub<kPrecMixed, false><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
-            brick_emax, band_cells, o, stats);
-    else
-        k_sdf_sub<kPrecFP64, false><<<grid, kSubThreads, 0, st>>>(
-            segs, nseg, work, nwork, grab, queue, soup, tinfo, tinfo_lo, r, tnorm, cand_off, cand,
-            brick_emax, band_cells, o, stats);
+    if (probe <= 0) probe = kProbe;
+    const bool hi = sdf_sub_minb(ctas) == 16;
+    auto go = [&](auto kernel) {
+        kernel<<<grid, kSubThreads, 0, st>>>(segs, nseg, work, nwork, grab, probe, queue, soup, tinfo,
+                                            tinfo_lo, r, tnorm, cand_off, cand, brick_emax, band_cells,
+                                            o, stats);
+    };
+    if (precision == kPrecMixed && stage) go(k_sdf_sub<kPrecMixed, true, 12>);
+    else if (precision == kPrecMixed) hi ? go(k_sdf_sub<kPrecMixed, false, 16>) : go(k_sdf_sub<kPrecMixed, false, 12>);
+    else hi ? go(k_sdf_sub<kPrecFP64, false, 16>) : go(k_sdf_sub<kPrecFP64, false, 12>);
     CMG_LAUNCH();
 }
 

@@ -43,10 +43,14 @@ class SDFPlan:
 
     ``grid`` is ``(corner, spacing, dims)``: the min corner of cell (0, 0, 0), the
     cubic cell edge and ``(nx, ny, nz)``. ``precision`` is ``PREC_FP64`` (plain,
-    bit-identical to the reference's distances) or ``PREC_MIXED``."""
+    bit-identical to the reference's distances) or ``PREC_MIXED``. ``autotune`` times
+    the pipeline's tunables on this mesh and grid at creation (brick edge, queue grab,
+    walk warps, probe head, evaluation CTAs per SM) and keeps the fastest; ``tuning``
+    (keys of ``make_opts``) sets them instead."""
 
     def __init__(self, vertices, faces, grid, precision: int = PREC_FP64,
-                 predicates: int = PRED_COMPAT, band: float = 1.0, brick: int = 0):
+                 predicates: int = PRED_COMPAT, band: float = 1.0, brick: int = 0,
+                 autotune: bool = False, **tuning):
         v = np.ascontiguousarray(
             vertices.detach().cpu().numpy() if isinstance(vertices, torch.Tensor) else vertices,
             dtype=np.float64)
@@ -61,7 +65,7 @@ class SDFPlan:
         self.spacing = float(spacing)
         self.npoints, self.ntriangles = len(v), len(f)
         o = make_opts(outputs=0, precision=precision, predicates=predicates, grid=grid,
-                      band=band, brick=brick)
+                      band=band, brick=brick, autotune=autotune, **tuning)
         out = ctypes.c_void_p()
         err = _err()
         _check(_clib.cmg_sdf_plan_create(v.ctypes.data_as(_L.c_double_p), len(v),

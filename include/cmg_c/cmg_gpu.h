@@ -48,11 +48,17 @@ typedef struct cmg_voxel_opts {
     double band;         /* mixed: FP64 refinement band around the surface, in cells */
     int brick;           /* SDF candidate brick edge: 0 = default (16, evaluated by 4^3
                             sub-bricks), 8 or 4 (one evaluation CTA per brick) */
-    int autotune;        /* nonzero (with brick 0): time the brick edges and queue grab
-                            sizes on this input and keep the fastest */
+    int autotune;        /* nonzero (with brick 0): time the brick edges, queue grab sizes,
+                            walk warps, probe heads and evaluation CTAs per SM on this
+                            input and keep the fastest */
     int grab;            /* sub-bricks taken per work-queue grab: 0 = default, 1, 2, 4, 8 */
     int stage;           /* mixed: 1 stage candidate records in shared memory, 0 read them
                             through L1/L2, -1 = default */
+    int walk_warps;      /* warps per brick of the candidate walk: 1, 2 or 4; 0 = by the
+                            brick count */
+    int probe;           /* mixed: brick-list head the probe scans (entries); 0 = 1024 */
+    int ctas;            /* evaluation CTAs per SM the registers are budgeted for: 16, or
+                            0 / 12 = 12 */
 } cmg_voxel_opts;
 
 /* Counters of one voxelization. */
@@ -71,6 +77,9 @@ typedef struct cmg_voxel_stats {
     int brick;                 /* brick edge used */
     int grab;                  /* sub-bricks per work-queue grab used (16^3 bricks) */
     double max_error_bound;    /* mixed: largest stated per-cell bound (0 for FP64) */
+    int walk_warps;            /* warps per brick of the candidate walk used */
+    int probe;                 /* probe head used (mixed; 0 for FP64) */
+    int ctas;                  /* evaluation CTAs per SM used (16^3 bricks) */
 } cmg_voxel_stats;
 
 /* Defaults: resolution 64, pad 1, occupancy, FP64, compat predicates, band 1. */
