@@ -330,7 +330,9 @@ def _geometry(h):
 @dataclass
 class VoxelResult:
     """Outputs of :func:`voxelize_ex`, flat in the C layout idx = (k*ny + j)*nx + i
-    (``as_xyz`` reshapes to (nx, ny, nz))."""
+    (``as_xyz`` reshapes to (nx, ny, nz)). ``dims`` counts the layers held; ``layers``
+    is (z_begin, z_end, nz of the grid): a slab holds layers z_begin .. z_end-1 of the
+    grid whose corner and origin it reports."""
 
     dims: tuple
     origin: np.ndarray
@@ -343,6 +345,7 @@ class VoxelResult:
     nearest_region: Optional[np.ndarray] = None
     error_bound: Optional[np.ndarray] = None
     stats: Dict[str, float] = field(default_factory=dict)
+    layers: tuple = (0, 0, 0)
 
     def as_xyz(self, a: np.ndarray) -> np.ndarray:
         return _to_xyz(a, self.dims)
@@ -352,7 +355,10 @@ def make_opts(resolution: int = 64, pad: int = 1, outputs: int = OUT_OCCUPANCY,
               precision: int = PREC_FP64, predicates: int = PRED_COMPAT, grid=None,
               band: float = 1.0, brick: int = 0, autotune: bool = False, grab: int = 0,
               stage: int = -1, walk_warps: int = 0, probe: int = 0,
-              ctas: int = 0) -> _L.VoxelOpts:
+              ctas: int = 0, layers=None) -> _L.VoxelOpts:
+    """Options of voxelize_ex / Batch. ``layers=(z_begin, z_end)`` evaluates cell layers
+    [z_begin, z_end) of the grid only (a z-slab; equal to those layers of the whole
+    grid bit for bit)."""
     o = _L.VoxelOpts()
     _clib.cmg_voxel_opts_init(ctypes.byref(o))
     o.resolution, o.pad, o.outputs = int(resolution), int(pad), int(outputs)
@@ -360,6 +366,8 @@ def make_opts(resolution: int = 64, pad: int = 1, outputs: int = OUT_OCCUPANCY,
     o.band, o.brick, o.autotune = float(band), int(brick), int(bool(autotune))
     o.grab, o.stage = int(grab), int(stage)
     o.walk_warps, o.probe, o.ctas = int(walk_warps), int(probe), int(ctas)
+    if layers is not None:
+        o.z_begin, o.z_end = int(layers[0]), int(layers[1])
     if grid is not None:
         corner, spacing, dims = grid
         o.explicit_grid = 1
@@ -410,6 +418,8 @@ def _result_from_handle(h, owner: Optional[_Owner] = None) -> VoxelResult:
 
     st = _L.VoxelStats()
     _clib.cmg_voxels_stats(h, ctypes.byref(st))
+    z0, z1, nzg = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _clib.cmg_voxels_layers(h, ctypes.byref(z0), ctypes.byref(z1), ctypes.byref(nzg))
     return VoxelResult(
         dims=dims, origin=origin, corner=np.array([cx.value, cy.value, cz.value]), spacing=spacing,
         occupancy=grab(_clib.cmg_voxels_occupancy, np.uint8),
@@ -418,7 +428,22 @@ def _result_from_handle(h, owner: Optional[_Owner] = None) -> VoxelResult:
         nearest_triangle=grab(_clib.cmg_voxels_nearest_triangle, np.int32),
         nearest_region=grab(_clib.cmg_voxels_nearest_region, np.uint8),
         error_bound=grab(_clib.cmg_voxels_error_bound, np.float32),
-        stats=st.as_dict())
+        stats=st.as_dict(), layers=(z0.value, z1.value, nzg.value))
+
+
+def plc_grid(plc: PLC, resolution: int = 64, pad: int = 1):
+    """(corner, spacing, dims) of the grid voxelize(plc, resolution, ., pad) uses (host
+    only, no GPU)."""
+    if not isinstance(plc, PLC):
+        raise TypeError("plc must be a PLC")
+    corner = np.zeros(3)
+    spacing = ctypes.c_double()
+    dims = np.zeros(3, dtype=np.int32)
+    err = ctypes.create_string_buffer(256)
+    _check(_clib.cmg_plc_grid(plc._handle, int(resolution), int(pad),
+                              corner.ctypes.data_as(_L.c_double_p), ctypes.byref(spacing),
+                              dims.ctypes.data_as(_L.c_int_p), err, 256), err)
+    return corner, spacing.value, tuple(int(d) for d in dims)
 
 
 def voxelize_ex(plc: PLC, **kw) -> VoxelResult:
@@ -620,7 +645,7 @@ def library_path() -> str:
     return _L.library_path()
 
 
-__all__ = ["orient3d_stream", "insphere_stream", "host_empty", "orient3d_signs", "orient3d_batch", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "make_opts", "Batch",
+__all__ = ["orient3d_stream", "insphere_stream", "host_empty", "orient3d_signs", "orient3d_batch", "PLC", "VoxelGrid", "VoxelResult", "voxelize", "voxelize_ex", "plc_grid", "make_opts", "Batch",
            "version", "gpu_version", "library_path", "OUT_OCCUPANCY", "OUT_SDF_F32", "OUT_SDF_F64",
            "OUT_NEAREST", "OUT_ERROR_BOUND", "PREC_FP64", "PREC_MIXED", "PRED_COMPAT", "PRED_EXACT",
            "read_plc", "plc_from_stl", "self_intersections", "simplify", "stl_last_timing",

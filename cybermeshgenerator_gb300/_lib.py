@@ -30,7 +30,8 @@ class VoxelOpts(ctypes.Structure):
                 ("corner", ctypes.c_double * 3), ("spacing", ctypes.c_double),
                 ("dims", ctypes.c_int * 3), ("band", ctypes.c_double), ("brick", ctypes.c_int),
                 ("autotune", ctypes.c_int), ("grab", ctypes.c_int), ("stage", ctypes.c_int),
-                ("walk_warps", ctypes.c_int), ("probe", ctypes.c_int), ("ctas", ctypes.c_int)]
+                ("walk_warps", ctypes.c_int), ("probe", ctypes.c_int), ("ctas", ctypes.c_int),
+                ("z_begin", ctypes.c_int), ("z_end", ctypes.c_int)]
 
 
 class VoxelStats(ctypes.Structure):
@@ -163,6 +164,8 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_voxels_nearest_region", c_ubyte_p, [V])
     sig("cmg_voxels_error_bound", c_float_p, [V])
     sig("cmg_voxels_corner", None, [V, c_double_p, c_double_p, c_double_p])
+    sig("cmg_voxels_layers", None, [V, c_int_p, c_int_p, c_int_p])
+    sig("cmg_plc_grid", I, [V, I, I, c_double_p, c_double_p, c_int_p, S, Z])
     sig("cmg_voxels_stats", None, [V, ctypes.POINTER(VoxelStats)])
     sig("cmg_batch_create", I, [ctypes.POINTER(V), c_int_p, c_int_p, I,
                                 ctypes.POINTER(VoxelOpts), c_void_pp, S, Z])

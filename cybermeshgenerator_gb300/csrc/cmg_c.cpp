@@ -69,7 +69,8 @@ struct cmg_voxels {
     double corner[3] = {0, 0, 0};
     double origin[3] = {0, 0, 0};
     double spacing = 0;
-    int nx = 0, ny = 0, nz = 0;
+    int nx = 0, ny = 0, nz = 0;   // nz: the layers held (the slab's)
+    int z0 = 0, z1 = 0, nz_grid = 0;  // the slab [z0, z1) of the grid's nz_grid layers
     cmg::gpu::HostResult r;
     cmg_voxel_stats stats{};
 };
@@ -262,6 +263,8 @@ void fill_stats(cmg_voxels* v, const cmg::gpu::RunInfo& ri) {
     s.max_error_bound = m;
 }
 
+// The handle's geometry: the grid's corner and origin (centre of cell (0,0,0) of the
+// whole grid) and, along z, the layers held (a slab's, or all).
 void set_geometry(cmg_voxels* v, const GridDesc& g) {
     for (int a = 0; a < 3; ++a) {
         v->corner[a] = g.corner[a];
@@ -270,8 +273,23 @@ void set_geometry(cmg_voxels* v, const GridDesc& g) {
     v->spacing = g.h;
     v->nx = g.nx;
     v->ny = g.ny;
-    v->nz = g.nz;
+    v->z0 = g.z1 > 0 ? g.z0 : 0;
+    v->z1 = g.z1 > 0 ? g.z1 : g.nz;
+    v->nz_grid = g.nz;
+    v->nz = v->z1 - v->z0;
 }
+
+// The cell layers [z_begin, z_end) of the options (z_end 0: through the last layer),
+// checked against the grid's nz layers.
+void set_layers(const cmg_voxel_opts& o, GridDesc& g) {
+    const int z1 = o.z_end == 0 ? g.nz : o.z_end;
+    if (o.z_begin < 0 || o.z_begin >= z1 || z1 > g.nz)
+        throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: cell layers [z_begin, z_end) outside the grid"};
+    g.z0 = o.z_begin;
+    g.z1 = z1;
+}
+
+bool has_layers(const cmg_voxel_opts& o) { return o.z_begin != 0 || o.z_end != 0; }
 
 // One voxelization of host arrays: pts (npts points of 3 coordinates), tris (ntris
 // triangles of 3 indices, already fanned and checked).
@@ -289,6 +307,7 @@ cmg_voxels* voxelize_arrays(const double* pts, int64_t npts, const int* tris, in
         throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
     }
     check_grid_size(g);
+    set_layers(o, g);
     const int outputs = effective_outputs(o);
     cmg::gpu::VoxOpts vo = to_vox(o, outputs);
     cmg::gpu::HostMesh m;
@@ -522,6 +541,31 @@ void cmg_voxels_corner(const cmg_voxels* v, double* x, double* y, double* z) {
     if (z) *z = v ? v->corner[2] : 0.0;
 }
 
+cmg_status cmg_plc_grid(const cmg_plc* plc, int resolution, int pad, double* corner,
+                        double* spacing, int* dims, char* errbuf, size_t len) {
+    if (!plc || !corner || !spacing || !dims) return CMG_ERR_INVALID_INPUT;
+    return guarded(errbuf, len, [&] {
+        if (resolution < 1)
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: resolution must be >= 1"};
+        if (plc->points.empty())
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: PLC has no points"};
+        GridDesc g{};
+        if (!make_grid(plc->points.data(), plc->points.size() / 3, resolution, pad, g))
+            throw CoreError{CMG_ERR_INVALID_INPUT, "voxelize: degenerate (zero-extent) PLC"};
+        for (int a = 0; a < 3; ++a) corner[a] = g.corner[a];
+        *spacing = g.h;
+        dims[0] = g.nx;
+        dims[1] = g.ny;
+        dims[2] = g.nz;
+    });
+}
+
+void cmg_voxels_layers(const cmg_voxels* v, int* z_begin, int* z_end, int* nz_grid) {
+    if (z_begin) *z_begin = v ? v->z0 : 0;
+    if (z_end) *z_end = v ? v->z1 : 0;
+    if (nz_grid) *nz_grid = v ? v->nz_grid : 0;
+}
+
 double cmg_voxels_spacing(const cmg_voxels* v) { return v ? v->spacing : 0.0; }
 
 const unsigned char* cmg_voxels_occupancy(const cmg_voxels* v) {
@@ -558,6 +602,10 @@ cmg_status cmg_batch_create(const cmg_plc* const* plcs, const int* resolutions, 
     if (out) *out = nullptr;
     if (!plcs || !opts || !out || n < 1) return CMG_ERR_INVALID_INPUT;
     if (!opts->explicit_grid && (!resolutions || !pads)) return CMG_ERR_INVALID_INPUT;
+    if (has_layers(*opts)) {
+        set_err(errbuf, len, "cmg_batch_create: a batch is split by whole meshes, not by cell layers");
+        return CMG_ERR_UNSUPPORTED_OPTION;
+    }
     return guarded(errbuf, len, [&] {
         std::vector<cmg::gpu::HostVec<int>> tris(static_cast<size_t>(n));
         std::vector<cmg::gpu::HostMesh> meshes(static_cast<size_t>(n));
@@ -687,6 +735,10 @@ cmg_status cmg_sdf_plan_create(const double* points, int64_t npoints, const int*
     if (out) *out = nullptr;
     if (!points || !triangles || !opts || !out || npoints < 1 || ntriangles < 1)
         return CMG_ERR_INVALID_INPUT;
+    if (has_layers(*opts)) {
+        set_err(errbuf, len, "cmg_sdf_plan_create: a plan holds the whole grid (no cell layers)");
+        return CMG_ERR_UNSUPPORTED_OPTION;
+    }
     return guarded(errbuf, len, [&] {
         if (!opts->explicit_grid)
             throw CoreError{CMG_ERR_INVALID_INPUT, "cmg_sdf_plan_create: an explicit grid is required"};

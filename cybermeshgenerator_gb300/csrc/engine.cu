@@ -225,7 +225,12 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
              bool transient)
     : opts_(opts), stream_(stream) {
     impl_.reset(new Impl(transient ? pool_for_device().a : nullptr));
-    const int brick = pick_brick(opts);
+    bool slab = false;
+    for (const HostMesh& m : meshes)
+        slab = slab || (m.g.z1 > 0 && (m.g.z0 != 0 || m.g.z1 != m.g.nz));
+    // a slab is evaluated by 16^3 bricks (their 4^3 sub-bricks keep the whole grid's
+    // geometry, which makes the slab's cells those of the whole grid)
+    const int brick = slab ? 16 : pick_brick(opts);
     opts_.brick = brick;
     const int rc = occ_row_cols();
     int64_t tb = 0, pb = 0;
@@ -234,6 +239,12 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
             throw std::invalid_argument("voxelize: empty grid");
         MeshSeg s{};
         s.g = m.g;
+        if (s.g.z1 <= 0) {  // the whole grid
+            s.g.z0 = 0;
+            s.g.z1 = s.g.nz;
+        }
+        if (s.g.z0 < 0 || s.g.z0 >= s.g.z1 || s.g.z1 > s.g.nz)
+            throw std::invalid_argument("voxelize: cell layers outside the grid");
         s.tri_begin = tb;
         s.tri_end = tb + m.ntris;
         s.col_begin = ncol_;
@@ -243,7 +254,9 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
         s.brick = brick;
         s.bnx = (m.g.nx + brick - 1) / brick;
         s.bny = (m.g.ny + brick - 1) / brick;
-        s.bnz = (m.g.nz + brick - 1) / brick;
+        // along z only the bricks that overlap the slab
+        s.bzo = s.g.z0 / brick;
+        s.bnz = (s.g.z1 - 1) / brick + 1 - s.bzo;
         double sc = 0.0;
         for (int64_t i = 0; i < m.npts; ++i)
             for (int a = 0; a < 3; ++a) sc = std::max(sc, std::fabs(m.pts[3 * i + a] - m.g.corner[a]));
@@ -254,7 +267,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
         pb += m.npts;
         ncol_ += static_cast<int64_t>(m.g.nx) * m.g.ny;
         nrow_ += static_cast<int64_t>(m.g.ny) * ((m.g.nx + rc - 1) / rc);
-        nvox_ += static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
+        nvox_ += slab_cells(s.g);
         nbrick_ += static_cast<int64_t>(s.bnx) * s.bny * s.bnz;
     }
     ntris_ = tb;
@@ -297,7 +310,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
             impl_->large_cnt = carve<int>(A, 2 * nseg);
             impl_->large_off = carve<int64_t>(A, nseg + 1);
             impl_->large_list = carve<int>(A, ntris_);
-            impl_->emax_bits = carve<unsigned>(A, 2 * nseg);  // emax, scale
+            impl_->emax_bits = carve<unsigned>(A, 3 * nseg);  // emax, scale, emax_all
             impl_->bound = carve<float>(A, nbrick_);
             impl_->cand_cnt = carve<int>(A, nbrick_);
             impl_->cand_off = carve<int64_t>(A, nbrick_ + 1);
@@ -477,7 +490,7 @@ void Batch::run_impl(bool sizing) {
 
     CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
     CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
-    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 2 * nseg, st));
+    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 3 * nseg, st));
     launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tnorm, I.tlo, I.thi,
                         I.tbin, I.bincnt, I.large_cnt, I.emax_bits, st);
     exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);
@@ -588,7 +601,7 @@ RunInfo Batch::info() {
 
 void Batch::download_one(int m, HostResult& r) {
     const MeshSeg& s = segs_[static_cast<size_t>(m)];
-    const int64_t n = static_cast<int64_t>(s.g.nx) * s.g.ny * s.g.nz;
+    const int64_t n = slab_cells(s.g);
     auto get = [&](auto* dev, auto& vec) {
         if (!dev) return;
         vec.resize(static_cast<size_t>(n));
@@ -634,7 +647,8 @@ void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t s
     int64_t tris = 0, cells = 0;
     for (const HostMesh& m : meshes) {
         tris += m.ntris;
-        cells += static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
+        cells += m.g.z1 > 0 ? static_cast<int64_t>(m.g.nx) * m.g.ny * (m.g.z1 - m.g.z0)
+                            : static_cast<int64_t>(m.g.nx) * m.g.ny * m.g.nz;
     }
     const bool sdf = opts.want_sdf32 || opts.want_sdf64 || opts.want_near;
     if (!sdf) return;  // the occupancy kernels have no tunables

@@ -152,6 +152,8 @@ extern "C" cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t n
         s.g.nx = dims[0];
         s.g.ny = dims[1];
         s.g.nz = dims[2];
+        s.g.z0 = 0;  // every layer
+        s.g.z1 = dims[2];
         s.tri_begin = 0;
         s.tri_end = T;
         CMG_CUDA(cudaMemcpyAsync(segs, &s, sizeof(s), cudaMemcpyHostToDevice, st));

@@ -227,17 +227,18 @@ k_occ_filter(const MeshSeg* __restrict__ segs, int nseg, const double* __restric
     }
     __syncthreads();
     // parity bytes: lane = column, warps stride k; one warp writes 32 consecutive bytes
+    // (the layers of the slab [z0, z1) only; the column spans the whole grid)
     {
         const int c = lane, i = i0 + lane;
         const bool live = i < g.nx && !cflag[c];
         const int m = min(hcnt[c], kHCap);
         uint8_t* base = occ + s.vox_begin + static_cast<int64_t>(j) * g.nx + i;
         const int64_t kstride = static_cast<int64_t>(g.nx) * g.ny;
-        for (int k = warp; k < g.nz; k += kOccThreads / 32) {
+        for (int k = g.z0 + warp; k < g.z1; k += kOccThreads / 32) {
             if (!live) continue;
             int par = 0;
             for (int q = 0; q < m; ++q) par ^= (nbelow[c][q] > k);
-            base[k * kstride] = static_cast<uint8_t>(par);
+            base[(k - g.z0) * kstride] = static_cast<uint8_t>(par);
         }
     }
     {
@@ -324,12 +325,12 @@ k_occ_exact(const MeshSeg* __restrict__ segs, int nseg, const double* __restrict
         // parity per cell: crossings of ids < limit strictly above the cell centre
         uint8_t* base = occ + s.vox_begin + static_cast<int64_t>(j) * g.nx + i;
         const int64_t kstride = static_cast<int64_t>(g.nx) * g.ny;
-        for (int k = lane; k < g.nz; k += 32) {
+        for (int k = g.z0 + lane; k < g.z1; k += 32) {  // the slab's layers
             const double zc = cell_center(g.corner[2], k, g.h);
             int par = 0;
             for (int64_t e = e0; e < e1; ++e)
                 if (hv[e] && col_list[e] < limit && hs[e] > zc) par ^= 1;
-            base[k * kstride] = static_cast<uint8_t>(par);
+            base[(k - g.z0) * kstride] = static_cast<uint8_t>(par);
         }
     }
 }

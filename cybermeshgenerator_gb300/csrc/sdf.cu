@@ -145,6 +145,8 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         const unsigned mx = __reduce_max_sync(grp, bits);
         if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&emax_bits[nseg + si], mx);
     }
+    // the largest radius of all the mesh's triangles (the mixed path's error bounds)
+    atomicMax(&emax_bits[2 * nseg + si], __float_as_uint(ci.w));
     // degenerate (zero-area) or larger than two bricks: always considered
     const double bw = static_cast<double>(s.brick) * s.g.h;
     bool large = degenerate || sqrt(r2) > 2.0 * bw;
@@ -154,9 +156,12 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         return;
     }
     atomicMax(&emax_bits[si], __float_as_uint(ci.w));
+    // the bin of the centroid among the mesh's bricks (along z those of its slab, from
+    // brick layer bzo), clamped: a clamped triangle lies outside the bins' box, and no
+    // point inside the box is nearer its clamped position than its own
     int bx = static_cast<int>(floor((cx - K[0]) / bw));
     int by = static_cast<int>(floor((cy - K[1]) / bw));
-    int bz = static_cast<int>(floor((cz - K[2]) / bw));
+    int bz = static_cast<int>(floor((cz - K[2]) / bw)) - s.bzo;
     bx = min(max(bx, 0), s.bnx - 1);
     by = min(max(by, 0), s.bny - 1);
     bz = min(max(bz, 0), s.bnz - 1);
@@ -192,6 +197,7 @@ __global__ void k_seg_finish(MeshSeg* segs, int nseg, const int64_t* __restrict_
     segs[i].large_begin = large_off[i];
     segs[i].large_end = large_off[i + 1];
     segs[i].emax = __uint_as_float(emax_bits[i]);
+    segs[i].emax_all = __uint_as_float(emax_bits[2 * nseg + i]);
     const GridDesc& g = segs[i].g;
     const double ext = g.h * static_cast<double>(max(g.nx, max(g.ny, g.nz)));
     const double sc = fmax(static_cast<double>(__uint_as_float(emax_bits[nseg + i])), ext);
@@ -214,7 +220,7 @@ __device__ __forceinline__ BrickGeo brick_geo(const MeshSeg& s, int64_t lb) {
     const int B = s.brick;
     q.x0 = q.bx * B; q.x1 = min(q.x0 + B, s.g.nx);
     q.y0 = q.by * B; q.y1 = min(q.y0 + B, s.g.ny);
-    q.z0 = q.bz * B; q.z1 = min(q.z0 + B, s.g.nz);
+    q.z0 = (q.bz + s.bzo) * B; q.z1 = min(q.z0 + B, s.g.nz);  // bz counts from the slab's bricks
     const float h = static_cast<float>(s.g.h);
     q.cx = 0.5f * (q.x0 + q.x1) * h;
     q.cy = 0.5f * (q.y0 + q.y1) * h;
@@ -996,8 +1002,8 @@ k_count_K(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
         int x, y, z;
         M::cell(threadIdx.x, v, x, y, z);
         x += q.x0; y += q.y0; z += q.z0;
-        if (!(x < q.x1 && y < q.y1 && z < q.z1)) continue;
-        int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+        if (!(x < q.x1 && y < q.y1 && z < q.z1 && z >= g.z0 && z < g.z1)) continue;
+        int64_t idx = s.vox_begin + (static_cast<int64_t>(z - g.z0) * g.ny + y) * g.nx + x;
         float d = sdf64 ? static_cast<float>(fabs(sdf64[idx])) : fabsf(sdf32[idx]);
         float px = (x + 0.5f) * h, py = (y + 0.5f) * h, pz = (z + 0.5f) * h;
         unsigned kk = 0;

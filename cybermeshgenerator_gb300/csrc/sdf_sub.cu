@@ -79,7 +79,7 @@ __device__ __forceinline__ float cell_bound(float d2, float kap) {
 
 // Largest computed plane distance |n . (cell - a)| of a triangle that can still reach
 // the cell's FP32 minimum, for a cell bound b (cell_bound): such a triangle is within b
-// of the cell, so |cell - a| <= b + 2e (a a vertex, e the brick's largest
+// of the cell, so |cell - a| <= b + 2e (a a vertex, e the mesh's largest
 // centroid-to-vertex distance), and the FP32 plane distance errs by at most
 // nerr |cell - a| (nerr bounds the FP32 unit normal's error, TriRec::nerr) plus the
 // rounding of the recentred offsets and the dot product, all within
@@ -111,11 +111,14 @@ __device__ __forceinline__ SubGeo sub_geo(const MeshSeg& s, int64_t lb, int sub)
     const int sx = sub % per, sy = (sub / per) % per, sz = sub / (per * per);
     q.x0 = bx * s.brick + sx * kSub;
     q.y0 = by * s.brick + sy * kSub;
-    q.z0 = bz * s.brick + sz * kSub;
+    q.z0 = (bz + s.bzo) * s.brick + sz * kSub;  // bz counts from the slab's first brick
     q.x1 = min(q.x0 + kSub, s.g.nx);
     q.y1 = min(q.y0 + kSub, s.g.ny);
     q.z1 = min(q.z0 + kSub, s.g.nz);
-    q.empty = q.x0 >= s.g.nx || q.y0 >= s.g.ny || q.z0 >= s.g.nz;
+    // the sub-brick keeps the whole grid's geometry; only its cells inside the slab
+    // [z0, z1) are evaluated (none: nothing to do)
+    q.empty = q.x0 >= s.g.nx || q.y0 >= s.g.ny || q.z0 >= s.g.nz || q.z1 <= s.g.z0 ||
+              q.z0 >= s.g.z1;
     return q;
 }
 
@@ -181,7 +184,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const float r4 = __double2float_ru(sqrt(hx * hx + hy * hy + hz * hz) * (1.0 + 1e-9));
         // this thread's cell
         const int x = q.x0 + (tid & 3), y = q.y0 + ((tid >> 2) & 3), z = q.z0 + (tid >> 4);
-        const bool valid = x < q.x1 && y < q.y1 && z < q.z1;
+        const bool valid = x < q.x1 && y < q.y1 && z < q.z1 && z >= g.z0 && z < g.z1;
         const float px = static_cast<float>((x + 0.5) * g.h - ckx);
         const float py = static_cast<float>((y + 0.5) * g.h - cky);
         const float pz = static_cast<float>((z + 0.5) * g.h - ckz);
@@ -244,9 +247,9 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const float U = __uint_as_float(static_cast<unsigned>(kmin >> 32));
         const int seed = static_cast<int>(static_cast<unsigned>(kmin & 0xffffffffull));
         // mixed: the stated FP32 error of a distance near d is 48u (d + 2 e + 2 r) (e the
-        // brick's largest centroid-to-vertex distance); kap carries its constant part
-        const float kap = PREC == kPrecMixed ? __fmul_ru(98.f * kU32, brick_emax[gb] + r4) : 0.f;
-        const float ebr4 = PREC == kPrecMixed ? __fmul_ru(4.f, __fadd_ru(brick_emax[gb], r4)) : 0.f;
+        // mesh's largest centroid-to-vertex distance); kap carries its constant part
+        const float kap = PREC == kPrecMixed ? __fmul_ru(98.f * kU32, __fadd_ru(s.emax_all, r4)) : 0.f;
+        const float ebr4 = PREC == kPrecMixed ? __fmul_ru(4.f, __fadd_ru(s.emax_all, r4)) : 0.f;
         // a triangle can be nearest to a cell only if its sphere reaches U + 2 r; in the
         // mixed path, also any triangle whose FP32 distance can undercut the nearest
         // one's (two stated errors more), so the filtered list holds every triangle the
@@ -490,7 +493,10 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         int bt64 = INT_MAX, br64 = 0;
         if (PREC == kPrecMixed) {
             const float d32 = sqrtf(best);
-            eb = 48.f * kU32 * (d32 + 2.f * brick_emax[gb] + 2.f * r4) + 1e-30f;
+            // the mesh's largest triangle radius (not the brick's candidates', which
+            // depend on the candidate walk): the bound, and the band it selects, are
+            // the same whatever slab of the grid is evaluated
+            eb = 48.f * kU32 * (d32 + 2.f * s.emax_all + 2.f * r4) + 1e-30f;
             inband = valid && d32 <= band_cells * static_cast<float>(g.h) + eb;
             if (__any_sync(0xffffffffu, inband) && lane == 0) s_band = 1;
             __syncthreads();
@@ -570,7 +576,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
             }
         }
         if (valid) {
-            const int64_t idx = s.vox_begin + (static_cast<int64_t>(z) * g.ny + y) * g.nx + x;
+            const int64_t idx = s.vox_begin + (static_cast<int64_t>(z - g.z0) * g.ny + y) * g.nx + x;
             if (PREC == kPrecFP64) {
                 write_cell(o, idx, __dsqrt_rn(best64), bt, br);
             } else if (inband) {

@@ -72,3 +72,56 @@ def gather_to_rank0(obj, group: Optional[dist.ProcessGroup] = None):
     out = [None] * world if rank == 0 else None
     dist.gather_object(obj, out, dst=0, group=group)
     return out
+
+
+# ---------------------------------------------------------------- the library, sharded
+SLAB_ARRAYS = ("occupancy", "sdf32", "sdf64", "nearest_triangle", "nearest_region")
+
+
+def voxelize_slab(plc, world: int, rank: int, resolution: int = 64, pad: int = 1, grid=None, **kw):
+    """Rank `rank`'s share of ``voxelize_ex(plc, ...)``: the cell layers
+    ``z_slab(nz, world, rank)`` of the grid (from resolution/pad, or ``grid`` =
+    (corner, spacing, dims)), evaluated by the library on this rank's GPU with the
+    whole grid's geometry, so the slab equals those layers of the whole grid bit for
+    bit. Returns (VoxelResult or None for an empty share, (z0, z1))."""
+    import cybermeshgenerator_gb300 as cm
+    dims = grid[2] if grid is not None else cm.plc_grid(plc, resolution, pad)[2]
+    z0, z1 = z_slab(int(dims[2]), world, rank)
+    if z0 == z1:
+        return None, (z0, z1)
+    if grid is not None:
+        kw["grid"] = grid
+    else:
+        kw["resolution"], kw["pad"] = resolution, pad
+    return cm.voxelize_ex(plc, layers=(z0, z1), **kw), (z0, z1)
+
+
+def gather_slabs(result, group: Optional[dist.ProcessGroup] = None):
+    """Rank 0 receives the whole grid's arrays: every rank's slab arrays (those
+    present of SLAB_ARRAYS) concatenated in rank order, which for the z-major cell
+    layout is the whole grid. Other ranks receive None."""
+    import numpy as np
+    mine = {} if result is None else {n: np.asarray(getattr(result, n)) for n in SLAB_ARRAYS
+                                       if getattr(result, n) is not None}
+    parts = gather_to_rank0(mine, group)
+    if parts is None:
+        return None
+    names = [n for n in SLAB_ARRAYS if any(n in p for p in parts)]
+    return {n: np.concatenate([p[n] for p in parts if n in p]) for n in names}
+
+
+def batch_shard(plcs, resolutions, pads, world: int, rank: int, **kw):
+    """Rank `rank`'s whole meshes of a batch (assign_meshes by cell count, from each
+    mesh's grid) as one library Batch on this rank's GPU: (Batch or None, the meshes'
+    indices in the batch)."""
+    import cybermeshgenerator_gb300 as cm
+    cells = []
+    for p, r, q in zip(plcs, resolutions, pads):
+        d = cm.plc_grid(p, int(r), int(q))[2]
+        cells.append(d[0] * d[1] * d[2])
+    mine = assign_meshes(cells, world)[rank]
+    if not mine:
+        return None, mine
+    b = cm.Batch([plcs[i] for i in mine], [int(resolutions[i]) for i in mine],
+                 [int(pads[i]) for i in mine], **kw)
+    return b, mine

@@ -59,6 +59,11 @@ typedef struct cmg_voxel_opts {
     int probe;           /* mixed: brick-list head the probe scans (entries); 0 = 1024 */
     int ctas;            /* evaluation CTAs per SM the registers are budgeted for: 16, or
                             0 / 12 = 12 */
+    int z_begin, z_end;  /* cell layers [z_begin, z_end) of the grid to evaluate (a z-slab,
+                            e.g. one rank's share); z_end 0 = through the last layer. The
+                            slab's cells equal the whole grid's bit for bit (same centres,
+                            occupancy columns through the whole grid); its outputs hold
+                            those layers only. cmg_plc_voxelize_ex only. */
 } cmg_voxel_opts;
 
 /* Counters of one voxelization. */
@@ -157,6 +162,14 @@ void cmg_intersections_destroy(cmg_intersections*);
  * binning and pair tests, without the host transfers. */
 float cmg_self_intersections_last_ms(void);
 
+/* The grid cmg_plc_voxelize(plc, resolution, ., pad) lays over the PLC (the
+ * reference's make_grid, src/voxelize/voxelize.cpp:52-74): corner of cell (0,0,0)
+ * (3 doubles), cubic spacing, dims nx, ny, nz (3 ints). Host only, no GPU call; the
+ * reference's errors for resolution < 1, no points and a zero-extent PLC. No
+ * counterpart in the reference's C ABI; for choosing slabs (cmg_voxel_opts.z_begin). */
+cmg_status cmg_plc_grid(const cmg_plc* plc, int resolution, int pad, double* corner,
+                        double* spacing, int* dims, char* errbuf, size_t errbuf_len);
+
 /* Voxelizes with explicit options. Same handle and error conventions as
  * cmg_plc_voxelize; the grid holds every requested output. */
 cmg_status cmg_plc_voxelize_ex(const cmg_plc*, const cmg_voxel_opts* opts, cmg_voxels** out,
@@ -169,6 +182,11 @@ const unsigned char* cmg_voxels_nearest_region(const cmg_voxels*);
 const float* cmg_voxels_error_bound(const cmg_voxels*);
 /* Corner of cell (0,0,0) (the origin is its centre). */
 void cmg_voxels_corner(const cmg_voxels*, double* x, double* y, double* z);
+/* The layers a grid holds: [z_begin, z_end) of the grid's nz_grid layers (0, nz, nz
+ * unless cmg_voxel_opts.z_begin / z_end chose a slab). cmg_voxels_dims reports the
+ * layers held; corner and origin are the whole grid's, so layer k of a slab is layer
+ * z_begin + k of the grid. */
+void cmg_voxels_layers(const cmg_voxels*, int* z_begin, int* z_end, int* nz_grid);
 void cmg_voxels_stats(const cmg_voxels*, cmg_voxel_stats* out);
 
 /* ---- batches: many meshes, one pipeline ---------------------------------- */

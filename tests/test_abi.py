@@ -226,3 +226,40 @@ def test_large_triangle_plc_readback(lib):
     t = plc.triangles
     assert len(t) == len(tris) + 2 and np.array_equal(t[:-2], tris)
     assert t[-2:].tolist() == [[0, 1, 2], [0, 2, 3]]
+
+
+@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "brick312_r20p1", "shsphere64_r30p1"])
+def test_plc_grid_equals_reference_grid(lib, golden, name):
+    """cmg_plc_grid is the reference's make_grid (host only): corner, spacing and dims
+    of the fixture's grid, bit for bit."""
+    import cybermeshgenerator_gb300 as cm
+    g = golden(name)
+    corner, spacing, dims = cm.plc_grid(cm.PLC.from_arrays(g["points"], g["triangles"]),
+                                        int(g["resolution"]), int(g["pad"]))
+    assert np.array_equal(corner, g["corner"]) and spacing == float(g["spacing"])
+    assert dims == tuple(int(d) for d in g["dims"])
+    with pytest.raises(RuntimeError, match="resolution must be >= 1"):
+        cm.plc_grid(cm.PLC.from_arrays(g["points"], g["triangles"]), 0, 1)
+
+
+def test_layers_validation_without_gpu(lib, golden):
+    """Slab options answer their errors on the host, before any GPU call."""
+    import cybermeshgenerator_gb300 as cm
+    from cybermeshgenerator_gb300 import _lib as L
+    g = golden("cube4_r16p1")
+    plc = cm.PLC.from_arrays(g["points"], g["triangles"])
+    nz = int(g["dims"][2])
+    for layers in ((5, 3), (-1, 4), (0, nz + 1), (nz, 0)):
+        with pytest.raises(RuntimeError, match="cell layers"):
+            cm.voxelize_ex(plc, resolution=16, pad=1, layers=layers)
+    with pytest.raises(RuntimeError, match="whole meshes"):
+        cm.Batch([plc], [16], [1], layers=(0, 4))
+    o = cm.make_opts(grid=(g["corner"], g["spacing"], g["dims"]), layers=(0, 4))
+    out = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(256)
+    pts = np.ascontiguousarray(g["points"], np.float64)
+    tri = np.ascontiguousarray(g["triangles"], np.int32)
+    assert lib.cmg_sdf_plan_create(pts.ctypes.data_as(L.c_double_p), len(pts),
+                                   tri.ctypes.data_as(L.c_int_p), len(tri), ctypes.byref(o),
+                                   ctypes.byref(out), err, 256) == 3
+    assert b"whole grid" in err.value and not out.value
