@@ -560,6 +560,12 @@ cmg_status cmg_plc_grid(const cmg_plc* plc, int resolution, int pad, double* cor
     });
 }
 
+cmg_status cmg_debug_fail_device_allocs(int skip, int count) {
+    if (skip < 0 || count < 0) return CMG_ERR_INVALID_INPUT;
+    cmg::gpu::set_alloc_failures(skip, count);
+    return CMG_OK;
+}
+
 void cmg_voxels_layers(const cmg_voxels* v, int* z_begin, int* z_end, int* nz_grid) {
     if (z_begin) *z_begin = v ? v->z0 : 0;
     if (z_end) *z_end = v ? v->z1 : 0;
@@ -781,9 +787,9 @@ cmg_status cmg_sdf_plan_create(const double* points, int64_t npoints, const int*
         cudaStream_t st = gpu_stream();
         if (vo.autotune && vo.brick == 0) cmg::gpu::autotune({m}, vo, st);
         p->batch.reset(new cmg::gpu::Batch({m}, vo, st, /*transient=*/false));
-        CMG_CUDA(cudaMalloc(&p->voff, sizeof(int64_t) * voff.size()));
-        CMG_CUDA(cudaMalloc(&p->vinc, sizeof(int) * vinc.size()));
-        CMG_CUDA(cudaMalloc(&p->tmp, cmg::gpu::adjoint_tmp_bytes(p->ncell, ntriangles)));
+        CMG_CUDA(cmg::gpu::device_alloc(&p->voff, sizeof(int64_t) * voff.size()));
+        CMG_CUDA(cmg::gpu::device_alloc(&p->vinc, sizeof(int) * vinc.size()));
+        CMG_CUDA(cmg::gpu::device_alloc(&p->tmp, cmg::gpu::adjoint_tmp_bytes(p->ncell, ntriangles)));
         CMG_CUDA(cudaMemcpy(p->voff, voff.data(), sizeof(int64_t) * voff.size(), cudaMemcpyHostToDevice));
         CMG_CUDA(cudaMemcpy(p->vinc, vinc.data(), sizeof(int) * vinc.size(), cudaMemcpyHostToDevice));
         *out = p.release();

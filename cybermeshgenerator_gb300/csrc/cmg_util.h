@@ -22,6 +22,17 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
                                std::to_string(line) + ")");
 }
 #define CMG_CUDA(x) ::cmg::gpu::cuda_check((x), #x, __FILE__, __LINE__)
+
+// Every device allocation of the library goes through here. A test can make some of
+// them fail on the host (set_alloc_failures, cmg_debug_fail_device_allocs): such an
+// allocation returns cudaErrorMemoryAllocation without calling cudaMalloc.
+cudaError_t device_alloc_raw(void** p, size_t bytes);
+template <typename T>
+inline cudaError_t device_alloc(T** p, size_t bytes) {
+    return device_alloc_raw(reinterpret_cast<void**>(p), bytes);
+}
+// The next `skip` device allocations succeed, the `count` after them fail.
+void set_alloc_failures(int skip, int count);
 // Kernels launched by this library (process-wide), for launch accounting.
 void note_launch(int n = 1);
 long long launches();
@@ -53,8 +64,8 @@ public:
 
     void reserve(size_t bytes) {
         if (bytes <= cap_) return;
-        release();
-        CMG_CUDA(cudaMalloc(&base_, bytes));
+        release();  // a failed allocation leaves the arena empty (and reusable)
+        CMG_CUDA(device_alloc(&base_, bytes));
         cap_ = bytes;
     }
     void reset() { used_ = 0; }

@@ -24,6 +24,33 @@ std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
+namespace {
+std::mutex g_alloc_mu;
+int g_alloc_skip = 0, g_alloc_fail = 0;
+}  // namespace
+
+void set_alloc_failures(int skip, int count) {
+    std::lock_guard<std::mutex> lk(g_alloc_mu);
+    g_alloc_skip = skip > 0 ? skip : 0;
+    g_alloc_fail = count > 0 ? count : 0;
+}
+
+cudaError_t device_alloc_raw(void** p, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_alloc_mu);
+        if (g_alloc_fail > 0) {
+            if (g_alloc_skip > 0) {
+                --g_alloc_skip;
+            } else {
+                --g_alloc_fail;
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;  // the fake: nothing was allocated
+            }
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
 // ------------------------------------------------------------------ host block pool
 namespace {
 
@@ -560,7 +587,7 @@ WorkModel Batch::work_model() {
     w.crossings = static_cast<double>(ri.stats.crossings);
     if (!(sdf32_ || sdf64_) || !I.cand) return w;
     unsigned long long* d = nullptr;
-    CMG_CUDA(cudaMalloc(&d, 3 * sizeof(unsigned long long)));
+    CMG_CUDA(device_alloc(&d, 3 * sizeof(unsigned long long)));
     CMG_CUDA(cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), stream_));
     launch_count_K(opts_.brick, dsegs_, static_cast<int>(segs_.size()), nbrick_, I.tinfo, I.cand_off,
                    I.cand, sdf64_, sdf32_, opts_.band, d, stream_);

@@ -1097,7 +1097,7 @@ struct SizingField {
     template <typename T>
     T* alloc(size_t n) {
         void* p = nullptr;
-        CMG_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+        CMG_CUDA(device_alloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
         owned.push_back(p);
         return static_cast<T*>(p);
     }
@@ -1173,7 +1173,7 @@ SizingField* sizing_create(const double* pts, int64_t np, const int* tets, int64
     std::vector<void*> tmp;
     auto talloc = [&](size_t bytes) {
         void* p = nullptr;
-        CMG_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+        CMG_CUDA(device_alloc(&p, std::max<size_t>(bytes, 16)));
         tmp.push_back(p);
         return p;
     };

@@ -365,6 +365,14 @@ cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t npoints,
                                     int predicates, unsigned char* d_occupancy, void* stream,
                                     char* errbuf, size_t errbuf_len);
 
+/* ---- testing the error paths ------------------------------------------------ */
+/* No counterpart in the reference. After the library's next `skip` device allocations
+ * succeed, the `count` after them report cudaErrorMemoryAllocation without allocating
+ * (a host-side fake of a failed cudaMalloc); (0, 0) turns the failures off. Each call
+ * that meets one returns CMG_ERR_INTERNAL with "out of memory" in its error buffer,
+ * releases what it holds, and leaves the library usable for the next call. */
+cmg_status cmg_debug_fail_device_allocs(int skip, int count);
+
 /* Library build identification, e.g. "cmg-gb300 sm_103a". */
 const char* cmg_gpu_version(void);
 
