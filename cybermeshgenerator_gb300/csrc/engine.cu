@@ -657,7 +657,7 @@ void Batch::download(std::vector<HostResult>& out, RunInfo* info) {
 //      taken 1 or 2 per grab, or 8^3 bricks with one evaluation CTA each;
 //   2. warps per brick of the candidate walk: 1, 2, 4 (the heaviest bricks' walks set
 //      the SDF preparation time when the bricks are few);
-//   3. mixed precision, 16^3 bricks: the probe head, 512 / 1024 / 2048 entries (a
+//   3. mixed precision, 16^3 bricks: the probe head, 256 / 512 / 1024 / 2048 entries (a
 //      longer head gives a tighter bound and shorter filtered lists for more loads);
 //   4. 16^3 bricks: evaluation CTAs per SM, 12 (80 registers) or 16 (64 registers).
 // Each step keeps the fastest value and moves on; the result is cached per process by
@@ -744,7 +744,7 @@ void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t s
     if (cur.brick == 16) {
         if (opts.precision == kPrecMixed) {
             const Tuned step2 = cur;
-            for (int pr : {512, 2048}) {
+            for (int pr : {256, 512, 2048}) {
                 Tuned t = step2;
                 t.probe = pr;
                 try_set(t);

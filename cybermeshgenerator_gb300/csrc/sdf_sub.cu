@@ -47,6 +47,9 @@ struct Cap {
 // mixed path: filtered entries per need-mask chunk (one bit per entry); the records a
 // warp needs in a chunk are staged in its own shared-memory slots
 constexpr int kChunk = 32;
+// a chunk whose warp pre-test passes at least this many entries tests all of them
+// unrolled, else only those that passed
+constexpr int kDenseChunk = 20;
 constexpr int kBatch = 4;  // candidates per thread per probe/filter step (loads in flight)
 constexpr int kProbe = 1024;  // default head of the brick list the mixed probe scans
 
@@ -86,6 +89,17 @@ __device__ __forceinline__ float cell_bound(float d2, float kap) {
 // (nerr + 64u)(b + 4e + 4r) (ebr4 = 4(e + r), rounded up).
 __device__ __forceinline__ float plane_reach(float b, float nerr, float ebr4) {
     return __fmaf_ru(__fadd_ru(b, ebr4), __fadd_ru(nerr, 64.f * kU32), b);
+}
+
+// Reach of the warp pre-test: the warp's cells lie within wr of its sphere's centre
+// (wr an upper bound, rounded up), and a cell's test passes only when the cell is
+// within lim (1 + 4u) of the centroid (the test's own rounding), lim = reach(b, term) at
+// most lim_max = reach(bmax, term) for the warp's largest bound bmax (reach grows with
+// b). So the centre is within (lim_max + wr)(1 + 4u) of the centroid, and the squared
+// distance computed from the centre (relative rounding within 7u) stays below the
+// square of RU(RU(lim_max + wr)(1 + 16u)) rounded to nearest.
+__device__ __forceinline__ float warp_reach(float lim_max, float wr) {
+    return __fmul_ru(__fadd_ru(lim_max, wr), 1.f + 16.f * kU32);
 }
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only) and its wait.
@@ -147,6 +161,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
     __shared__ int s_t[kCap];
     __shared__ TriRec s_rec[STAGE ? kCap : 1];
     __shared__ TriRec s_wrec[PREC == kPrecMixed && !STAGE ? (kSubThreads / 32) * kChunk : 1];
+    __shared__ float4 s_wsph[PREC == kPrecMixed && !STAGE ? kSubThreads / 32 : 1];  // per warp
     __shared__ int s_n;
     __shared__ long long s_item;
     __shared__ unsigned long long s_red[kSubThreads / 32];
@@ -189,6 +204,28 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const float py = static_cast<float>((y + 0.5) * g.h - cky);
         const float pz = static_cast<float>((z + 0.5) * g.h - ckz);
         const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
+        if (PREC == kPrecMixed && !STAGE) {
+            // the warp's sphere for the chunk pre-test: centre at the middle of the box of
+            // its valid cells, radius an upper bound on their distances from it (none
+            // valid: radius 0, and no cell tests anything)
+            float lox = valid ? px : FLT_MAX, loy = valid ? py : FLT_MAX, loz = valid ? pz : FLT_MAX;
+            float hix = valid ? px : -FLT_MAX, hiy = valid ? py : -FLT_MAX, hiz = valid ? pz : -FLT_MAX;
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, sh));
+                loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, sh));
+                loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, sh));
+                hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, sh));
+                hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, sh));
+                hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, sh));
+            }
+            const float wcx = 0.5f * (lox + hix), wcy = 0.5f * (loy + hiy), wcz = 0.5f * (loz + hiz);
+            const float ox = px - wcx, oy = py - wcy, oz = pz - wcz;
+            const float dw = valid ? sqrtf(ox * ox + oy * oy + oz * oz) : 0.f;
+            const float wr =
+                __fmul_ru(__uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dw))), 1.f + 16.f * kU32);
+            if (lane == 0) s_wsph[warp] = make_float4(wcx, wcy, wcz, wr);
+        }
 
         // ---- 1. probe: upper bound on the distance from the centre to the surface,
         //         and the triangle that gives it (the seed of every cell below)
@@ -372,13 +409,30 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 // one-by-one test with the running bound admits, so every triangle that
                 // can be nearest is evaluated; the running minimum is of (distance,
                 // triangle id) pairs, so the extra evaluations change nothing.
+                // Before the cells' tests, lane k tests entry k of the chunk once against
+                // the warp's sphere (s_wsph) with the largest bound of its cells: the
+                // entries that fail are beyond every cell's reach and skip the cells'
+                // tests (see warp_reach).
                 TriRec* wrec = s_wrec + warp * kChunk;
                 for (int j0 = 0; j0 < n; j0 += kChunk) {
                     const int cnt = min(kChunk, n - j0);
+                    const float bmax =
+                        __uint_as_float(__reduce_max_sync(0xffffffffu, valid ? __float_as_uint(bestd) : 0u));
+                    bool pass = false;
+                    if (lane < cnt) {
+                        const float4 ws = s_wsph[warp];
+                        const float4 e = s_c[j0 + lane];
+                        const float dx = ws.x - e.x, dy = ws.y - e.y, dz = ws.z - e.z;
+                        const float lw = warp_reach(reach(bmax, e.w), ws.w);
+                        pass = dx * dx + dy * dy + dz * dz <= lw * lw;
+                    }
+                    const unsigned cand = __ballot_sync(0xffffffffu, pass);
                     unsigned mine = 0;
                     if (valid) {
                         const float bl = bestd;
-                        if (cnt == kChunk) {
+                        if (cnt == kChunk && __popc(cand) >= kDenseChunk) {
+                            // most entries passed: every entry, unrolled (the entries that
+                            // failed the warp test fail here too)
 #pragma unroll
                             for (int k = 0; k < kChunk; ++k) {
                                 const float4 e = s_c[j0 + k];
@@ -387,7 +441,8 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                                 if (dx * dx + dy * dy + dz * dz <= lim * lim) mine |= 1u << k;
                             }
                         } else {
-                            for (int k = 0; k < cnt; ++k) {
+                            for (unsigned m = cand; m; m &= m - 1u) {
+                                const int k = __ffs(m) - 1;
                                 const float4 e = s_c[j0 + k];
                                 const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
                                 const float lim = reach(bl, e.w);
