@@ -10,7 +10,8 @@
 //   k_pred_fp32   one thread per query, coordinates streamed from HBM (SoA) into
 //                 shared memory by the TMA engine (bulk copies, mbarrier pipeline;
 //                 per-thread loads for unaligned columns and the tail), the
-//                 determinant in FP32 with a rigorous bound that
+//                 queries it leaves listed per CTA with their coordinates (see
+//                 Seg), the determinant in FP32 with a rigorous bound that
 //                 covers the rounding of the inputs to FP32 and of every FP32
 //                 operation, plus the FP64 filter bound of the reference: a sign it
 //                 certifies is the exact sign and also the sign of the FP64 rounded
@@ -44,9 +45,27 @@ namespace {
 
 constexpr float kU = 5.9604645e-8f;  // 2^-24
 constexpr int kThreads = 256;
+constexpr int kTile = 256;  // queries per tile of the FP32 pass: one per thread
 
 struct Soa {
     const double* c[15];
+};
+
+// The list of the queries the FP32 pass leaves, in segments: CTA b of the pass (of
+// nseg, b = tile % nseg) appends the queries of its tiles to segment b, entries
+// [b * segcap, b * segcap + cnt[b]), counting them in shared memory, so no global
+// atomic sits between a tile's certification and the release of its stage. Entry j of
+// segment b with j < ccap also has its coordinates at cc[.][b * ccap + j], copied by
+// the FP32 pass from the tile it holds, so that the FP64 pass reads them contiguously
+// instead of gathering each from its own column at a scattered index (a whole DRAM
+// access per 8-byte value); entries at j >= ccap are gathered.
+constexpr int kMaxSeg = 2048;
+struct Seg {
+    int64_t* list;
+    unsigned long long* cnt;  // [nseg]
+    int nseg;
+    int64_t segcap, ccap;
+    double* cc[15];
 };
 
 __device__ __forceinline__ float amax3(float a, float b, float c) {
@@ -188,54 +207,59 @@ __device__ __forceinline__ void push(bool flag, int64_t i, int64_t* list,
     if (flag) list[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
-// Queries [i0, n), one thread each, coordinates loaded per thread.
-template <int NPT>
-__global__ void __launch_bounds__(kThreads) k_pred_fp32(Soa s, int64_t i0, int64_t n,
-                                                        int8_t* __restrict__ out,
-                                                        int64_t* __restrict__ list,
-                                                        unsigned long long* __restrict__ count) {
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    const int64_t n_round = i0 + ((n - i0 + 31) & ~int64_t(31));  // whole warps in the loop
-    for (int64_t i = i0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
-         i += stride) {
-        int sg = 0;
-        const bool live = i < n;
-        if (live) {
-            double v[3 * NPT];
-            load_query<NPT>(s, i, v);
-            sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
-            out[i] = static_cast<int8_t>(sg);
-        }
-        push(live && sg == 0, i, list, count);
-    }
+// Position of the lanes with `flag` in this CTA's segment (warp-aggregated on the
+// CTA's shared count); -1 without flag.
+__device__ __forceinline__ int64_t seg_pos(bool flag, unsigned long long* s_cnt) {
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    if (!m) return -1;
+    const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == lead) base = atomicAdd(s_cnt, static_cast<unsigned long long>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    return flag ? static_cast<int64_t>(base + __popc(m & ((1u << lane) - 1u))) : -1;
 }
 
-// The FP32 pass over coordinates the device reads straight from host memory (a
-// system whose GPU shares the host's page tables): each query is loaded once over
-// the host link, certified, and its coordinates stored to the device columns `dst`
-// that the FP64 and exact passes read.
-template <int NPT>
-__global__ void __launch_bounds__(kThreads) k_pred_fp32_pull(Soa src, Soa dst, int64_t n,
-                                                             int8_t* __restrict__ out,
-                                                             int64_t* __restrict__ list,
-                                                             unsigned long long* __restrict__ count) {
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    const int64_t n_round = (n + 31) & ~int64_t(31);
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_round;
-         i += stride) {
-        int sg = 0;
+// The FP32 pass with per-thread loads over tiles [t0, t1) (queries below n): CTA b of
+// the grid (gridDim.x == L.nseg) takes the tiles t with t % nseg == b and appends to
+// segment b, after what an earlier launch left there. Serves the tail tile and
+// columns the bulk copies cannot take, the rerun after a TMA wait ran out, and (PULL)
+// host memory the device reads through the host's page tables: each query is then
+// loaded once over the host link and its coordinates stored to the device columns
+// `dst` that the FP64 and exact passes read.
+template <int NPT, bool PULL>
+__global__ void __launch_bounds__(kThreads) k_pred_fp32_seg(Soa src, Soa dst, int64_t t0, int64_t t1,
+                                                            int64_t n, int8_t* __restrict__ out, Seg L) {
+    __shared__ unsigned long long s_cnt;
+    const int b = blockIdx.x, G = gridDim.x;
+    if (threadIdx.x == 0) s_cnt = L.cnt[b];
+    __syncthreads();
+    int64_t* seg = L.list + static_cast<int64_t>(b) * L.segcap;
+    for (int64_t t = t0 + ((b - t0 % G) % G + G) % G; t < t1; t += G) {
+        const int64_t i = t * kTile + threadIdx.x;
         const bool live = i < n;
+        int sg = 0;
+        double v[3 * NPT] = {};
         if (live) {
-            double v[3 * NPT];
 #pragma unroll
-            for (int k = 0; k < 3 * NPT; ++k) v[k] = src.c[k][i];
+            for (int k = 0; k < 3 * NPT; ++k) v[k] = PULL ? src.c[k][i] : __ldg(src.c[k] + i);
+            if (PULL) {
 #pragma unroll
-            for (int k = 0; k < 3 * NPT; ++k) const_cast<double*>(dst.c[k])[i] = v[k];
+                for (int k = 0; k < 3 * NPT; ++k) const_cast<double*>(dst.c[k])[i] = v[k];
+            }
             sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
             out[i] = static_cast<int8_t>(sg);
         }
-        push(live && sg == 0, i, list, count);
+        const int64_t pos = seg_pos(live && sg == 0, &s_cnt);
+        if (pos >= 0) {
+            seg[pos] = i;
+            if (pos < L.ccap) {
+#pragma unroll
+                for (int k = 0; k < 3 * NPT; ++k) L.cc[k][b * L.ccap + pos] = v[k];
+            }
+        }
     }
+    __syncthreads();
+    if (threadIdx.x == 0) L.cnt[b] = s_cnt;
 }
 
 // Bytes [0, n) of src to dst (host memory written by the device): 16-byte words
@@ -258,13 +282,13 @@ __global__ void k_put_bytes(const int8_t* __restrict__ src, int8_t* __restrict__
 // A persistent CTA streams tiles of kTile queries: per tile one bulk copy per
 // coordinate column (cp.async.bulk, global -> shared, completion counted on an
 // mbarrier), kStages tiles in flight, one thread per query computing from shared
-// memory, and one atomic per tile for the undecided list. Every wait is bounded: a
+// memory, the queries left appended to the CTA's own list segment (a shared-memory
+// count), and one barrier per tile before its stage is refilled. Every wait is bounded: a
 // wait that runs out (it never should) stops the CTA after draining its copies, and
 // sets `fault`, on which the host reruns the pass with the per-thread loads. When the
 // drain's own bounded waits run out as well, the CTA sets `drain_fault` too: copies
 // may still have been writing its shared memory, and the host reports an error
 // instead of rerunning.
-constexpr int kTile = 256;  // queries per tile: one per thread
 template <int NPT>
 struct Tma {
     static constexpr int kCols = 3 * NPT;
@@ -310,9 +334,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 
 template <int NPT>
 __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntiles,
-                                                            int8_t* __restrict__ out,
-                                                            int64_t* __restrict__ list,
-                                                            unsigned long long* __restrict__ count,
+                                                            int8_t* __restrict__ out, Seg L,
                                                             unsigned long long* __restrict__ fault,
                                                             unsigned long long* __restrict__ drain_fault) {
     using T = Tma<NPT>;
@@ -320,13 +342,14 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
     extern __shared__ __align__(128) unsigned char smem[];
     double* buf = reinterpret_cast<double*>(smem);  // [S][C][kTile]
     __shared__ __align__(8) unsigned long long bar[S];
-    __shared__ int s_wcnt[kThreads / 32];
-    __shared__ unsigned long long s_base;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t K = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    __shared__ unsigned long long s_cnt;  // entries of this CTA's segment so far
+    const int tid = threadIdx.x, b = blockIdx.x;
+    const int64_t K = ntiles > b ? (ntiles - 1 - b) / gridDim.x + 1 : 0;
+    int64_t* seg = L.list + static_cast<int64_t>(b) * L.segcap;
+    const int64_t cbase = static_cast<int64_t>(b) * L.ccap;
     auto issue = [&](int64_t k) {  // thread 0: tile k of this CTA into stage k % S
         const int st = static_cast<int>(k % S);
-        const int64_t tile = blockIdx.x + k * gridDim.x;
+        const int64_t tile = b + k * gridDim.x;
         mbar_expect_tx(&bar[st], T::kStageBytes);
 #pragma unroll
         for (int c = 0; c < C; ++c)
@@ -334,6 +357,7 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
                       kTile * 8u, &bar[st]);
     };
     if (tid == 0) {
+        s_cnt = 0;
         for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -343,8 +367,30 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
     for (int64_t k = 0; k < K; ++k) {
         const int st = static_cast<int>(k % S);
         const bool ok = mbar_wait(&bar[st], static_cast<unsigned>((k / S) & 1));
+        const int64_t i = (b + k * gridDim.x) * kTile + tid;
+        const double* sb = buf + static_cast<size_t>(st) * C * kTile;
+        int sg = 0;
+        if (ok) {
+            double v[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) v[c] = sb[c * kTile + tid];
+            sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
+            out[i] = static_cast<int8_t>(sg);
+        }
+        // a query left goes to this CTA's segment, and its coordinates, read again from
+        // the stage (still held; reading them again keeps the values out of registers
+        // across the append), to the segment's compact slots
+        const int64_t pos = seg_pos(ok && sg == 0, &s_cnt);
+        if (pos >= 0) {
+            seg[pos] = i;
+            if (pos < L.ccap) {
+                const volatile double* vb = sb;
+#pragma unroll
+                for (int c = 0; c < C; ++c) L.cc[c][cbase + pos] = vb[c * kTile + tid];
+            }
+        }
         if (__syncthreads_or(!ok)) {
-            // drain this CTA's copies still in flight (bounded), then stop
+            // a wait ran out: drain this CTA's copies still in flight (bounded), then stop
             if (tid == 0) {
                 atomicExch(fault, 1ull);
                 bool drained = true;
@@ -354,43 +400,60 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntile
             }
             return;
         }
-        const int64_t i = (blockIdx.x + k * gridDim.x) * kTile + tid;
-        const double* b = buf + static_cast<size_t>(st) * C * kTile;
-        double v[C];
-#pragma unroll
-        for (int c = 0; c < C; ++c) v[c] = b[c * kTile + tid];
-        const int sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
-        out[i] = static_cast<int8_t>(sg);
-        const unsigned m = __ballot_sync(0xffffffffu, sg == 0);
-        if (lane == 0) s_wcnt[warp] = __popc(m);
-        __syncthreads();  // the stage is consumed; the warp counts are in
-        if (tid == 0) {
-            int tot = 0;
-            for (int w = 0; w < kThreads / 32; ++w) {
-                const int c = s_wcnt[w];
-                s_wcnt[w] = tot;
-                tot += c;
-            }
-            s_base = tot ? atomicAdd(count, static_cast<unsigned long long>(tot)) : 0ull;
-            if (k + S < K) {
-                // the next copy into this stage follows the generic reads of it
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(k + S);
-            }
+        // the stage is consumed: the next copy into it follows the generic reads of it
+        if (tid == 0 && k + S < K) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k + S);
         }
-        __syncthreads();
-        if (sg == 0) list[s_base + s_wcnt[warp] + __popc(m & ((1u << lane) - 1u))] = i;
     }
+    if (tid == 0) L.cnt[b] = s_cnt;
 }
 
+// Exclusive prefix of the segment counts into pre[0..nseg] (pre[nseg] = the total), by
+// the whole CTA (kThreads threads, at most kMaxSeg segments).
+__device__ __forceinline__ void seg_prefix(const Seg& L, unsigned long long* pre) {
+    constexpr int kPer = kMaxSeg / kThreads;
+    __shared__ unsigned long long s_w[kThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned long long loc[kPer], sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const int b = tid * kPer + j;
+        loc[j] = b < L.nseg ? L.cnt[b] : 0ull;
+        sum += loc[j];
+    }
+    unsigned long long x = sum;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    unsigned long long before = x - sum;
+    for (int w = 0; w < warp; ++w) before += s_w[w];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const int b = tid * kPer + j;
+        if (b <= L.nseg) pre[b] = before;
+        before += loc[j];
+    }
+    __syncthreads();
+}
+
+// The FP64 pass over the segmented list of the FP32 pass (list position k counts
+// through the segments in order); writes the list's length to *n32.
 template <int NPT, int MODE>
-__global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __restrict__ in,
-                                                        const unsigned long long* __restrict__ nin,
+__global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, Seg L,
+                                                        unsigned long long* __restrict__ n32,
                                                         int8_t* __restrict__ out,
                                                         int64_t* __restrict__ list,
                                                         unsigned long long* __restrict__ count,
                                                         unsigned long long* __restrict__ ncert) {
-    const int64_t n = static_cast<int64_t>(*nin);
+    __shared__ unsigned long long s_pre[kMaxSeg + 1];
+    seg_prefix(L, s_pre);
+    const int64_t n = static_cast<int64_t>(s_pre[L.nseg]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n32 = static_cast<unsigned long long>(n);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     const int64_t n_round = (n + 31) & ~int64_t(31);
     for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n_round;
@@ -398,9 +461,22 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp64(Soa s, const int64_t* __
         bool undecided = false, certified = false;
         int64_t i = 0;
         if (k < n) {
-            i = in[k];
+            // the segment holding position k: the last with pre[b] <= k
+            int lo = 0, hi = L.nseg - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= static_cast<unsigned long long>(k)) lo = mid;
+                else hi = mid - 1;
+            }
+            const int64_t j = k - static_cast<int64_t>(s_pre[lo]);
+            i = L.list[static_cast<int64_t>(lo) * L.segcap + j];
             double v[3 * NPT];
-            load_query<NPT>(s, i, v);
+            if (j < L.ccap) {
+#pragma unroll
+                for (int c = 0; c < 3 * NPT; ++c) v[c] = L.cc[c][static_cast<int64_t>(lo) * L.ccap + j];
+            } else {
+                load_query<NPT>(s, i, v);
+            }
             const d3 a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]}, d{v[9], v[10], v[11]};
             // integer coordinates first (integer pipe): in EXACT mode their sign decides;
             // in COMPAT mode too when the FP64 evaluation is provably exact there (it then
@@ -523,7 +599,24 @@ struct Counters {
     unsigned long long certified;  // decided in the FP64 pass by an exact evaluation
     unsigned long long fault;      // a TMA wait of the FP32 pass ran out
     unsigned long long drain_fault;  // ... and so did the drain of the copies in flight
+    unsigned long long seg[kMaxSeg];  // entries per segment of the FP32 pass's list
 };
+
+// The segmented list for streams (or chunks) of at most nmax queries: at most `per_sm`
+// segments (CTAs of the FP32 pass) per SM, at most one per tile; each segment holds
+// every query of its tiles, and compact slots for a quarter of them (uniform queries
+// leave about a tenth to the FP64 pass; beyond the slots it gathers by index).
+Seg take_seg(Arena& a, int64_t nmax, int ncol, int sms, int per_sm) {
+    const int64_t tiles = std::max<int64_t>(1, (nmax + kTile - 1) / kTile);
+    Seg L{};
+    L.nseg = static_cast<int>(std::min<int64_t>({tiles, static_cast<int64_t>(per_sm) * sms,
+                                                  static_cast<int64_t>(kMaxSeg - 1)}));
+    L.segcap = (tiles + L.nseg - 1) / L.nseg * kTile;
+    L.ccap = std::min<int64_t>(L.segcap, L.segcap / 4 + 64);
+    L.list = a.take<int64_t>(L.nseg * L.segcap);
+    for (int k = 0; k < ncol; ++k) L.cc[k] = a.take<double>(L.nseg * L.ccap);
+    return L;
+}
 
 // Queries per chunk of a host-resident stream (two buffer sets of up to 15 columns:
 // at most 1 GB of device memory).
@@ -534,20 +627,22 @@ constexpr int64_t kPullChunk = int64_t{1} << 24;
 
 }  // namespace
 
-// The FP64 pass over the queries the FP32 pass left, then the exact pass.
-static void pred_stream_finish(int npt, const Soa& s, int mode, int8_t* d_out, int64_t* list_a,
+// The FP64 pass over the queries the FP32 pass left in the segments of L (their counts
+// in c->seg), then the exact pass.
+static void pred_stream_finish(int npt, const Soa& s, int mode, int8_t* d_out, Seg L,
                                int64_t* list_b, Counters* c, cudaStream_t st, int sms) {
+    L.cnt = c->seg;
     if (npt == 4 && mode == kPredExact)
-        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+        k_pred_fp64<4, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, L, &c->n32, d_out, list_b, &c->n64,
                                                                       &c->certified);
     else if (npt == 4)
-        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+        k_pred_fp64<4, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, L, &c->n32, d_out, list_b, &c->n64,
                                                                       &c->certified);
     else if (mode == kPredExact)
-        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+        k_pred_fp64<5, kPredExact><<<2 * sms, kThreads, 0, st>>>(s, L, &c->n32, d_out, list_b, &c->n64,
                                                                       &c->certified);
     else
-        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, list_a, &c->n32, d_out, list_b, &c->n64,
+        k_pred_fp64<5, kPredCompat><<<2 * sms, kThreads, 0, st>>>(s, L, &c->n32, d_out, list_b, &c->n64,
                                                                       &c->certified);
     CMG_LAUNCH();
     if (npt == 4) k_pred_exact<4><<<2 * sms, 128, 0, st>>>(s, list_b, &c->n64, d_out, &c->overflow);
@@ -555,45 +650,50 @@ static void pred_stream_finish(int npt, const Soa& s, int mode, int8_t* d_out, i
     CMG_LAUNCH();
 }
 
-// Runs the three passes on device-resident SoA coordinates. Returns the number of
-// times the FP32 pass was rerun with per-thread loads after a TMA wait ran out (0 or
-// 1); throws when copies may have outlived their CTA.
+// The FP32 pass with per-thread loads over tiles [t0, t1) into the segments of L.
+static void pred_fp32_loads(int npt, const Soa& s, int64_t t0, int64_t t1, int64_t n, int8_t* d_out,
+                            const Seg& L, cudaStream_t st) {
+    if (npt == 4) k_pred_fp32_seg<4, false><<<L.nseg, kThreads, 0, st>>>(s, s, t0, t1, n, d_out, L);
+    else k_pred_fp32_seg<5, false><<<L.nseg, kThreads, 0, st>>>(s, s, t0, t1, n, d_out, L);
+    CMG_LAUNCH();
+}
+
+// Runs the three passes on device-resident SoA coordinates, the FP32 pass's list in
+// the segments of L (shaped for at least n queries). Returns the number of times the
+// FP32 pass was rerun with per-thread loads after a TMA wait ran out (0 or 1); throws
+// when copies may have outlived their CTA.
 int pred_stream_device(int npt, const double* const* coords, int64_t n, int mode, int8_t* d_out,
-                        int64_t* list_a, int64_t* list_b, void* counters, cudaStream_t st,
-                        int sms, cudaEvent_t* fp32_events) {
+                        Seg L, int64_t* list_b, void* counters, cudaStream_t st, int sms,
+                        cudaEvent_t* fp32_events) {
     Soa s{};
     for (int k = 0; k < 3 * npt; ++k) s.c[k] = coords[k];
     Counters* c = static_cast<Counters*>(counters);
+    L.cnt = c->seg;
+    const int64_t T = (n + kTile - 1) / kTile;
+    if ((T + L.nseg - 1) / L.nseg > L.segcap / kTile)
+        throw std::logic_error("predicate stream: list segments too small for the stream");
     CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
-    const int grid = 8 * sms;
     // the TMA pass takes the whole tiles when every column starts on a 16-byte boundary
     // (the bulk copies' rule); the rest, and unaligned columns, take the per-thread loads
     bool aligned = true;
     for (int k = 0; k < 3 * npt; ++k) aligned = aligned && (reinterpret_cast<uintptr_t>(coords[k]) % 16 == 0);
     const int64_t ntiles = aligned ? n / kTile : 0;
-    const int64_t i0 = ntiles * kTile;
     if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[0], st));
     if (ntiles > 0) {
         if (npt == 4) {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<4>::kSmem)));
-            k_pred_fp32_tma<4><<<2 * sms, kThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, list_a,
-                                                                         &c->n32, &c->fault,
-                                                                         &c->drain_fault);
+            k_pred_fp32_tma<4><<<L.nseg, kThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
+                                                                        &c->drain_fault);
         } else {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<5>::kSmem)));
-            k_pred_fp32_tma<5><<<2 * sms, kThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, list_a,
-                                                                         &c->n32, &c->fault,
-                                                                         &c->drain_fault);
+            k_pred_fp32_tma<5><<<L.nseg, kThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
+                                                                        &c->drain_fault);
         }
         CMG_LAUNCH();
     }
-    if (i0 < n) {
-        if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, i0, n, d_out, list_a, &c->n32);
-        else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, i0, n, d_out, list_a, &c->n32);
-        CMG_LAUNCH();
-    }
+    if (ntiles < T) pred_fp32_loads(npt, s, ntiles, T, n, d_out, L, st);
     if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[1], st));
     int reruns = 0;
     if (ntiles > 0) {
@@ -607,13 +707,11 @@ int pred_stream_device(int npt, const double* const* coords, int64_t n, int mode
                 "predicate stream: a bulk copy of the FP32 pass did not complete within its wait");
         if (fault[0]) {
             CMG_CUDA(cudaMemsetAsync(c, 0, sizeof(Counters), st));
-            if (npt == 4) k_pred_fp32<4><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
-            else k_pred_fp32<5><<<grid, kThreads, 0, st>>>(s, 0, n, d_out, list_a, &c->n32);
-            CMG_LAUNCH();
+            pred_fp32_loads(npt, s, 0, T, n, d_out, L, st);
             reruns = 1;
         }
     }
-    pred_stream_finish(npt, s, mode, d_out, list_a, list_b, c, st, sms);
+    pred_stream_finish(npt, s, mode, d_out, L, list_b, c, st, sms);
     return reruns;
 }
 
@@ -667,12 +765,9 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const int sms = device_sms();
         const bool host = where == CMG_MEM_HOST;
-        auto plan = [&](Arena& a, const double** dc, int8_t** dout, int64_t** la, int64_t** lb,
-                        void** cnt) {
+        auto plan = [&](Arena& a, Seg* la, int64_t** lb, void** cnt) {
             a.reset();
-            for (int k = 0; k < 3 * npt; ++k) dc[k] = host ? a.take<double>(n) : coords[k];
-            *dout = host ? a.take<int8_t>(n) : reinterpret_cast<int8_t*>(out);
-            *la = a.take<int64_t>(n);
+            *la = take_seg(a, n, 3 * npt, sms, 2);
             *lb = a.take<int64_t>(n);
             *cnt = a.take<Counters>(1);
         };
@@ -682,18 +777,17 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
         Counters hc{};
         int reruns = 0;
         if (!host) {
-            const double* dc[15];
-            int8_t* dout;
-            int64_t *la, *lb;
+            Seg la;
+            int64_t* lb;
             void* cnt;
             w.arena.clear_need();
-            plan(w.arena, dc, &dout, &la, &lb, &cnt);
+            plan(w.arena, &la, &lb, &cnt);
             if (w.arena.overflowed()) {
                 w.arena.reserve(w.arena.need());
-                plan(w.arena, dc, &dout, &la, &lb, &cnt);
+                plan(w.arena, &la, &lb, &cnt);
             }
-            reruns += pred_stream_device(npt, dc, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, dout,
-                               la, lb, cnt, st, sms, w.ev);
+            reruns += pred_stream_device(npt, coords, n, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat,
+                                         reinterpret_cast<int8_t*>(out), la, lb, cnt, st, sms, w.ev);
             CMG_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
             CMG_CUDA(cudaStreamSynchronize(st));
             if (stats) CMG_CUDA(cudaEventElapsedTime(&stats->fp32_pass_ms, w.ev[0], w.ev[1]));
@@ -706,13 +800,14 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             const int64_t nch = (n + chunk - 1) / chunk;
             double* col[15];
             int8_t* sg;
-            int64_t *la, *lb;
+            Seg la;
+            int64_t* lb;
             Counters* cnt;
             auto plan_pull = [&](Arena& a) {
                 a.reset();
                 for (int k = 0; k < ncol; ++k) col[k] = a.take<double>(chunk);
                 sg = a.take<int8_t>(chunk);
-                la = a.take<int64_t>(chunk);
+                la = take_seg(a, chunk, ncol, sms, 8);
                 lb = a.take<int64_t>(chunk);
                 cnt = a.take<Counters>(nch);
             };
@@ -736,10 +831,13 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
                     dst.c[k] = col[k];
                 }
                 CMG_CUDA(cudaEventRecord(w.chunk_ev[2 * c], st));
+                Seg lc = la;
+                lc.cnt = cnt[c].seg;
+                const int64_t T = (m + kTile - 1) / kTile;
                 if (npt == 4)
-                    k_pred_fp32_pull<4><<<8 * sms, kThreads, 0, st>>>(src, dst, m, sg, la, &cnt[c].n32);
+                    k_pred_fp32_seg<4, true><<<lc.nseg, kThreads, 0, st>>>(src, dst, 0, T, m, sg, lc);
                 else
-                    k_pred_fp32_pull<5><<<8 * sms, kThreads, 0, st>>>(src, dst, m, sg, la, &cnt[c].n32);
+                    k_pred_fp32_seg<5, true><<<lc.nseg, kThreads, 0, st>>>(src, dst, 0, T, m, sg, lc);
                 CMG_LAUNCH();
                 CMG_CUDA(cudaEventRecord(w.chunk_ev[2 * c + 1], st));
                 pred_stream_finish(npt, dst, mode == CMG_PRED_EXACT ? kPredExact : kPredCompat, sg, la,
@@ -769,7 +867,8 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
             const int64_t nch = (n + chunk - 1) / chunk;
             double* col[2][15];
             int8_t* sg[2];
-            int64_t *la, *lb;
+            Seg la;
+            int64_t* lb;
             Counters* cnt;
             auto plan_host = [&](Arena& a) {
                 a.reset();
@@ -777,7 +876,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
                     for (int k = 0; k < ncol; ++k) col[b][k] = a.take<double>(chunk);
                     sg[b] = a.take<int8_t>(chunk);
                 }
-                la = a.take<int64_t>(chunk);
+                la = take_seg(a, chunk, ncol, sms, 2);
                 lb = a.take<int64_t>(chunk);
                 cnt = a.take<Counters>(nch);
             };
@@ -884,22 +983,24 @@ cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int 
         std::lock_guard<std::mutex> lk(w.mu);
         cudaStream_t st = nullptr;
         const int64_t N = n;
+        const int sms = device_sms();
         auto plan = [&](Arena& a, double** dx, int** dt, double** soa, int8_t** d8, int** dsg,
-                        int64_t** la, int64_t** lb, void** cnt) {
+                        Seg* la, int64_t** lb, void** cnt) {
             a.reset();
             *dx = a.take<double>(3 * static_cast<size_t>(npts));
             *dt = a.take<int>(4 * N);
             *soa = a.take<double>(12 * N);
             *d8 = a.take<int8_t>(N);
             *dsg = a.take<int>(N);
-            *la = a.take<int64_t>(N);
+            *la = take_seg(a, N, 12, sms, 2);
             *lb = a.take<int64_t>(N);
             *cnt = a.take<Counters>(1);
         };
         double *dx, *soa;
         int *dt, *dsg;
         int8_t* d8;
-        int64_t *la, *lb;
+        Seg la;
+        int64_t* lb;
         void* cnt;
         w.arena.clear_need();
         plan(w.arena, &dx, &dt, &soa, &d8, &dsg, &la, &lb, &cnt);
@@ -913,7 +1014,7 @@ cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int 
         CMG_LAUNCH();
         const double* cols[12];
         for (int k = 0; k < 12; ++k) cols[k] = soa + k * N;
-        pred_stream_device(4, cols, N, kPredCompat, d8, la, lb, cnt, st, device_sms(), nullptr);
+        pred_stream_device(4, cols, N, kPredCompat, d8, la, lb, cnt, st, sms, nullptr);
         k_widen<<<static_cast<unsigned>((N + 255) / 256), 256, 0, st>>>(d8, N, dsg);
         CMG_LAUNCH();
         CMG_CUDA(cudaMemcpyAsync(out_sign, dsg, sizeof(int) * N, cudaMemcpyDeviceToHost, st));

@@ -36,6 +36,24 @@ def test_stream_matches_oracle_large(cm, orc, kind):
         assert st["exact_queries"] - st["expansion_queries"] >= int(0.09 * S.shape[1])
 
 
+@pytest.mark.parametrize("kind", ["orient3d", "insphere"])
+def test_stream_left_queries_beyond_compact_slots(cm, orc, kind):
+    """The FP32 pass stores the coordinates of the queries it leaves at their list
+    positions, up to a quarter of the stream (+256); the FP64 pass reads those and
+    gathers the rest by index. With 60 % exactly degenerate and 20 % near queries both
+    kinds of entries occur; signs equal the oracle's in both modes."""
+    import oracle as O
+    from cybermeshgenerator_gb300 import workloads as W
+    n = 120_000
+    S = W.predicate_stream(n, kind, degenerate=0.6, near=0.2, seed=34)
+    fn = cm.orient3d_stream if kind == "orient3d" else cm.insphere_stream
+    for mode in (cm.PRED_COMPAT, cm.PRED_EXACT):
+        got, st = fn(S, mode)
+        assert st["fp64_queries"] > n // 4 + 256
+        want = orc.stream(kind, S, O.COMPAT if mode == cm.PRED_COMPAT else O.EXACT)
+        assert np.array_equal(got, want)
+
+
 def test_stream_device_memory(cm):
     torch = pytest.importorskip("torch")
     from cybermeshgenerator_gb300 import workloads as W
