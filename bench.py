@@ -224,17 +224,20 @@ def traffic_from_profile():
 
 def stream_traffic_per_query():
     """DRAM bytes per query of the FP32 stream passes (orient3d, insphere) from the
-    committed ncu summary."""
+    committed ncu summary, when that capture was of the current predicates.cu."""
     path = os.path.join(ROOT, "profiles", "k_pred_fp32_tma_stream2e7.md")
+    q, sha = None, None
     try:
         with open(path) as f:
             for line in f:
                 if line.startswith("dram_bytes_per_query:"):
                     w = line.split(":", 1)[1].split()
-                    return float(w[w.index("orient3d") + 1]), float(w[w.index("insphere") + 1])
+                    q = float(w[w.index("orient3d") + 1]), float(w[w.index("insphere") + 1])
+                elif line.startswith("kernel_source_sha:"):
+                    sha = line.split(":", 1)[1].split()[0]
     except (OSError, ValueError, IndexError):
-        pass
-    return None
+        return None
+    return q if sha == kernel_source_sha(("predicates.cu",)) else None
 
 
 def cpu_baseline(pts, tris, dims_grid, seconds=12.0, threads=None, probe=2000):

@@ -227,19 +227,21 @@ __device__ __forceinline__ int64_t seg_pos(bool flag, unsigned long long* s_cnt)
 // loaded once over the host link and its coordinates stored to the device columns
 // `dst` that the FP64 and exact passes read.
 template <int NPT, bool PULL>
-__global__ void __launch_bounds__(kThreads) k_pred_fp32_seg(Soa src, Soa dst, int64_t t0, int64_t t1,
-                                                            int64_t n, int8_t* __restrict__ out, Seg L) {
+__global__ void __launch_bounds__(kThreads, 4) k_pred_fp32_seg(Soa src, Soa dst, int64_t t0, int64_t t1,
+                                                               int64_t n, int8_t* __restrict__ out, Seg L) {
     __shared__ unsigned long long s_cnt;
     const int b = blockIdx.x, G = gridDim.x;
     if (threadIdx.x == 0) s_cnt = L.cnt[b];
     __syncthreads();
     int64_t* seg = L.list + static_cast<int64_t>(b) * L.segcap;
+    // the device copy of the coordinates (PULL: the columns written here)
+    const Soa& dev = PULL ? dst : src;
     for (int64_t t = t0 + ((b - t0 % G) % G + G) % G; t < t1; t += G) {
         const int64_t i = t * kTile + threadIdx.x;
         const bool live = i < n;
         int sg = 0;
-        double v[3 * NPT] = {};
         if (live) {
+            double v[3 * NPT];
 #pragma unroll
             for (int k = 0; k < 3 * NPT; ++k) v[k] = PULL ? src.c[k][i] : __ldg(src.c[k] + i);
             if (PULL) {
@@ -253,8 +255,10 @@ __global__ void __launch_bounds__(kThreads) k_pred_fp32_seg(Soa src, Soa dst, in
         if (pos >= 0) {
             seg[pos] = i;
             if (pos < L.ccap) {
+                // read again from device memory (this thread's own loads or stores, in
+                // L1 / L2), which keeps the values out of registers across the append
 #pragma unroll
-                for (int k = 0; k < 3 * NPT; ++k) L.cc[k][b * L.ccap + pos] = v[k];
+                for (int k = 0; k < 3 * NPT; ++k) L.cc[k][b * L.ccap + pos] = dev.c[k][i];
             }
         }
     }
@@ -807,7 +811,7 @@ cmg_status run_stream(int npt, const double* const* coords, int64_t n, int mode,
                 a.reset();
                 for (int k = 0; k < ncol; ++k) col[k] = a.take<double>(chunk);
                 sg = a.take<int8_t>(chunk);
-                la = take_seg(a, chunk, ncol, sms, 8);
+                la = take_seg(a, chunk, ncol, sms, 4);  // 4 resident CTAs per SM
                 lb = a.take<int64_t>(chunk);
                 cnt = a.take<Counters>(nch);
             };
