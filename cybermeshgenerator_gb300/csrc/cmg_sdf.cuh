@@ -76,65 +76,91 @@ __device__ __forceinline__ void load_soup(const double* __restrict__ soup, int64
 }
 
 // ------------------------------------------------------------------ FP32 record
-// Translation-invariant FP32 data of a triangle, computed once from FP64: vertex
-// offsets from the centroid, edges (v1-v0, v2-v1, v0-v2), unit normal, in-plane
-// inward edge normals (n x e_k), 1/|e_k|^2 (0 for a degenerate edge), a flag
-// that allows the plane branch (nonzero area), and a bound on the distance of the
-// FP32 unit normal from the exact one (0 for a degenerate triangle).
+// Translation-invariant FP32 data of a triangle (a, b, c), computed once from FP64, in
+// the triangle's own orthonormal frame (u, v, n): u along b - a, v in the triangle's
+// plane toward c, n = u x v. In that frame a = (0, 0), b = (bx, 0), c = (cx, cy) with
+// cy >= 0, the triangle lies in the plane n = 0, and a point's squared distance is its
+// squared in-plane distance to the 2-D triangle plus its squared n component. The frame
+// is built by two Gram-Schmidt passes, so b and c lie in it to FP64 rounding even for
+// slivers and collinear or repeated vertices (then v is any unit vector across u).
 struct alignas(16) TriRec {
-    float o0[3], o1[3], o2[3];
-    float e0[3], e1[3], e2[3];
-    float nn[3];
-    float m0[3], m1[3], m2[3];
-    float inv[3];
-    float ok;
-    float nerr;
-    float pad_;
+    float o0[3];       // a - centroid
+    float nn[3];       // n
+    float nerr;        // bound on |n (FP32) - n| (the plane test's normal error)
+    float uu[3];       // u
+    float vv[3];       // v
+    float bx;          // |b - a|
+    float cx, cy;      // c - a in the frame
+    float e1x;         // (c - b) . u
+    float ib;          // 1 / bx (0 if a == b)
+    float inv1, inv2;  // 1 / |c - b|^2, 1 / |c - a|^2 (0 for a zero edge)
+    float ok;          // 1: the face branch is allowed (bx > 0 and cy > 0)
+    float pad_[3];
 };
-static_assert(sizeof(TriRec) == 144, "record layout");
+static_assert(sizeof(TriRec) == 96, "record layout");
+constexpr int kRecVec = static_cast<int>(sizeof(TriRec) / 16);  // float4 words per record
 
 __device__ __forceinline__ void load_rec(const TriRec* __restrict__ recs, int t, TriRec& r) {
     const float4* s = reinterpret_cast<const float4*>(recs + t);
     float4* d = reinterpret_cast<float4*>(&r);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) d[i] = __ldg(s + i);
+    for (int i = 0; i < kRecVec; ++i) d[i] = __ldg(s + i);
 }
 
-// Squared FP32 distance from a point to the triangle, given (dx,dy,dz) = point -
-// centroid; region numbered as the FP64 Ericson regions. A point that projects inside
-// a non-degenerate triangle (every in-plane edge function >= 0) is at its plane
-// distance; otherwise its nearest point lies on the boundary, and the distance is the
-// smallest of the three segment distances (the segment of a satisfied edge is never
-// nearer than the triangle, so the minimum is the boundary distance up to rounding,
-// within the same bound as each segment distance). Every lane measures all three
-// segments: no branch splits a warp whose cells lie in different regions.
-// Explicit intrinsics fix the operation sequence, so the value does not depend on
-// whether the region is wanted (REG) or on the inlining context.
 __device__ __forceinline__ float dot3f(float ax, float ay, float az, const float* b) {
     return fmaf(ax, b[0], fmaf(ay, b[1], __fmul_rn(az, b[2])));
 }
 
-__device__ __forceinline__ void seg2(float px, float py, float pz, const float* e, float inv,
-                                     float& d, float& t) {
-    t = __saturatef(__fmul_rn(dot3f(px, py, pz, e), inv));
-    const float qx = fmaf(-t, e[0], px), qy = fmaf(-t, e[1], py), qz = fmaf(-t, e[2], pz);
-    d = fmaf(qx, qx, fmaf(qy, qy, __fmul_rn(qz, qz)));
+// The point's offset from a, pa = (point - centroid) - (a - centroid), and its n
+// component: the first steps of the distance, shared with the plane test.
+struct PaN {
+    float x, y, z, n;
+};
+__device__ __forceinline__ PaN pa_n(const TriRec& r, float dx, float dy, float dz) {
+    PaN p;
+    p.x = __fsub_rn(dx, r.o0[0]);
+    p.y = __fsub_rn(dy, r.o0[1]);
+    p.z = __fsub_rn(dz, r.o0[2]);
+    p.n = dot3f(p.x, p.y, p.z, r.nn);
+    return p;
 }
 
+// Squared FP32 distance from a point to the triangle, from pa_n; region numbered as the
+// FP64 Ericson regions (0 a, 1 b, 2 ab, 3 c, 4 ac, 5 bc, 6 face). In the frame the
+// point is (pu, pv, pn); it projects inside when the three 2-D edge functions
+// (pv, (c - b) x (p - b), (a - c) x (p - c)) are >= 0 and the triangle has area, and
+// is then at |pn|; otherwise its nearest point is on the boundary, at the smallest of
+// the three 2-D segment distances (each with pn^2 added once at the end). Every lane
+// measures all three segments: no branch splits a warp whose cells lie in different
+// regions. Explicit intrinsics fix the operation sequence, so the value does not depend
+// on whether the region is wanted (REG) or on the inlining context.
+// Error (u = 2^-24, d the distance, e the largest centroid-to-vertex distance, r the
+// sub-brick radius): pa errs by at most u (3 r + 4 d + 6 e) (the recentring, as
+// before), |pa| <= d + 2 e; the frame rounded to FP32 and the three dots move the
+// point by at most 7 u |pa|, the FP32 2-D vertices the triangle by 3 u e; the segment
+// parameter, the residual and the sums add at most 7 u (d + 2 e), a face decision on
+// the wrong side of an edge 4 u (d + 2 e): together below u (22 d + 39 e + 3 r), well
+// inside the stated 48 u (d + 2 e + 2 r).
 template <bool REG>
-__device__ __forceinline__ float dist_rec_t(const TriRec& r, float dx, float dy, float dz, int* reg) {
-    const float pax = __fsub_rn(dx, r.o0[0]), pay = __fsub_rn(dy, r.o0[1]), paz = __fsub_rn(dz, r.o0[2]);
-    const float pbx = __fsub_rn(dx, r.o1[0]), pby = __fsub_rn(dy, r.o1[1]), pbz = __fsub_rn(dz, r.o1[2]);
-    const float pcx = __fsub_rn(dx, r.o2[0]), pcy = __fsub_rn(dy, r.o2[1]), pcz = __fsub_rn(dz, r.o2[2]);
-    const float s0 = dot3f(pax, pay, paz, r.m0);
-    const float s1 = dot3f(pbx, pby, pbz, r.m1);
-    const float s2 = dot3f(pcx, pcy, pcz, r.m2);
-    const float dp = dot3f(pax, pay, paz, r.nn);
-    float d0, t0, d1, t1, d2, t2;
-    seg2(pax, pay, paz, r.e0, r.inv[0], d0, t0);
-    seg2(pbx, pby, pbz, r.e1, r.inv[1], d1, t1);
-    seg2(pcx, pcy, pcz, r.e2, r.inv[2], d2, t2);
-    const bool face = r.ok > 0.f && s0 >= 0.f && s1 >= 0.f && s2 >= 0.f;
+__device__ __forceinline__ float dist_rec_t(const TriRec& r, const PaN& p, int* reg) {
+    const float pu = dot3f(p.x, p.y, p.z, r.uu), pv = dot3f(p.x, p.y, p.z, r.vv);
+    const float qu1 = __fsub_rn(pu, r.bx);
+    const float qu2 = __fsub_rn(pu, r.cx), qv2 = __fsub_rn(pv, r.cy);
+    const float s1 = fmaf(r.e1x, pv, -__fmul_rn(r.cy, qu1));
+    const float s2 = fmaf(r.cy, qu2, -__fmul_rn(r.cx, qv2));
+    // a -> b along u
+    const float t0 = __saturatef(__fmul_rn(pu, r.ib));
+    const float r0u = fmaf(-t0, r.bx, pu);
+    const float d0 = fmaf(r0u, r0u, __fmul_rn(pv, pv));
+    // b -> c, direction (e1x, cy)
+    const float t1 = __saturatef(__fmul_rn(fmaf(qu1, r.e1x, __fmul_rn(pv, r.cy)), r.inv1));
+    const float r1u = fmaf(-t1, r.e1x, qu1), r1v = fmaf(-t1, r.cy, pv);
+    const float d1 = fmaf(r1u, r1u, __fmul_rn(r1v, r1v));
+    // c -> a, direction (-cx, -cy)
+    const float t2 = __saturatef(__fmul_rn(-fmaf(qu2, r.cx, __fmul_rn(qv2, r.cy)), r.inv2));
+    const float r2u = fmaf(t2, r.cx, qu2), r2v = fmaf(t2, r.cy, qv2);
+    const float d2 = fmaf(r2u, r2u, __fmul_rn(r2v, r2v));
+    const bool face = r.ok > 0.f && pv >= 0.f && s1 >= 0.f && s2 >= 0.f;
     float d = d0;
     int g = 0;
     if (REG) g = t0 <= 0.f ? 0 : (t0 >= 1.f ? 1 : 2);
@@ -147,20 +173,20 @@ __device__ __forceinline__ float dist_rec_t(const TriRec& r, float dx, float dy,
         if (REG) g = t2 <= 0.f ? 3 : (t2 >= 1.f ? 0 : 4);
     }
     if (face) {
-        d = __fmul_rn(dp, dp);
+        d = 0.f;
         g = 6;
     }
     if (REG) *reg = g;
-    return d;
+    return fmaf(p.n, p.n, d);
 }
 
 // The distance and its region.
 __device__ __forceinline__ float dist_rec(const TriRec& r, float dx, float dy, float dz, int* reg) {
-    return dist_rec_t<true>(r, dx, dy, dz, reg);
+    return dist_rec_t<true>(r, pa_n(r, dx, dy, dz), reg);
 }
 // The distance alone (the same value as dist_rec).
 __device__ __forceinline__ float dist_rec_val(const TriRec& r, float dx, float dy, float dz) {
-    return dist_rec_t<false>(r, dx, dy, dz, nullptr);
+    return dist_rec_t<false>(r, pa_n(r, dx, dy, dz), nullptr);
 }
 
 // ------------------------------------------------------------------ outputs

@@ -327,7 +327,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
             impl_->tinfo = carve<float4>(A, ntris_);
             impl_->tinfo_lo = carve<float4>(A, ntris_);
             impl_->tnorm = carve<float4>(A, ntris_);
-            impl_->trec = carve<char>(A, 144 * static_cast<size_t>(ntris_));
+            impl_->trec = carve<char>(A, kTriRecBytes * static_cast<size_t>(ntris_));
             impl_->tlo = carve<float4>(A, ntris_);
             impl_->thi = carve<float4>(A, ntris_);
             impl_->tbin = carve<int64_t>(A, ntris_);

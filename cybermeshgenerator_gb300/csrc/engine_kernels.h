@@ -31,7 +31,9 @@ void launch_occ_exact(int mode, const MeshSeg* segs, int nseg, const double* sou
 int occ_row_cols();
 
 // sdf.cu
-// trec: one 144-byte translation-invariant FP32 record per triangle (sdf::TriRec).
+// trec: one kTriRecBytes-byte translation-invariant FP32 record per triangle (sdf::TriRec,
+// the triangle in its own frame).
+constexpr size_t kTriRecBytes = 96;
 void launch_sdf_tri_prep(const MeshSeg* segs, int nseg, int64_t ntris, const double* soup,
                          float4* tinfo, float4* tinfo_lo, void* trec, float4* tnorm, float4* tlo,
                          float4* thi,

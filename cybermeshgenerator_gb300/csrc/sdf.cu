@@ -42,6 +42,7 @@ namespace cmg::gpu {
 namespace {
 
 using namespace sdf;
+static_assert(sizeof(TriRec) == kTriRecBytes, "the workspace carves kTriRecBytes per record");
 
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
 
@@ -94,44 +95,65 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
     double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
     bool degenerate = !(nx * nx + ny * ny + nz * nz > 0.0);
     {
-        TriRec r;
-        const double E[3][3] = {{b.x - a.x, b.y - a.y, b.z - a.z},
-                                {c.x - b.x, c.y - b.y, c.z - b.z},
-                                {a.x - c.x, a.y - c.y, a.z - c.z}};
         double nl = sqrt(nx * nx + ny * ny + nz * nz);
         double n3[3] = {0.0, 0.0, 0.0};
         if (nl > 0.0) { n3[0] = nx / nl; n3[1] = ny / nl; n3[2] = nz / nl; }
-        float* O[3] = {r.o0, r.o1, r.o2};
-        float* Ef[3] = {r.e0, r.e1, r.e2};
-        float* Mf[3] = {r.m0, r.m1, r.m2};
-        const double C[3] = {cx, cy, cz};
-        for (int k = 0; k < 3; ++k) {
-            const double Vk[3] = {V[k].x, V[k].y, V[k].z};
-            for (int q = 0; q < 3; ++q) {
-                O[k][q] = static_cast<float>(Vk[q] - C[q]);
-                Ef[k][q] = static_cast<float>(E[k][q]);
-            }
-            const double* e = E[k];
-            Mf[k][0] = static_cast<float>(n3[1] * e[2] - n3[2] * e[1]);
-            Mf[k][1] = static_cast<float>(n3[2] * e[0] - n3[0] * e[2]);
-            Mf[k][2] = static_cast<float>(n3[0] * e[1] - n3[1] * e[0]);
-            double ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-            r.inv[k] = ee > 0.0 ? static_cast<float>(1.0 / ee) : 0.f;
-        }
-        for (int q = 0; q < 3; ++q) r.nn[q] = static_cast<float>(n3[q]);
-        r.ok = nl > 0.0 ? 1.f : 0.f;
-        // unit normal in FP32 and a bound on its distance from the exact one: the cross
-        // product of rounded edges errs by at most 21 u |u| |v| (as a vector), which
-        // turns its direction by at most twice that over |u x v|; then the
-        // normalisation and the FP32 rounding of the components
+        // the FP64 path's plane bound: the unit normal in FP32 and a bound on its distance
+        // from the exact one: the cross product of rounded edges errs by at most
+        // 21 u |u| |v| (as a vector), which turns its direction by at most twice that
+        // over |u x v|; then the normalisation and the FP32 rounding of the components
         const double lu = sqrt(ux * ux + uy * uy + uz * uz), lv = sqrt(vx * vx + vy * vy + vz * vz);
         const double en = nl > 0.0 ? 50.0 * kU64 * lu * lv / nl + 1.2e-7 : 0.0;
         if (tnorm)
             tnorm[t] = make_float4(static_cast<float>(n3[0]), static_cast<float>(n3[1]),
                                    static_cast<float>(n3[2]), round_up_f(en));
-        // the record carries the same bound (nerr) for the plane test of the mixed path
-        r.nerr = round_up_f(en);
-        r.pad_ = 0.f;
+        // the mixed path's record in the triangle's frame: u along b - a (else along
+        // c - a, else x), v from c - a by two Gram-Schmidt passes (so c = a + cx u +
+        // cy v to FP64 rounding however thin the triangle), n = u x v
+        double U[3], Vv[3], bx;
+        const double lab = lu, lac = lv;
+        if (lab > 0.0) { U[0] = ux / lab; U[1] = uy / lab; U[2] = uz / lab; bx = lab; }
+        else if (lac > 0.0) { U[0] = vx / lac; U[1] = vy / lac; U[2] = vz / lac; bx = 0.0; }
+        else { U[0] = 1.0; U[1] = 0.0; U[2] = 0.0; bx = 0.0; }
+        double ccx = vx * U[0] + vy * U[1] + vz * U[2];
+        double rx = vx - ccx * U[0], ry = vy - ccx * U[1], rz = vz - ccx * U[2];
+        const double kk = rx * U[0] + ry * U[1] + rz * U[2];
+        ccx += kk;
+        rx -= kk * U[0]; ry -= kk * U[1]; rz -= kk * U[2];
+        const double ccy = sqrt(rx * rx + ry * ry + rz * rz);
+        if (ccy > 0.0) {
+            Vv[0] = rx / ccy; Vv[1] = ry / ccy; Vv[2] = rz / ccy;
+        } else {
+            // collinear: any unit vector across u (u x the axis least aligned with u)
+            const int ax = fabs(U[0]) <= fabs(U[1]) && fabs(U[0]) <= fabs(U[2]) ? 0 : (fabs(U[1]) <= fabs(U[2]) ? 1 : 2);
+            const double A[3] = {ax == 0 ? 1.0 : 0.0, ax == 1 ? 1.0 : 0.0, ax == 2 ? 1.0 : 0.0};
+            double wx = A[1] * U[2] - A[2] * U[1], wy = A[2] * U[0] - A[0] * U[2], wz = A[0] * U[1] - A[1] * U[0];
+            const double wl = sqrt(wx * wx + wy * wy + wz * wz);
+            Vv[0] = wx / wl; Vv[1] = wy / wl; Vv[2] = wz / wl;
+        }
+        const double N[3] = {U[1] * Vv[2] - U[2] * Vv[1], U[2] * Vv[0] - U[0] * Vv[2], U[0] * Vv[1] - U[1] * Vv[0]};
+        TriRec r;
+        r.o0[0] = static_cast<float>(a.x - cx);
+        r.o0[1] = static_cast<float>(a.y - cy);
+        r.o0[2] = static_cast<float>(a.z - cz);
+        for (int q = 0; q < 3; ++q) {
+            r.nn[q] = static_cast<float>(N[q]);
+            r.uu[q] = static_cast<float>(U[q]);
+            r.vv[q] = static_cast<float>(Vv[q]);
+        }
+        // the triangle lies in the frame's plane (to FP64 rounding), every triangle has
+        // one, and its FP32 normal is within the rounding of a unit vector (sqrt(3) u)
+        r.nerr = 2.4e-7f;
+        r.bx = static_cast<float>(bx);
+        r.cx = static_cast<float>(ccx);
+        r.cy = static_cast<float>(ccy);
+        r.e1x = static_cast<float>(ccx - bx);
+        r.ib = bx > 0.0 ? static_cast<float>(1.0 / bx) : 0.f;
+        const double l1 = (ccx - bx) * (ccx - bx) + ccy * ccy, l2 = ccx * ccx + ccy * ccy;
+        r.inv1 = l1 > 0.0 ? static_cast<float>(1.0 / l1) : 0.f;
+        r.inv2 = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
+        r.ok = bx > 0.0 && ccy > 0.0 ? 1.f : 0.f;
+        r.pad_[0] = r.pad_[1] = r.pad_[2] = 0.f;
         trec[t] = r;
     }
     // the mesh's coordinate scale max |v - K| (rounded up), per segment, for the

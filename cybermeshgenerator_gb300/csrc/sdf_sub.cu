@@ -389,7 +389,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                             const float4* src = reinterpret_cast<const float4*>(trec + t);
                             float4* dst = reinterpret_cast<float4*>(&s_rec[pos]);
 #pragma unroll
-                            for (int q2 = 0; q2 < 9; ++q2) cp_async16(dst + q2, src + q2);
+                            for (int q2 = 0; q2 < kRecVec; ++q2) cp_async16(dst + q2, src + q2);
                         }
                     }
                 }
@@ -456,11 +456,11 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                         const int slot = __popc(any & ((1u << lane) - 1u));
                         const float4* src = reinterpret_cast<const float4*>(trec + s_t[j0 + lane]);
                         float4* dst = reinterpret_cast<float4*>(wrec + slot);
-                        float4 v[9];
+                        float4 v[kRecVec];
 #pragma unroll
-                        for (int q2 = 0; q2 < 9; ++q2) v[q2] = __ldg(src + q2);
+                        for (int q2 = 0; q2 < kRecVec; ++q2) v[q2] = __ldg(src + q2);
 #pragma unroll
-                        for (int q2 = 0; q2 < 9; ++q2) dst[q2] = v[q2];
+                        for (int q2 = 0; q2 < kRecVec; ++q2) dst[q2] = v[q2];
                     }
                     __syncwarp();
                     unsigned m = any;
@@ -469,17 +469,16 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                         m &= m - 1u;
                         const float4 e = s_c[j0 + k];
                         const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
-                        // the plane: a triangle is no nearer than its plane, so a marked
+                        // the plane: a triangle is no nearer than the plane of its frame
+                        // (every triangle, degenerate or not, lies in one), so a marked
                         // triangle whose plane lies beyond every lane's bound is skipped
-                        // (see plane_reach; a degenerate triangle has a zero normal and
-                        // is never skipped)
+                        // (see plane_reach); its n component is the distance's first step
                         const TriRec& R = wrec[slot];
-                        const float dp = dot3f(__fsub_rn(dx, R.o0[0]), __fsub_rn(dy, R.o0[1]),
-                                               __fsub_rn(dz, R.o0[2]), R.nn);
-                        if (!__any_sync(0xffffffffu, valid && fabsf(dp) <= plane_reach(bestd, R.nerr, ebr4)))
+                        const PaN pn = pa_n(R, dx, dy, dz);
+                        if (!__any_sync(0xffffffffu, valid && fabsf(pn.n) <= plane_reach(bestd, R.nerr, ebr4)))
                             continue;
                         if (valid) {
-                            const float d2 = dist_rec_val(wrec[slot], dx, dy, dz);
+                            const float d2 = dist_rec_t<false>(R, pn, nullptr);
                             ++evals;
                             const int t = s_t[j0 + k];
                             if (d2 < best || (d2 == best && t < bt)) {
