@@ -287,12 +287,13 @@ __global__ void k_put_bytes(const int8_t* __restrict__ src, int8_t* __restrict__
 // coordinate column (cp.async.bulk, global -> shared, completion counted on an
 // mbarrier), kStages tiles in flight, one thread per query computing from shared
 // memory, the queries left appended to the CTA's own list segment (a shared-memory
-// count), and one barrier per tile before its stage is refilled. Every wait is bounded: a
-// wait that runs out (it never should) stops the CTA after draining its copies, and
-// sets `fault`, on which the host reruns the pass with the per-thread loads. When the
-// drain's own bounded waits run out as well, the CTA sets `drain_fault` too: copies
-// may still have been writing its shared memory, and the host reports an error
-// instead of rerunning.
+// count); a producer warp refills a stage once every consumer warp has arrived on the
+// stage's `empty` mbarrier. Every wait is bounded: a wait that runs out (it never
+// should) stops every warp of the CTA (a shared flag the other waits watch), the CTA
+// drains the last copy issued into each stage, and sets `fault`, on which the host
+// reruns the pass with the per-thread loads. When the drain's own bounded waits run out
+// as well, the CTA sets `drain_fault` too: copies may still have been writing its
+// shared memory, and the host reports an error instead of rerunning.
 template <int NPT>
 struct Tma {
     static constexpr int kCols = 3 * NPT;
@@ -335,80 +336,121 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
         if (clock64() - t0 > (1ll << 31)) return false;
     return true;
 }
+// The same, giving up at once when *abort is set (another warp's wait ran out).
+__device__ __forceinline__ bool mbar_wait_or_abort(unsigned long long* bar, unsigned parity,
+                                                   const volatile int* abort) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (*abort || clock64() - t0 > (1ll << 31)) return false;
+    return true;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Warp kConsumers of the CTA (thread kThreads on) issues the copies; warps 0 ..
+// kConsumers - 1 certify, one query per thread. A stage is refilled when its consumer
+// warps have each arrived on its `empty` mbarrier, so no warp waits for the others
+// between tiles.
+constexpr int kConsumers = kThreads / 32;
+constexpr int kTmaThreads = kThreads + 32;
 
 template <int NPT>
-__global__ void __launch_bounds__(kThreads) k_pred_fp32_tma(Soa s, int64_t ntiles,
-                                                            int8_t* __restrict__ out, Seg L,
-                                                            unsigned long long* __restrict__ fault,
-                                                            unsigned long long* __restrict__ drain_fault) {
+__global__ void __launch_bounds__(kTmaThreads) k_pred_fp32_tma(Soa s, int64_t ntiles,
+                                                               int8_t* __restrict__ out, Seg L,
+                                                               unsigned long long* __restrict__ fault,
+                                                               unsigned long long* __restrict__ drain_fault) {
     using T = Tma<NPT>;
     constexpr int C = T::kCols, S = T::kStages;
     extern __shared__ __align__(128) unsigned char smem[];
     double* buf = reinterpret_cast<double*>(smem);  // [S][C][kTile]
-    __shared__ __align__(8) unsigned long long bar[S];
+    __shared__ __align__(8) unsigned long long full[S], empty[S];
     __shared__ unsigned long long s_cnt;  // entries of this CTA's segment so far
-    const int tid = threadIdx.x, b = blockIdx.x;
+    __shared__ long long s_last[S];       // the last tile issued into each stage (-1: none)
+    __shared__ int s_abort;               // a wait ran out: every warp stops
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, b = blockIdx.x;
     const int64_t K = ntiles > b ? (ntiles - 1 - b) / gridDim.x + 1 : 0;
     int64_t* seg = L.list + static_cast<int64_t>(b) * L.segcap;
     const int64_t cbase = static_cast<int64_t>(b) * L.ccap;
-    auto issue = [&](int64_t k) {  // thread 0: tile k of this CTA into stage k % S
-        const int st = static_cast<int>(k % S);
-        const int64_t tile = b + k * gridDim.x;
-        mbar_expect_tx(&bar[st], T::kStageBytes);
-#pragma unroll
-        for (int c = 0; c < C; ++c)
-            bulk_copy(buf + (static_cast<size_t>(st) * C + c) * kTile, s.c[c] + tile * kTile,
-                      kTile * 8u, &bar[st]);
-    };
     if (tid == 0) {
         s_cnt = 0;
-        for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+        s_abort = 0;
+        for (int st = 0; st < S; ++st) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], kConsumers);
+            s_last[st] = -1;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0)
-        for (int64_t k = 0; k < S && k < K; ++k) issue(k);
-    for (int64_t k = 0; k < K; ++k) {
-        const int st = static_cast<int>(k % S);
-        const bool ok = mbar_wait(&bar[st], static_cast<unsigned>((k / S) & 1));
-        const int64_t i = (b + k * gridDim.x) * kTile + tid;
-        const double* sb = buf + static_cast<size_t>(st) * C * kTile;
-        int sg = 0;
-        if (ok) {
-            double v[C];
+    if (warp == kConsumers) {
+        if (lane == 0) {
+            for (int64_t k = 0; k < K; ++k) {
+                const int st = static_cast<int>(k % S);
+                // tile k - S has been read by every consumer warp (its phase of `empty`)
+                if (k >= S &&
+                    !mbar_wait_or_abort(&empty[st], static_cast<unsigned>((k / S - 1) & 1), &s_abort)) {
+                    if (atomicExch(&s_abort, 1) == 0) atomicExch(fault, 1ull);
+                    break;
+                }
+                // the copy into the stage follows the consumers' generic reads of it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const int64_t tile = b + k * gridDim.x;
+                mbar_expect_tx(&full[st], T::kStageBytes);
 #pragma unroll
-            for (int c = 0; c < C; ++c) v[c] = sb[c * kTile + tid];
-            sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
-            out[i] = static_cast<int8_t>(sg);
-        }
-        // a query left goes to this CTA's segment, and its coordinates, read again from
-        // the stage (still held; reading them again keeps the values out of registers
-        // across the append), to the segment's compact slots
-        const int64_t pos = seg_pos(ok && sg == 0, &s_cnt);
-        if (pos >= 0) {
-            seg[pos] = i;
-            if (pos < L.ccap) {
-                const volatile double* vb = sb;
-#pragma unroll
-                for (int c = 0; c < C; ++c) L.cc[c][cbase + pos] = vb[c * kTile + tid];
+                for (int c = 0; c < C; ++c)
+                    bulk_copy(buf + (static_cast<size_t>(st) * C + c) * kTile, s.c[c] + tile * kTile,
+                              kTile * 8u, &full[st]);
+                s_last[st] = k;
             }
         }
-        if (__syncthreads_or(!ok)) {
-            // a wait ran out: drain this CTA's copies still in flight (bounded), then stop
-            if (tid == 0) {
-                atomicExch(fault, 1ull);
-                bool drained = true;
-                for (int64_t j = k; j < K && j < k + S; ++j)
-                    drained = mbar_wait(&bar[j % S], static_cast<unsigned>((j / S) & 1)) && drained;
-                if (!drained) atomicExch(drain_fault, 1ull);
+    } else {
+        for (int64_t k = 0; k < K; ++k) {
+            const int st = static_cast<int>(k % S);
+            const bool ok = __all_sync(
+                0xffffffffu, mbar_wait_or_abort(&full[st], static_cast<unsigned>((k / S) & 1), &s_abort));
+            if (!ok) {
+                if (lane == 0 && atomicExch(&s_abort, 1) == 0) atomicExch(fault, 1ull);
+                break;
             }
-            return;
+            const int64_t i = (b + k * gridDim.x) * kTile + tid;
+            const double* sb = buf + static_cast<size_t>(st) * C * kTile;
+            int sg;
+            {
+                double v[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) v[c] = sb[c * kTile + tid];
+                sg = NPT == 4 ? o3d_fp32(v) : isp_fp32(v);
+                out[i] = static_cast<int8_t>(sg);
+            }
+            // a query left goes to this CTA's segment, and its coordinates, read again
+            // from the stage (still held; reading them again keeps the values out of
+            // registers across the append), to the segment's compact slots
+            const int64_t pos = seg_pos(sg == 0, &s_cnt);
+            if (pos >= 0) {
+                seg[pos] = i;
+                if (pos < L.ccap) {
+                    const volatile double* vb = sb;
+#pragma unroll
+                    for (int c = 0; c < C; ++c) L.cc[c][cbase + pos] = vb[c * kTile + tid];
+                }
+            }
+            // this warp is done with the stage
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
         }
-        // the stage is consumed: the next copy into it follows the generic reads of it
-        if (tid == 0 && k + S < K) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(k + S);
+    }
+    __syncthreads();
+    if (s_abort) {
+        // a wait ran out: drain the last copy issued into each stage (bounded), then stop
+        if (tid == 0) {
+            bool drained = true;
+            for (int st = 0; st < S; ++st)
+                if (s_last[st] >= 0)
+                    drained = mbar_wait(&full[st], static_cast<unsigned>((s_last[st] / S) & 1)) && drained;
+            if (!drained) atomicExch(drain_fault, 1ull);
         }
+        return;
     }
     if (tid == 0) L.cnt[b] = s_cnt;
 }
@@ -687,13 +729,13 @@ int pred_stream_device(int npt, const double* const* coords, int64_t n, int mode
         if (npt == 4) {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<4>::kSmem)));
-            k_pred_fp32_tma<4><<<L.nseg, kThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
-                                                                        &c->drain_fault);
+            k_pred_fp32_tma<4><<<L.nseg, kTmaThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
+                                                                           &c->drain_fault);
         } else {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<5>::kSmem)));
-            k_pred_fp32_tma<5><<<L.nseg, kThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
-                                                                        &c->drain_fault);
+            k_pred_fp32_tma<5><<<L.nseg, kTmaThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
+                                                                           &c->drain_fault);
         }
         CMG_LAUNCH();
     }
