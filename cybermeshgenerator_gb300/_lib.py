@@ -167,6 +167,7 @@ def _bind(lib: ctypes.CDLL) -> None:
     sig("cmg_voxels_layers", None, [V, c_int_p, c_int_p, c_int_p])
     sig("cmg_plc_grid", I, [V, I, I, c_double_p, c_double_p, c_int_p, S, Z])
     sig("cmg_debug_fail_device_allocs", I, [I, I])
+    sig("cmg_debug_fail_pred_wait", I, [ctypes.c_int64])
     sig("cmg_voxels_stats", None, [V, ctypes.POINTER(VoxelStats)])
     sig("cmg_batch_create", I, [ctypes.POINTER(V), c_int_p, c_int_p, I,
                                 ctypes.POINTER(VoxelOpts), c_void_pp, S, Z])

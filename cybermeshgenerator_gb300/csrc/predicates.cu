@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -355,11 +356,15 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
 constexpr int kConsumers = kThreads / 32;
 constexpr int kTmaThreads = kThreads + 32;
 
+// fail_at >= 0 (tests): consumer warp 0 of CTA 0 takes its wait for tile fail_at as
+// having run out, which drives the abort, the drain and the host's rerun without a
+// wait that really runs out.
 template <int NPT>
 __global__ void __launch_bounds__(kTmaThreads) k_pred_fp32_tma(Soa s, int64_t ntiles,
                                                                int8_t* __restrict__ out, Seg L,
                                                                unsigned long long* __restrict__ fault,
-                                                               unsigned long long* __restrict__ drain_fault) {
+                                                               unsigned long long* __restrict__ drain_fault,
+                                                               int64_t fail_at) {
     using T = Tma<NPT>;
     constexpr int C = T::kCols, S = T::kStages;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -407,8 +412,10 @@ __global__ void __launch_bounds__(kTmaThreads) k_pred_fp32_tma(Soa s, int64_t nt
     } else {
         for (int64_t k = 0; k < K; ++k) {
             const int st = static_cast<int>(k % S);
-            const bool ok = __all_sync(
-                0xffffffffu, mbar_wait_or_abort(&full[st], static_cast<unsigned>((k / S) & 1), &s_abort));
+            const bool ok =
+                __all_sync(0xffffffffu,
+                           mbar_wait_or_abort(&full[st], static_cast<unsigned>((k / S) & 1), &s_abort) &&
+                               !(b == 0 && warp == 0 && k == fail_at));
             if (!ok) {
                 if (lane == 0 && atomicExch(&s_abort, 1) == 0) atomicExch(fault, 1ull);
                 break;
@@ -638,6 +645,10 @@ PredWork& pred_work() {
     return w[dev & 63];
 }
 
+// One-shot test knob: the next TMA-staged FP32 pass takes its wait for this tile (of
+// CTA 0, warp 0) as having run out; -1 = off.
+std::atomic<long long> g_fail_wait_at{-1};
+
 struct Counters {
     unsigned long long n32;  // left by the FP32 pass
     unsigned long long n64;  // left by the FP64 pass
@@ -726,16 +737,17 @@ int pred_stream_device(int npt, const double* const* coords, int64_t n, int mode
     const int64_t ntiles = aligned ? n / kTile : 0;
     if (fp32_events) CMG_CUDA(cudaEventRecord(fp32_events[0], st));
     if (ntiles > 0) {
+        const int64_t fail_at = g_fail_wait_at.exchange(-1);
         if (npt == 4) {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<4>::kSmem)));
             k_pred_fp32_tma<4><<<L.nseg, kTmaThreads, Tma<4>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
-                                                                           &c->drain_fault);
+                                                                           &c->drain_fault, fail_at);
         } else {
             CMG_CUDA(cudaFuncSetAttribute(k_pred_fp32_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(Tma<5>::kSmem)));
             k_pred_fp32_tma<5><<<L.nseg, kTmaThreads, Tma<5>::kSmem, st>>>(s, ntiles, d_out, L, &c->fault,
-                                                                           &c->drain_fault);
+                                                                           &c->drain_fault, fail_at);
         }
         CMG_LAUNCH();
     }
@@ -1016,6 +1028,12 @@ cmg_status cmg_insphere_stream(const double* const* coords, int64_t n, int mode,
                                signed char* out, cmg_pred_stats* stats, void* stream, char* errbuf,
                                size_t errbuf_len) {
     return run_stream(5, coords, n, mode, where, out, stats, stream, errbuf, errbuf_len);
+}
+
+cmg_status cmg_debug_fail_pred_wait(int64_t tile) {
+    if (tile < -1) return CMG_ERR_INVALID_INPUT;
+    cmg::gpu::g_fail_wait_at.store(tile);
+    return CMG_OK;
 }
 
 cmg_status cmg_orient3d_signs(const double* xyz, int npts, const int* tets, int n, int* out_sign) {

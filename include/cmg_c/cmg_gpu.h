@@ -373,6 +373,13 @@ cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t npoints,
  * releases what it holds, and leaves the library usable for the next call. */
 cmg_status cmg_debug_fail_device_allocs(int skip, int count);
 
+/* Test hook, no reference counterpart: the next predicate stream whose FP32 pass is
+ * TMA-staged takes the wait of its first CTA's first warp for that CTA's tile `tile`
+ * as having run out (-1 = off; used once). The pass then stops every warp, drains the
+ * copies in flight and is rerun with per-thread loads (cmg_pred_stats.tma_reruns = 1),
+ * with the same signs. No wait runs out for real and the GPU stays usable. */
+cmg_status cmg_debug_fail_pred_wait(int64_t tile);
+
 /* Library build identification, e.g. "cmg-gb300 sm_103a". */
 const char* cmg_gpu_version(void);
 

@@ -54,6 +54,46 @@ def test_stream_left_queries_beyond_compact_slots(cm, orc, kind):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("kind", ["orient3d", "insphere"])
+def test_stream_wait_taken_as_run_out_reruns(cm, kind):
+    """A wait of the TMA-staged FP32 pass taken as having run out (cmg_debug_fail_pred_wait,
+    set on the host; no wait runs out for real): every warp of the CTA stops, the copies
+    in flight are drained, and the host reruns the pass with per-thread loads. The signs
+    equal a normal call's, the stats count the rerun, and the next call runs normally."""
+    torch = pytest.importorskip("torch")
+    from cybermeshgenerator_gb300 import _lib
+    from cybermeshgenerator_gb300 import workloads as W
+    L = _lib.load()
+    S = W.predicate_stream(300_000, kind, degenerate=0.1, near=0.1, seed=35)
+    fn = cm.orient3d_stream if kind == "orient3d" else cm.insphere_stream
+    n = S.shape[1]
+    d = torch.tensor(S, device="cuda")  # device columns: the TMA-staged pass takes them
+    ptrs = [d[k].data_ptr() for k in range(S.shape[0])]
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def run():
+        out = torch.zeros(n, dtype=torch.int8, device="cuda")
+        _, st = fn((ptrs, n, out.data_ptr()), cm.PRED_COMPAT, stream=stream)
+        torch.cuda.synchronize()
+        return out.cpu().numpy(), st
+
+    want, st0 = run()
+    assert st0["tma_reruns"] == 0
+    try:
+        assert L.cmg_debug_fail_pred_wait(2) == 0   # CTA 0's third tile
+        got, st = run()
+    finally:
+        L.cmg_debug_fail_pred_wait(-1)
+    assert st["tma_reruns"] == 1
+    assert np.array_equal(got, want)
+    for k in ("fp64_queries", "exact_queries", "expansion_queries"):
+        assert st[k] == st0[k], k
+    again, st2 = run()
+    assert st2["tma_reruns"] == 0 and np.array_equal(again, want)
+    host, _ = fn(S, cm.PRED_COMPAT)
+    assert np.array_equal(host, want)
+
+
 def test_stream_device_memory(cm):
     torch = pytest.importorskip("torch")
     from cybermeshgenerator_gb300 import workloads as W
