@@ -110,10 +110,18 @@ void set_err(char* buf, size_t len, const std::string& msg) {
     }
 }
 
-// The GPU entry points are serialised per process (one workspace per device).
+// The GPU entry points are serialised per device (one workspace pool and one library
+// stream per device), on the calling thread's current device: calls on different
+// devices run concurrently. Never throws (no current device: the first lock).
 std::mutex& gpu_mutex() {
-    static std::mutex m;
-    return m;
+    constexpr int kMaxDevices = 64;
+    static std::mutex m[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    return m[dev >= 0 && dev < kMaxDevices ? dev : 0];
 }
 
 // The library's own stream on the current device, created on first use and kept
