@@ -341,15 +341,43 @@ def run_ours(args):
         wm = mixed.work_model()
         st = mixed.stats()
         line["config"]["tuning"] = dict(chosen(st), autotuned=bool(tune["autotune"]))
-        plain = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64, **tune)
+        # every candidate evaluated in FP64 (the reference's arithmetic throughout)
+        plain = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64_PLAIN, **tune)
         plain.run().sync()
         p_ms = time_batch(cm, torch, plain, max(1, min(3, args.steps)), 1, flush)
         plain.set_timing(True)
         plain.run().sync()
         tp = plain.timing()
         p_value = cells * len(p_ms) / (sum(p_ms) * 1e-3)
+        # the library's FP64 path (the FP32 pass, then the FP64 distance of each cell's
+        # near-ties): the same bits as the plain one, checked here on the whole grid
+        exact = cm.Batch([plc], [RESOLUTION], [PAD], outputs=outs, precision=cm.PREC_FP64, **tune)
+        exact.run().sync()
+        x_ms = time_batch(cm, torch, exact, max(3, args.steps), 1, flush)
+        exact.set_timing(True)
+        exact.run().sync()
+        tx, sx = exact.timing(), exact.stats()
+        x_e2e = []
+        for i in range(4):
+            t0 = time.perf_counter()
+            cm.voxelize_ex(plc, resolution=RESOLUTION, pad=PAD, outputs=outs, precision=cm.PREC_FP64,
+                           **tune)
+            if i >= 1:
+                x_e2e.append(time.perf_counter() - t0)
         # accuracy of this run: mixed vs plain (FP64, bit-identical to the reference)
         rm, rp = mixed.result(0), plain.result(0)
+        rx = exact.result(0)
+        line["fp64_exact"] = {
+            "value": cells * len(x_ms) / (sum(x_ms) * 1e-3),
+            "e2e": cells / (sum(x_e2e) / len(x_e2e)),
+            "identical_to_plain": bool(np.array_equal(rx.occupancy, rp.occupancy) and
+                                       np.array_equal(rx.sdf32.view(np.uint32), rp.sdf32.view(np.uint32))),
+            "eval_ms": tx["eval_ms"], "phase_ms": tx, "plain_eval_ms": tp["eval_ms"],
+            "evaluations": int(sx["evaluations"]), "fp64_evaluations": int(sx["fp64_evaluations"]),
+            "band_cells": int(sx["band_cells"]), "tuning": chosen(sx),
+            "path": "CMG_PREC_FP64 (the default of cmg_plc_voxelize): FP32 pass with bounds "
+                    "widened to every near-tie of the FP32 minimum, FP64 distances in the "
+                    "reference's order over those; plain = CMG_PREC_FP64_PLAIN"}
         diag = float(np.linalg.norm(pts.max(0) - pts.min(0)))
         err = np.abs(rm.sdf32.astype(np.float64) - rp.sdf32.astype(np.float64))
         occ_same = bool(np.array_equal(rm.occupancy, rp.occupancy))

@@ -33,7 +33,7 @@ from . import _lib as _L
 _clib = _L.Lazy()
 
 OUT_OCCUPANCY, OUT_SDF_F32, OUT_SDF_F64, OUT_NEAREST, OUT_ERROR_BOUND = 1, 2, 4, 8, 16
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP64_PLAIN = 0, 1, 2
 PRED_COMPAT, PRED_EXACT = 0, 1
 
 

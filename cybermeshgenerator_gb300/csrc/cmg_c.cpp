@@ -227,6 +227,7 @@ cmg::gpu::VoxOpts to_vox(const cmg_voxel_opts& o, int outputs) {
     cmg::gpu::VoxOpts v;
     v.predicates = o.predicates == CMG_PRED_EXACT ? cmg::gpu::kPredExact : cmg::gpu::kPredCompat;
     v.precision = o.precision == CMG_PREC_MIXED ? cmg::gpu::kPrecMixed : cmg::gpu::kPrecFP64;
+    v.fp64_filter = o.precision != CMG_PREC_FP64_PLAIN;
     v.brick = o.brick;
     v.band = static_cast<float>(o.band);
     v.want_occ = outputs & CMG_OUT_OCCUPANCY;

@@ -63,6 +63,10 @@ struct Stats {
 
 enum : int { kPredCompat = 0, kPredExact = 1 };
 enum : int { kPrecFP64 = 0, kPrecMixed = 1 };
+// The evaluation kernel's own third precision: FP64 results through the FP32 pass and an
+// FP64 refinement of each cell's near-ties (kPrecFP64 on 16^3 bricks unless plain FP64 is
+// asked for).
+enum : int { kPrecExact = 2 };
 
 // Triangle record in the soup: 9 coordinates + 1 pad (80 bytes, 16-byte aligned).
 constexpr int kSoupStride = 10;

@@ -179,6 +179,13 @@ T* carve(Arena& a, size_t n) {
 // 4 or 8: one list and one evaluation CTA per brick of that edge.
 int pick_brick(const VoxOpts& o) { return (o.brick == 4 || o.brick == 8) ? o.brick : 16; }
 
+// The 4^3 sub-brick kernel's precision: mixed, exact FP64 through the FP32 pass
+// (kPrecExact), or every candidate in FP64.
+int sub_precision(const VoxOpts& o) {
+    if (o.precision == kPrecMixed) return kPrecMixed;
+    return o.fp64_filter ? kPrecExact : kPrecFP64;
+}
+
 }  // namespace
 
 // Workspace arenas shared by transient batches on a device (one call at a time,
@@ -395,7 +402,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
     // persistent evaluation grid: resident CTAs per SM for the chosen kernel
     if (opts_.grab <= 0) opts_.grab = 1;
     if (opts_.stage < 0) opts_.stage = 0;
-    if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(opts_.precision, opts_.stage != 0, opts_.ctas) : sms;
+    if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(sub_precision(opts_), opts_.stage != 0, opts_.ctas) : sms;
     else impl_->grid_eval = (brick == 4 ? 8 : 3) * sms;
 }
 
@@ -557,7 +564,7 @@ void Batch::run_impl(bool sizing) {
     CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
     if (timed) CMG_CUDA(cudaEventRecord(ev_[2], st));
     if (opts_.brick == 16)
-        launch_sdf_sub(opts_.precision, opts_.stage != 0, opts_.grab, opts_.probe, opts_.ctas, dsegs_,
+        launch_sdf_sub(sub_precision(opts_), opts_.stage != 0, opts_.grab, opts_.probe, opts_.ctas, dsegs_,
                        nseg, I.work, nwork_, queue_, I.soup, I.tinfo,
                        I.tinfo_lo, I.trec, I.tnorm, I.cand_off, I.cand, I.brick_emax, opts_.band, occ,
                        sdf32_, sdf64_, near_tri_, near_reg_, err_, stats_, I.grid_eval, st);
@@ -618,7 +625,7 @@ RunInfo Batch::info() {
     r.brick = opts_.brick;
     r.grab = opts_.brick == 16 ? opts_.grab : 0;
     r.walk_warps = brick_walk_warps(nbrick_, opts_.walk_warps);
-    r.probe = opts_.precision == kPrecMixed ? (opts_.probe > 0 ? opts_.probe : 1024) : 0;
+    r.probe = sub_precision(opts_) != kPrecFP64 ? (opts_.probe > 0 ? opts_.probe : 1024) : 0;
     r.ctas = opts_.brick == 16 ? sdf_sub_minb(opts_.ctas) : 0;
     r.cells = nvox_;
     r.pairs = pairs_cap_;
@@ -680,7 +687,7 @@ void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t s
     const bool sdf = opts.want_sdf32 || opts.want_sdf64 || opts.want_near;
     if (!sdf) return;  // the occupancy kernels have no tunables
     auto lg = [](int64_t v) { return v > 0 ? static_cast<int>(std::log2(static_cast<double>(v)) * 2) : 0; };
-    auto key = std::make_tuple(opts.precision, lg(tris), lg(cells),
+    auto key = std::make_tuple(sub_precision(opts), lg(tris), lg(cells),
                                static_cast<int>(std::min<size_t>(meshes.size(), 4)),
                                static_cast<int>(opts.want_sdf64));
     auto apply = [&](const Tuned& t) {
@@ -742,7 +749,7 @@ void autotune(const std::vector<HostMesh>& meshes, VoxOpts& opts, cudaStream_t s
         try_set(t);
     }
     if (cur.brick == 16) {
-        if (opts.precision == kPrecMixed) {
+        if (sub_precision(opts) != kPrecFP64) {  // the FP32 pass's probe head
             const Tuned step2 = cur;
             for (int pr : {256, 512, 2048}) {
                 Tuned t = step2;

@@ -25,7 +25,10 @@ namespace cmg::gpu {
 
 struct VoxOpts {
     int predicates = kPredCompat;  // kPredCompat (reference semantics) | kPredExact
-    int precision = kPrecFP64;     // kPrecFP64 (plain, bit-exact) | kPrecMixed
+    int precision = kPrecFP64;     // kPrecFP64 (bit-exact) | kPrecMixed
+    bool fp64_filter = true;       // kPrecFP64 on 16^3 bricks: the FP32 pass with an FP64
+                                   // refinement of each cell's near-ties (kPrecExact);
+                                   // false: every candidate in FP64 (the same results)
     int brick = 0;                 // candidate brick edge: 16 (default; 4^3 sub-brick
                                    // evaluation), 8 or 4 (one CTA per brick)
     float band = 1.0f;             // mixed: FP64 refinement band, in cells

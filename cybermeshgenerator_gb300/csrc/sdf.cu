@@ -120,7 +120,11 @@ __global__ void k_sdf_tri_prep(const MeshSeg* __restrict__ segs, int nseg, int64
         const double kk = rx * U[0] + ry * U[1] + rz * U[2];
         ccx += kk;
         rx -= kk * U[0]; ry -= kk * U[1]; rz -= kk * U[2];
-        const double ccy = sqrt(rx * rx + ry * ry + rz * rz);
+        // a residual at the rounding level (exactly collinear vertices leave one along u)
+        // carries no direction: the triangle is taken as collinear, which moves c by at
+        // most 1e-9 of the triangle's size (far inside the stated FP32 error)
+        double ccy = sqrt(rx * rx + ry * ry + rz * rz);
+        if (!(ccy > 1e-9 * fmax(lab, lac))) ccy = 0.0;
         if (ccy > 0.0) {
             Vv[0] = rx / ccy; Vv[1] = ry / ccy; Vv[2] = rz / ccy;
         } else {
@@ -486,8 +490,11 @@ k_brick_walk(const MeshSeg* __restrict__ segs, int nseg, int64_t nbricks,
     } else {
         U = bound[gb];
     }
-    // ---- candidates: lower bound <= U + 2 r_B (+ margins)
-    const float lim = (U + 2.f * q.rb) * (1.f + 1e-5f) + 2.f * tol;
+    // ---- candidates: lower bound <= U + 2 r_B (+ margins). The relative margin (4e-5,
+    // about 670 u) covers four stated FP32 errors 48u (d + 2e + 2r) beyond any cell's
+    // distance (e at most two bricks here; larger triangles are always considered): the
+    // exact FP64 path's near-ties and its band pass need them, the mixed path two
+    const float lim = (U + 2.f * q.rb) * (1.f + 4e-5f) + 2.f * tol;
     const int64_t out = FILL ? cand_off[gb] : 0;
     const unsigned below = (1u << lane) - 1u;
     float bemax = 0.f;

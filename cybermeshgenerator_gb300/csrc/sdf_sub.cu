@@ -50,6 +50,12 @@ constexpr int kChunk = 32;
 // a chunk whose warp pre-test passes at least this many entries tests all of them
 // unrolled, else only those that passed
 constexpr int kDenseChunk = 20;
+// kPrecExact, the exact FP64 path: the mixed kernel's FP32 pass with its bounds widened
+// to admit every triangle whose FP32 distance is within twice the stated error of the
+// cell's FP32 minimum, those near-ties kept per cell (kNear slots), and the FP64 distance
+// in the reference's order over them, which is the FP64 minimum over all triangles (a
+// cell with more near-ties takes the band pass).
+constexpr int kNear = 6;
 constexpr int kBatch = 4;  // candidates per thread per probe/filter step (loads in flight)
 constexpr int kProbe = 1024;  // default head of the brick list the mixed probe scans
 
@@ -78,6 +84,22 @@ __device__ __forceinline__ float reach(float b, float term) {
 // independent of the order of the filtered list (which the warps' scheduling sets).
 __device__ __forceinline__ float cell_bound(float d2, float kap) {
     return __fmaf_ru(sqrtf(d2), 1.f + 58.f * kU32, kap);
+}
+
+// The exact path's bound: a near-tie's FP32 distance is within two stated errors of the
+// cell's FP32 minimum m = sqrt(d2) and its true distance d one more, so d <= m + 3 E(d),
+// E(d) = 48u (d + 2e + 2r), which gives 3 E(d) <= 144.1u m + 288.2u (e + r); with the
+// square root's rounding, sqrt(d2)(1 + 160u) + kapx, kapx = RU(300u (e + r)), covers it.
+__device__ __forceinline__ float cell_bound_x(float d2, float kapx) {
+    return __fmaf_ru(sqrtf(d2), 1.f + 160.f * kU32, kapx);
+}
+
+// The near-tie threshold of a cell whose FP32 minimum is sqrt(d2), squared and rounded
+// up: at least (m + 2 eb)^2, eb = 48u (m + 2e + 2r) the band pass's stated bound, so the
+// kept triangles include every one the band pass would refine (kap = 98u (e + r)).
+__device__ __forceinline__ float near_thr2(float d2, float kap) {
+    const float thr = __fmaf_ru(sqrtf(d2), 1.f + 100.f * kU32, __fmul_ru(2.f, kap));
+    return __fmul_ru(thr, thr);
 }
 
 // Largest computed plane distance |n . (cell - a)| of a triangle that can still reach
@@ -152,7 +174,11 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
           const int64_t* __restrict__ cand_off,
           const int* __restrict__ cand, const float* __restrict__ brick_emax, float band_cells,
           Out o, Stats* __restrict__ st) {
+    constexpr bool MIX = PREC != kPrecFP64;     // the FP32 pass (mixed or exact)
+    constexpr bool EXACT = PREC == kPrecExact;  // ... refined to the FP64 minimum everywhere
     constexpr int kCap = Cap<STAGE>::value;
+    // exact path: per cell, its near-ties (triangle, FP32 squared distance), slot-major
+    __shared__ int2 s_near[EXACT ? kNear : 1][kSubThreads];
     __shared__ float4 s_c[kCap];  // centroid relative to the sub-brick centre, radius
     // FP64 path: unit normal and plane offset n . centroid, and a bound on the error of
     // the plane distances computed from them
@@ -160,8 +186,8 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
     __shared__ float s_pe[PREC == kPrecFP64 ? kCap : 1];
     __shared__ int s_t[kCap];
     __shared__ TriRec s_rec[STAGE ? kCap : 1];
-    __shared__ TriRec s_wrec[PREC == kPrecMixed && !STAGE ? (kSubThreads / 32) * kChunk : 1];
-    __shared__ float4 s_wsph[PREC == kPrecMixed && !STAGE ? kSubThreads / 32 : 1];  // per warp
+    __shared__ TriRec s_wrec[MIX && !STAGE ? (kSubThreads / 32) * kChunk : 1];
+    __shared__ float4 s_wsph[MIX && !STAGE ? kSubThreads / 32 : 1];  // per warp
     __shared__ int s_n;
     __shared__ long long s_item;
     __shared__ unsigned long long s_red[kSubThreads / 32];
@@ -204,7 +230,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const float py = static_cast<float>((y + 0.5) * g.h - cky);
         const float pz = static_cast<float>((z + 0.5) * g.h - ckz);
         const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
-        if (PREC == kPrecMixed && !STAGE) {
+        if (MIX && !STAGE) {
             // the warp's sphere for the chunk pre-test: centre at the middle of the box of
             // its valid cells, radius an upper bound on their distances from it (none
             // valid: radius 0, and no cell tests anything)
@@ -235,7 +261,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         // triangles, then bins ring by ring), so its head holds the centre's nearest. The
         // mixed path scans only the head (a looser U lengthens the filtered lists a
         // little, which the cheap FP32 distances absorb); the FP64 path scans it all
-        const int64_t cp = PREC == kPrecMixed && c1 - c0 > probe_n ? c0 + probe_n : c1;
+        const int64_t cp = MIX && c1 - c0 > probe_n ? c0 + probe_n : c1;
         for (int64_t k0 = c0 + tid; k0 < cp; k0 += kBatch * kSubThreads) {
             // loads of kBatch candidates in flight before any of them is used
             int tt[kBatch];
@@ -285,19 +311,27 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const int seed = static_cast<int>(static_cast<unsigned>(kmin & 0xffffffffull));
         // mixed: the stated FP32 error of a distance near d is 48u (d + 2 e + 2 r) (e the
         // mesh's largest centroid-to-vertex distance); kap carries its constant part
-        const float kap = PREC == kPrecMixed ? __fmul_ru(98.f * kU32, __fadd_ru(s.emax_all, r4)) : 0.f;
-        const float ebr4 = PREC == kPrecMixed ? __fmul_ru(4.f, __fadd_ru(s.emax_all, r4)) : 0.f;
+        const float kap = MIX ? __fmul_ru(98.f * kU32, __fadd_ru(s.emax_all, r4)) : 0.f;
+        // the cells' pruning bound's constant: one stated error (mixed), three (exact)
+        const float kapb = EXACT ? __fmul_ru(300.f * kU32, __fadd_ru(s.emax_all, r4)) : kap;
+        const float ebr4 = MIX ? __fmul_ru(4.f, __fadd_ru(s.emax_all, r4)) : 0.f;
         // a triangle can be nearest to a cell only if its sphere reaches U + 2 r; in the
         // mixed path, also any triangle whose FP32 distance can undercut the nearest
         // one's (two stated errors more), so the filtered list holds every triangle the
-        // FP32 minimum can come from
+        // FP32 minimum can come from; in the exact path every near-tie too (four)
         const float limf = (U + 2.f * r4) * (1.f + 32.f * kU32) + 32.f * kU32 * (U + r4) +
-                           (PREC == kPrecMixed ? __fmaf_ru(100.f * kU32, U + 4.f * r4, 2.f * kap) : 0.f);
+                           (EXACT ? __fmaf_ru(200.f * kU32, U + 4.f * r4, 4.f * kap)
+                                  : MIX ? __fmaf_ru(100.f * kU32, U + 4.f * r4, 2.f * kap) : 0.f);
 
         // ---- 2+3. rounds: filter into shared memory, then evaluate the cells
         float best = FLT_MAX, bestd = FLT_MAX;  // FP32 path
         double best64 = DBL_MAX;                // FP64 path
         int bt = INT_MAX, br = 0;
+        // exact path: the near-ties kept (s_near[0 .. nnear)), whether more were met, and
+        // the squared threshold that keeps them (near_thr2 of the current minimum)
+        int nnear = 0;
+        bool over = false;
+        float thr2 = 0.f;
         d3 P{0, 0, 0};
         if (PREC == kPrecFP64)
             P = {cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
@@ -308,7 +342,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
             const float dx = px - ((hi.x - chx) + (lo.x - clx));
             const float dy = py - ((hi.y - chy) + (lo.y - cly));
             const float dz = pz - ((hi.z - chz) + (lo.z - clz));
-            if (PREC == kPrecMixed) {
+            if (MIX) {
                 TriRec r;
                 load_rec(trec, seed, r);
                 int reg;
@@ -316,7 +350,12 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 ++evals;
                 bt = seed;
                 br = reg;
-                bestd = cell_bound(best, kap);
+                bestd = EXACT ? cell_bound_x(best, kapb) : cell_bound(best, kap);
+                if (EXACT) {
+                    thr2 = near_thr2(best, kap);
+                    s_near[0][tid] = make_int2(seed, __float_as_int(best));
+                    nnear = 1;
+                }
             } else {
                 d3 a, b, c;
                 load_soup(soup, seed, a, b, c);
@@ -378,7 +417,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     base = __shfl_sync(0xffffffffu, base, 0);
                     if (take) {
                         const int pos = base + __popc(m & ((1u << lane) - 1u));
-                        if (PREC == kPrecMixed && !STAGE) e.w = reach_term(e.w, r4);
+                        if (MIX && !STAGE) e.w = reach_term(e.w, r4);
                         s_c[pos] = e;
                         if (PREC == kPrecFP64) {
                             s_nrm[pos] = nv;
@@ -399,7 +438,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                 n = s_n;
             }
             if (tid == 0 && n) atomicAdd(&st->filtered, static_cast<unsigned long long>(n));
-            if (PREC == kPrecMixed && !STAGE) {
+            if (MIX && !STAGE) {
                 // In chunks of kChunk entries: each lane marks the entries its cell may
                 // need under its bound at the start of the chunk (s_c[].w holds the
                 // radius term of the reach, see reach_term); the warp stages the records
@@ -485,7 +524,24 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                                 best = d2;
                                 bt = t;
                                 br = -1;  // the region of the final triangle is found below
-                                bestd = cell_bound(d2, kap);
+                                bestd = EXACT ? cell_bound_x(d2, kapb) : cell_bound(d2, kap);
+                                if (EXACT) {
+                                    // a new minimum: drop the kept near-ties beyond its
+                                    // (smaller) threshold
+                                    thr2 = near_thr2(d2, kap);
+                                    int kept = 0;
+                                    for (int q = 0; q < nnear; ++q) {
+                                        const int2 nt = s_near[q][tid];
+                                        if (__int_as_float(nt.y) <= thr2) s_near[kept++][tid] = nt;
+                                    }
+                                    nnear = kept;
+                                }
+                            }
+                            // every triangle within the threshold when evaluated is kept
+                            // (the threshold only shrinks; the seed is kept already)
+                            if (EXACT && d2 <= thr2 && t != seed) {
+                                if (nnear < kNear) s_near[nnear++][tid] = make_int2(t, __float_as_int(d2));
+                                else over = true;
                             }
                         }
                     }
@@ -506,7 +562,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     if (!__any_sync(0xffffffffu, need)) continue;
                 }
                 const int t = s_t[j];
-                if (PREC == kPrecMixed) {
+                if (MIX) {
                     TriRec rr;
                     if (!STAGE) load_rec(trec, t, rr);
                     const TriRec& r = STAGE ? s_rec[j] : rr;
@@ -545,13 +601,37 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         bool inband = false;
         double best_band = DBL_MAX;
         int bt64 = INT_MAX, br64 = 0;
-        if (PREC == kPrecMixed) {
+        if (MIX) {
             const float d32 = sqrtf(best);
             // the mesh's largest triangle radius (not the brick's candidates', which
             // depend on the candidate walk): the bound, and the band it selects, are
             // the same whatever slab of the grid is evaluated
             eb = 48.f * kU32 * (d32 + 2.f * s.emax_all + 2.f * r4) + 1e-30f;
-            inband = valid && d32 <= band_cells * static_cast<float>(g.h) + eb;
+            if (EXACT) {
+                // the FP64 distance, in the reference's order, of every kept near-tie: the
+                // FP64 minimum over all triangles (lowest index on ties). A cell that met
+                // more near-ties than it could keep, or none, takes the band pass below.
+                if (valid && !over) {
+                    const d3 Pc{cell_center(g.corner[0], x, g.h), cell_center(g.corner[1], y, g.h),
+                                cell_center(g.corner[2], z, g.h)};
+                    for (int q = 0; q < nnear; ++q) {
+                        const int2 nt = s_near[q][tid];
+                        d3 a, b, c;
+                        load_soup(soup, nt.x, a, b, c);
+                        int r64;
+                        const double e2 = ericson(Pc, a, b, c, &r64);
+                        ++evals64;
+                        if (e2 < best_band || (e2 == best_band && nt.x < bt64)) {
+                            best_band = e2;
+                            bt64 = nt.x;
+                            br64 = r64;
+                        }
+                    }
+                }
+                inband = valid && (over || nnear == 0);
+            } else {
+                inband = valid && d32 <= band_cells * static_cast<float>(g.h) + eb;
+            }
             if (__any_sync(0xffffffffu, inband) && lane == 0) s_band = 1;
             __syncthreads();
             if (s_band) {
@@ -633,12 +713,15 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
             const int64_t idx = s.vox_begin + (static_cast<int64_t>(z - g.z0) * g.ny + y) * g.nx + x;
             if (PREC == kPrecFP64) {
                 write_cell(o, idx, __dsqrt_rn(best64), bt, br);
+            } else if (EXACT) {
+                if (inband) ++bandc;
+                write_cell(o, idx, __dsqrt_rn(best_band), bt64, br64);
             } else if (inband) {
                 ++bandc;
                 write_cell(o, idx, __dsqrt_rn(best_band), bt64, br64);
                 if (o.errbound) o.errbound[idx] = 0.f;
             } else {
-                if (PREC == kPrecMixed && !STAGE && br < 0 && o.near_reg) {
+                if (MIX && !STAGE && br < 0 && o.near_reg) {
                     // the region of the nearest triangle: its distance again, recentred
                     // exactly as the filter recentred it (the same value, now with the
                     // region)
@@ -707,6 +790,8 @@ int sdf_sub_grid(int precision, bool stage, int ctas) {
     if (precision == kPrecMixed && stage) per = resident_ctas<kPrecMixed, true, 12>();
     else if (precision == kPrecMixed) per = hi ? resident_ctas<kPrecMixed, false, 16>()
                                                : resident_ctas<kPrecMixed, false, 12>();
+    else if (precision == kPrecExact) per = hi ? resident_ctas<kPrecExact, false, 16>()
+                                               : resident_ctas<kPrecExact, false, 12>();
     else per = hi ? resident_ctas<kPrecFP64, false, 16>() : resident_ctas<kPrecFP64, false, 12>();
     return sms * per;
 }
@@ -731,6 +816,7 @@ void launch_sdf_sub(int precision, bool stage, int grab, int probe, int ctas, co
     };
     if (precision == kPrecMixed && stage) go(k_sdf_sub<kPrecMixed, true, 12>);
     else if (precision == kPrecMixed) hi ? go(k_sdf_sub<kPrecMixed, false, 16>) : go(k_sdf_sub<kPrecMixed, false, 12>);
+    else if (precision == kPrecExact) hi ? go(k_sdf_sub<kPrecExact, false, 16>) : go(k_sdf_sub<kPrecExact, false, 12>);
     else hi ? go(k_sdf_sub<kPrecFP64, false, 16>) : go(k_sdf_sub<kPrecFP64, false, 12>);
     CMG_LAUNCH();
 }

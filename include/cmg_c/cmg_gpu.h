@@ -26,8 +26,13 @@ extern "C" {
 #define CMG_OUT_ERROR_BOUND 16 /* mixed precision: stated per-cell bound (float) */
 
 /* Distance arithmetic. */
-#define CMG_PREC_FP64 0   /* all FP64, reference operation order: bit-identical */
+#define CMG_PREC_FP64 0   /* FP64 distances in the reference's operation order,
+                             bit-identical to the reference: on 16^3 bricks an FP32 pass
+                             with a stated error bound finds each cell's near-ties, whose
+                             FP64 distances give the FP64 minimum */
 #define CMG_PREC_MIXED 1  /* FP32 on brick-recentred coordinates + FP64 band */
+#define CMG_PREC_FP64_PLAIN 2 /* the same results as CMG_PREC_FP64 with every
+                                 candidate evaluated in FP64 (for comparison) */
 
 /* Predicate semantics for occupancy. */
 #define CMG_PRED_COMPAT 0 /* the reference as initialised: sign of the rounded

@@ -101,9 +101,12 @@ def test_sdf64_matches_reference_distance(cm, golden, name):
     assert np.all(np.signbit(r.sdf64[occ])) and not np.any(np.signbit(r.sdf64[~occ]))
 
 
-@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "shsphere64_r30p1", "boxtorus64_facegrid"])
+@pytest.mark.parametrize("name", ["icosphere_s3_r58p3", "shsphere64_r30p1", "boxtorus64_facegrid",
+                                  "cube4deg_r16p1", "uvsphere16_r20p1"])
 @pytest.mark.parametrize("brick", [4, 8, 16])
 def test_mixed_precision_error(cm, golden, name, brick):
+    # cube4deg_r16p1 holds a zero-area facet of exactly collinear dyadic points,
+    # uvsphere16_r20p1 slivers at its poles
     g = golden(name)
     plain = _run(cm, g, name, outputs=cm.OUT_SDF_F64, brick=brick)
     mixed = _run(cm, g, name, outputs=cm.OUT_SDF_F64 | cm.OUT_ERROR_BOUND,
