@@ -39,10 +39,11 @@ using namespace sdf;
 
 constexpr int kSub = 4;          // sub-brick edge (cells)
 constexpr int kSubThreads = 64;  // one cell per thread
-// filtered candidates per round in shared memory (STAGE: their records as well)
-template <bool STAGE>
+// filtered candidates per round in shared memory (STAGE: their records as well; the
+// exact path, whose near-tie slots take 3 KB, 256: 16 CTAs per SM still fit)
+template <int PREC, bool STAGE>
 struct Cap {
-    static constexpr int value = STAGE ? 256 : 384;
+    static constexpr int value = STAGE || PREC == kPrecExact ? 256 : 384;
 };
 // mixed path: filtered entries per need-mask chunk (one bit per entry); the records a
 // warp needs in a chunk are staged in its own shared-memory slots
@@ -176,7 +177,7 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
           Out o, Stats* __restrict__ st) {
     constexpr bool MIX = PREC != kPrecFP64;     // the FP32 pass (mixed or exact)
     constexpr bool EXACT = PREC == kPrecExact;  // ... refined to the FP64 minimum everywhere
-    constexpr int kCap = Cap<STAGE>::value;
+    constexpr int kCap = Cap<PREC, STAGE>::value;
     // exact path: per cell, its near-ties (triangle, FP32 squared distance), slot-major
     __shared__ int2 s_near[EXACT ? kNear : 1][kSubThreads];
     __shared__ float4 s_c[kCap];  // centroid relative to the sub-brick centre, radius
