@@ -52,6 +52,15 @@ def test_exact_equals_plain_on_the_headline_grid(cm, golden):
     assert 0 < exact.stats["band_cells"] < exact.stats["cells"] // 10
 
 
+def test_exact_equals_plain_on_the_ellipsoid_field(cm):
+    """2000 small ellipsoids (2.56M triangles) at resolution 254 pad 1: cells mostly far
+    from every surface, whose near-ties come from neighbouring bodies."""
+    from cybermeshgenerator_gb300 import workloads as W
+    pts, tris = W.ellipsoid_field()
+    exact, plain = _both(cm, cm.PLC.from_arrays(pts, tris), resolution=254, pad=1)
+    assert exact.stats["fp64_evaluations"] * 20 < plain.stats["evaluations"]
+
+
 def test_exact_equals_plain_on_the_box_torus_face_grid(cm, golden):
     z = golden("boxtorus512")
     grid = (z["facegrid_corner"], float(z["facegrid_spacing"]), z["facegrid_dims"])
