@@ -70,13 +70,17 @@ def workload():
 
 
 def kernel_source_sha(files=("sdf_sub.cu", "cmg_sdf.cuh")):
-    """SHA-256 (16 hex digits) of the evaluation kernel's sources, recorded in its ncu
-    summary so that the bench line takes DRAM traffic only from a capture of this code."""
+    """SHA-256 (16 hex digits) of the evaluation kernel's code (the sources with their
+    // comments and blank lines taken out), recorded in its ncu summary so that the bench
+    line takes DRAM traffic only from a capture of this code."""
     import hashlib
     h = hashlib.sha256()
     for f in files:
-        with open(os.path.join(ROOT, "cybermeshgenerator_gb300", "csrc", f), "rb") as fh:
-            h.update(fh.read())
+        with open(os.path.join(ROOT, "cybermeshgenerator_gb300", "csrc", f), encoding="utf-8") as fh:
+            for line in fh:
+                code = line.split("//", 1)[0].rstrip()
+                if code:
+                    h.update(code.encode() + b"\n")
     return h.hexdigest()[:16]
 
 

@@ -16,6 +16,9 @@
 //   4. mixed only: cells within `band` cells of the surface are re-evaluated in FP64
 //      over the triangles whose FP32 distance is within twice the stated bound of
 //      the FP32 best, which gives the FP64 minimum exactly there.
+// The exact FP64 path (kPrecExact) is the mixed kernel with bounds widened to every
+// such near-tie, the near-ties kept per cell as the FP32 pass meets them, and the FP64
+// distance over them for every cell (step 4 only for cells with too many near-ties).
 // Centroids are stored as FP32 hi + lo pairs relative to the grid corner, so the
 // centroid-to-centre differences are formed in FP32 without losing the low bits
 // (the sub-brick recentring).
@@ -159,7 +162,7 @@ __device__ __forceinline__ SubGeo sub_geo(const MeshSeg& s, int64_t lb, int sub)
     return q;
 }
 
-// PREC: kPrecMixed or kPrecFP64. STAGE (mixed only): copy the records of the
+// PREC: kPrecMixed, kPrecExact or kPrecFP64. STAGE (mixed only): copy the records of the
 // filtered candidates into shared memory (cp.async) instead of reading them
 // from L1/L2 at evaluation time. MINB: resident CTAs per SM the registers are
 // budgeted for (12: 80 registers; 16: 64). grab: consecutive sub-bricks taken from
