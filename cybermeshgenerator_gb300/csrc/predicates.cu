@@ -76,15 +76,18 @@ __device__ __forceinline__ float amax3(float a, float b, float c) {
 // FP64 -> FP32 by truncating the significand, on the integer pipe (the hardware
 // conversion is far slower on this part): |f - x| < 2^-23 |x|. Zero maps to zero;
 // values outside the FP32 normal range, subnormals, infinities and NaN set ok = false.
+// The FP64 fields shifted left by 3 (a funnel shift of hi:lo) put the exponent's low 9
+// bits over the FP32 exponent and the top 23 significand bits over the FP32 significand;
+// adding 128 to that 9-bit field turns e64 mod 512 into e64 - 896 = e32 for every
+// exponent of the FP32 normal range (e64 in [897, 1150]), with the 9th bit clear.
 __device__ __forceinline__ float trunc32(double x, bool& ok) {
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
-    const int e = static_cast<int>((hi >> 20) & 0x7ffu) - 1023 + 127;
-    const bool zero = (b << 1) == 0ull;
-    ok = ok && (zero || (e >= 1 && e <= 254));
-    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned bits = (hi & 0x80000000u) | (zero ? 0u : ((static_cast<unsigned>(e) << 23) | m));
-    return __uint_as_float(bits);
+    const unsigned hi = static_cast<unsigned>(__double2hiint(x));
+    const unsigned lo = static_cast<unsigned>(__double2loint(x));
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    const bool zero = ((hi << 1) | lo) == 0u;
+    ok = ok && (zero || e - 897u <= 253u);
+    const unsigned r = __funnelshift_l(lo, hi, 3) + (128u << 23);
+    return __uint_as_float(zero ? (hi & 0x80000000u) : (r | (hi & 0x80000000u)));
 }
 
 // FP32 orient3d: certified sign (+1/-1) or 0 when the bound does not decide.
