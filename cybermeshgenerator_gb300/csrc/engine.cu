@@ -223,6 +223,7 @@ struct Batch::Impl {
     int64_t* col_off = nullptr;
     int64_t* flagged = nullptr;
     int64_t* scan_tmp = nullptr;
+    int64_t* scan_tmp_side = nullptr;  // the SDF preparation's, on the second stream
     uint8_t* occ_internal = nullptr;
     int* col_list = nullptr;
     double* hs = nullptr;
@@ -331,6 +332,7 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
         impl_->scan_tmp = carve<int64_t>(A, scan_tmp_elems(smax));
         if (!opts_.want_occ) impl_->occ_internal = carve<uint8_t>(A, nvox_);
         if (sdf) {
+            impl_->scan_tmp_side = carve<int64_t>(A, scan_tmp_elems(smax));
             impl_->tinfo = carve<float4>(A, ntris_);
             impl_->tinfo_lo = carve<float4>(A, ntris_);
             impl_->tnorm = carve<float4>(A, ntris_);
@@ -404,11 +406,22 @@ Batch::Batch(const std::vector<HostMesh>& meshes, const VoxOpts& opts, cudaStrea
     if (opts_.stage < 0) opts_.stage = 0;
     if (brick == 16) impl_->grid_eval = sdf ? sdf_sub_grid(sub_precision(opts_), opts_.stage != 0, opts_.ctas) : sms;
     else impl_->grid_eval = (brick == 4 ? 8 : 3) * sms;
+    if (sdf) {  // made here: a graph capture must not create them
+        CMG_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+        CMG_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+        CMG_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
+    }
 }
 
 Batch::~Batch() {
     for (cudaEvent_t& e : ev_)
         if (e) cudaEventDestroy(e);
+    if (fork_) cudaEventDestroy(fork_);
+    if (join_) cudaEventDestroy(join_);
+    if (side_) {
+        if (side_open_) cudaStreamSynchronize(side_);  // pooled arenas are reused next
+        cudaStreamDestroy(side_);
+    }
     if (graph_) cudaGraphExecDestroy(graph_);
     if (impl_ && impl_->graph) cudaGraphDestroy(impl_->graph);
 }
@@ -477,15 +490,23 @@ void Batch::run_impl(bool sizing) {
     const bool timed = timing_ && cap == cudaStreamCaptureStatusNone;
     if (timed && !ev_[0])
         for (cudaEvent_t& e : ev_) CMG_CUDA(cudaEventCreate(&e));
+    if (side_open_) {
+        CMG_CUDA(cudaStreamSynchronize(side_));
+        side_open_ = false;
+    }
     if (timed) CMG_CUDA(cudaEventRecord(ev_[0], st));
 
     CMG_CUDA(cudaMemsetAsync(stats_, 0, sizeof(Stats), st));
     launch_tri_prep(dsegs_, nseg, ntris_, pts_, tris_, I.soup, I.xybox, I.pairs_n, st);
-    exclusive_scan(I.pairs_n, I.pair_off, ntris_, I.scan_tmp, st);
-    if (sizing) {
+
+    // Ray-parity occupancy: (triangle, column) pairs, filter, exact pass. The pair count
+    // sizes the pair arena in a sizing run.
+    auto occ_head = [&](cudaStream_t s) {
+        exclusive_scan(I.pairs_n, I.pair_off, ntris_, I.scan_tmp, s);
+        if (!sizing) return;
         int64_t P = 0;
-        CMG_CUDA(cudaMemcpyAsync(&P, I.pair_off + ntris_, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CMG_CUDA(cudaStreamSynchronize(st));
+        CMG_CUDA(cudaMemcpyAsync(&P, I.pair_off + ntris_, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        CMG_CUDA(cudaStreamSynchronize(s));
         Arena& B = I.pairs;
         auto planb = [&]() {
             B.reset();
@@ -500,48 +521,58 @@ void Batch::run_impl(bool sizing) {
             planb();
         }
         pairs_cap_ = P;
-    }
-    const int pair_grid = 4 * device_sms();
-    CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), st));
-    launch_col_pairs(false, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, nullptr, nullptr,
-                     pair_grid, st);
-    exclusive_scan(I.colcnt, I.col_off, ncol_, I.scan_tmp, st);
-    CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), st));
-    launch_col_pairs(true, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, I.col_off,
-                     I.col_list, pair_grid, st);
-    launch_occ_filter(opts_.predicates, dsegs_, nseg, nrow_, I.soup, I.col_off, I.col_list, occ,
-                      I.flagged, stats_, st);
-    launch_occ_exact(opts_.predicates, dsegs_, nseg, I.soup, I.col_off, I.col_list, I.flagged,
-                     I.hs, I.hv, occ, stats_, I.grid_exact, st);
-    if (timed) CMG_CUDA(cudaEventRecord(ev_[1], st));
+    };
+    auto occ_tail = [&](cudaStream_t s) {
+        const int pair_grid = 4 * device_sms();
+        CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), s));
+        launch_col_pairs(false, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, nullptr, nullptr,
+                         pair_grid, s);
+        exclusive_scan(I.colcnt, I.col_off, ncol_, I.scan_tmp, s);
+        CMG_CUDA(cudaMemsetAsync(I.colcnt, 0, sizeof(int) * std::max<int64_t>(ncol_, 1), s));
+        launch_col_pairs(true, dsegs_, nseg, ntris_, I.xybox, I.pair_off, I.colcnt, I.col_off,
+                         I.col_list, pair_grid, s);
+        launch_occ_filter(opts_.predicates, dsegs_, nseg, nrow_, I.soup, I.col_off, I.col_list, occ,
+                          I.flagged, stats_, s);
+        launch_occ_exact(opts_.predicates, dsegs_, nseg, I.soup, I.col_off, I.col_list, I.flagged,
+                         I.hs, I.hv, occ, stats_, I.grid_exact, s);
+        if (timed) CMG_CUDA(cudaEventRecord(ev_[1], s));
+    };
     if (!sdf) {
-        if (timed) {
-            CMG_CUDA(cudaEventRecord(ev_[2], st));
-            CMG_CUDA(cudaEventRecord(ev_[3], st));
-        }
+        occ_head(st);
+        occ_tail(st);
+        if (timed)
+            for (int e : {4, 5, 2, 3}) CMG_CUDA(cudaEventRecord(ev_[e], st));
         return;
     }
 
-    CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
-    CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, st));
-    CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 3 * nseg, st));
-    launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tnorm, I.tlo, I.thi,
-                        I.tbin, I.bincnt, I.large_cnt, I.emax_bits, st);
-    exclusive_scan(I.bincnt, I.bin_off, nbrick_, I.scan_tmp, st);
-    exclusive_scan(I.large_cnt, I.large_off, nseg, I.scan_tmp, st);
-    launch_seg_finish(dsegs_, nseg, I.large_off, I.emax_bits, st);
-    CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, st));
-    CMG_CUDA(cudaMemsetAsync(I.large_cnt + nseg, 0, sizeof(int) * nseg, st));
-    launch_bin_fill(ntris_, I.tbin, I.bin_off, I.bincnt, I.bin_list, dsegs_, nseg,
-                    I.large_cnt + nseg, I.large_list, st);
-    launch_brick_walk(false, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
-                      I.bin_list, I.large_list, I.bound, I.cand_cnt, nullptr, nullptr, nullptr,
-                      stats_, opts_.walk_warps, st);
-    exclusive_scan(I.cand_cnt, I.cand_off, nbrick_, I.scan_tmp, st);
-    if (sizing) {
+    // SDF preparation: triangle bins, brick walk (candidate lists), work order. It reads
+    // the soup, never the occupancy, so it runs on the second stream beside the
+    // occupancy passes. The candidate count sizes the candidate arena in a sizing run.
+    cudaStream_t ss = side_;
+    int64_t* tmp = I.scan_tmp_side;
+    auto prep_head = [&]() {
+        if (timed) CMG_CUDA(cudaEventRecord(ev_[4], ss));
+        CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, ss));
+        CMG_CUDA(cudaMemsetAsync(I.large_cnt, 0, sizeof(int) * 2 * nseg, ss));
+        CMG_CUDA(cudaMemsetAsync(I.emax_bits, 0, sizeof(unsigned) * 3 * nseg, ss));
+        launch_sdf_tri_prep(dsegs_, nseg, ntris_, I.soup, I.tinfo, I.tinfo_lo, I.trec, I.tnorm, I.tlo,
+                            I.thi, I.tbin, I.bincnt, I.large_cnt, I.emax_bits, ss);
+        exclusive_scan(I.bincnt, I.bin_off, nbrick_, tmp, ss);
+        exclusive_scan(I.large_cnt, I.large_off, nseg, tmp, ss);
+        launch_seg_finish(dsegs_, nseg, I.large_off, I.emax_bits, ss);
+        CMG_CUDA(cudaMemsetAsync(I.bincnt, 0, sizeof(int) * nbrick_, ss));
+        CMG_CUDA(cudaMemsetAsync(I.large_cnt + nseg, 0, sizeof(int) * nseg, ss));
+        launch_bin_fill(ntris_, I.tbin, I.bin_off, I.bincnt, I.bin_list, dsegs_, nseg,
+                        I.large_cnt + nseg, I.large_list, ss);
+        launch_brick_walk(false, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
+                          I.bin_list, I.large_list, I.bound, I.cand_cnt, nullptr, nullptr, nullptr,
+                          stats_, opts_.walk_warps, ss);
+        exclusive_scan(I.cand_cnt, I.cand_off, nbrick_, tmp, ss);
+    };
+    auto prep_size = [&]() {
         int64_t C = 0;
-        CMG_CUDA(cudaMemcpyAsync(&C, I.cand_off + nbrick_, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CMG_CUDA(cudaStreamSynchronize(st));
+        CMG_CUDA(cudaMemcpyAsync(&C, I.cand_off + nbrick_, sizeof(int64_t), cudaMemcpyDeviceToHost, ss));
+        CMG_CUDA(cudaStreamSynchronize(ss));
         Arena& Cn = I.cands;
         auto planc = [&]() {
             Cn.reset();
@@ -554,14 +585,34 @@ void Batch::run_impl(bool sizing) {
             planc();
         }
         cand_cap_ = C;
+    };
+    auto prep_tail = [&]() {
+        launch_brick_walk(true, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
+                          I.bin_list, I.large_list, I.bound, I.cand_cnt, I.cand_off, I.cand,
+                          I.brick_emax, stats_, opts_.walk_warps, ss);
+        if (opts_.brick == 16) launch_sub_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, ss);
+        else launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, ss);
+        radix_sort_pairs(I.work_keys, I.work, nwork_, 32, I.sort_tmp, ss);
+        CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), ss));
+        if (timed) CMG_CUDA(cudaEventRecord(ev_[5], ss));
+    };
+
+    // The longer preparation is issued first. In a sizing run each arena is re-planned
+    // while the other stream's passes, which do not touch it, keep the device busy.
+    CMG_CUDA(cudaEventRecord(fork_, st));
+    CMG_CUDA(cudaStreamWaitEvent(ss, fork_, 0));
+    side_open_ = true;
+    prep_head();
+    occ_head(st);
+    if (!sizing) prep_tail();
+    occ_tail(st);
+    if (sizing) {
+        prep_size();
+        prep_tail();
     }
-    launch_brick_walk(true, dsegs_, nseg, nbrick_, I.soup, I.tinfo, I.tlo, I.thi, I.bin_off,
-                      I.bin_list, I.large_list, I.bound, I.cand_cnt, I.cand_off, I.cand,
-                      I.brick_emax, stats_, opts_.walk_warps, st);
-    if (opts_.brick == 16) launch_sub_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
-    else launch_work_keys(I.cand_cnt, nbrick_, I.work_keys, I.work, st);
-    radix_sort_pairs(I.work_keys, I.work, nwork_, 32, I.sort_tmp, st);
-    CMG_CUDA(cudaMemsetAsync(queue_, 0, sizeof(unsigned long long), st));
+    CMG_CUDA(cudaEventRecord(join_, ss));
+    CMG_CUDA(cudaStreamWaitEvent(st, join_, 0));
+    side_open_ = false;
     if (timed) CMG_CUDA(cudaEventRecord(ev_[2], st));
     if (opts_.brick == 16)
         launch_sdf_sub(sub_precision(opts_), opts_.stage != 0, opts_.grab, opts_.probe, opts_.ctas, dsegs_,
@@ -580,7 +631,7 @@ Timing Batch::timing() {
     if (!ev_[0]) return t;
     CMG_CUDA(cudaEventSynchronize(ev_[3]));
     CMG_CUDA(cudaEventElapsedTime(&t.occupancy_ms, ev_[0], ev_[1]));
-    CMG_CUDA(cudaEventElapsedTime(&t.sdf_prep_ms, ev_[1], ev_[2]));
+    CMG_CUDA(cudaEventElapsedTime(&t.sdf_prep_ms, ev_[4], ev_[5]));
     CMG_CUDA(cudaEventElapsedTime(&t.eval_ms, ev_[2], ev_[3]));
     CMG_CUDA(cudaEventElapsedTime(&t.total_ms, ev_[0], ev_[3]));
     return t;

@@ -115,7 +115,9 @@ struct HostResult {
     HostBuf<float> err;
 };
 
-// Phase times of the last run(), from CUDA events on the batch's stream.
+// Phase times of the last run(), from CUDA events on the batch's streams. The SDF
+// preparation overlaps the occupancy passes (a second stream), so the phases can
+// sum to more than the total.
 struct Timing {
     float occupancy_ms = 0.f;  // triangle prep .. exact pass
     float sdf_prep_ms = 0.f;   // bins, candidate lists, work order
@@ -226,7 +228,15 @@ private:
     cudaGraphExec_t graph_ = nullptr;
     int64_t h2d_bytes_ = 0;
     bool timing_ = false;
-    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+    // step start, occupancy done, evaluation start, step end, SDF preparation start / end
+    cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // The SDF preparation needs the triangle soup but not the occupancy, so it runs on
+    // a second stream beside the occupancy passes and joins before the evaluation.
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    // work on side_ not yet joined (a run that threw between fork and join): the next
+    // run and the destructor wait for it before the buffers are used again
+    bool side_open_ = false;
     void run_impl(bool sizing);
     bool needs_sizing() const { return pairs_cap_ < 0 || cand_cap_ < 0 || resize_; }
     void sized_run();

@@ -214,7 +214,9 @@ int64_t cmg_batch_cells(const cmg_batch*);
 void cmg_batch_destroy(cmg_batch*);
 
 /* ---- measurement ---------------------------------------------------------- */
-/* Phase times of a batch's last run (CUDA events on its stream), once enabled. */
+/* Phase times of a batch's last run (CUDA events on its streams), once enabled. The
+   SDF preparation runs on a second stream beside the occupancy passes, so the phases
+   can sum to more than total_ms. */
 typedef struct cmg_batch_timing {
     float occupancy_ms; /* triangle prep .. exact pass */
     float sdf_prep_ms;  /* triangle bins, brick candidate lists, work order */

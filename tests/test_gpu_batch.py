@@ -70,6 +70,29 @@ def test_batch_graph_replay_equals_eager(cm, c4, mixed_batch):
         assert np.array_equal(r0.sdf32, r1.sdf32)
 
 
+def test_batch_overlapped_phases_equal_the_sizing_pass(cm, c4, mixed_batch):
+    """The SDF preparation runs on a second stream beside the occupancy passes, in the
+    sizing pass (arenas re-planned between the two streams' halves) and in later runs:
+    eager runs after the sizing pass give the same outputs, the timed phases are all
+    recorded and the evaluation starts after both phases end."""
+    ref = cm.Batch(c4["plcs"][:64], c4["res"][:64], c4["pads"][:64],
+                   outputs=cm.OUT_OCCUPANCY | cm.OUT_SDF_F32, precision=cm.PREC_MIXED)
+    ref.run().sync()
+    sized = [ref.result(i) for i in range(0, 64, 9)]
+    ref.set_timing(True)
+    for _ in range(3):
+        ref.run()
+    ref.sync()
+    t = ref.timing()
+    for i, r0 in zip(range(0, 64, 9), sized):
+        r1 = ref.result(i)
+        assert np.array_equal(r0.occupancy, r1.occupancy)
+        assert np.array_equal(r0.sdf32, r1.sdf32)
+    assert all(t[k] > 0 for k in ("occupancy_ms", "sdf_prep_ms", "eval_ms", "total_ms")), t
+    assert t["eval_ms"] < t["total_ms"]
+    assert max(t["occupancy_ms"], t["sdf_prep_ms"]) + t["eval_ms"] <= t["total_ms"] * 1.01, t
+
+
 def test_fp64_batch_bit_exact_and_equals_single_calls(cm, orc, c4):
     """A plain FP64 batch of every 16th mesh: FP64 distances equal the oracle's
     brute-force minimum bit for bit on sampled cells, and each mesh's outputs equal
