@@ -43,10 +43,12 @@ using namespace sdf;
 constexpr int kSub = 4;          // sub-brick edge (cells)
 constexpr int kSubThreads = 64;  // one cell per thread
 // filtered candidates per round in shared memory (STAGE: their records as well; the
-// exact path, whose near-tie slots take 3 KB, 256: 16 CTAs per SM still fit)
+// exact path, whose near-tie slots take 3 KB, 256). The mixed path's 296 keeps its
+// shared memory (13.3 KB, plus the 1 KB the SM reserves per CTA) within 1/16 of the
+// SM's 228 KB, so that 16 CTAs are resident; at least one filter step (kBatch x 64).
 template <int PREC, bool STAGE>
 struct Cap {
-    static constexpr int value = STAGE || PREC == kPrecExact ? 256 : 384;
+    static constexpr int value = STAGE || PREC == kPrecExact ? 256 : 296;
 };
 // mixed path: filtered entries per need-mask chunk (one bit per entry); the records a
 // warp needs in a chunk are staged in its own shared-memory slots
@@ -77,6 +79,35 @@ __device__ __forceinline__ float reach_term(float w, float r) {
 }
 __device__ __forceinline__ float reach(float b, float term) {
     return __fmaf_ru(b, 1.f + 20.f * kU32, term);
+}
+
+// The mixed path's sphere test in expanded form: 4 FMAs and a compare per entry. For a
+// cell p (|p| <= r (1 + 2u), r the sub-brick radius) and an entry c with the reach L = reach(b,
+// term) above, let
+//   T = RU(term (1 + 51u) + RU(0.002 r + 1e-18))   per entry (exp_term),
+//   G = RN(|c|^2 - T^2)                             per entry (exp_g),
+//   B = RU(b (1 + 71u)), K = RN(B^2 - |p|^2)        per cell and chunk,
+// so that B + T >= L (1 + 50u) + 0.002 r. The test
+//   fma(-2p, c) + (-2B) T + G <= K,               i.e. |p - c|^2 <= (B + T)^2 expanded,
+// is passed by every entry with |p - c| <= L: its rounding error (four FMA roundings,
+// G's and K's) is at most 20.1u (R + r)^2 <= 40.2u (R^2 + r^2), R = B + T, while
+// R^2 - L^2 >= (R - L) R >= (50u R^2 + 0.002 r R) / (1 + 50u), which exceeds it because
+// R >= 0.002 r and 0.002^2 > 40.2u (the 1e-18 keeps R^2 above FP32's underflow error).
+// The entries store c' = -2c (exact), so the dot product is fma(p, c') and the offsets
+// p - c and w - c are fma(0.5, c', p), bit for bit the subtractions. Conversely an
+// entry that passes has |p - c| <= (R + 0.00155 r)(1 + 21u) (exp_pass_reach).
+__device__ __forceinline__ float exp_term(float term, float sr) {
+    return __fmaf_ru(term, 1.f + 51.f * kU32, sr);
+}
+__device__ __forceinline__ float exp_sr(float r) { return __fmaf_ru(0.002f, r, 1e-18f); }
+__device__ __forceinline__ float exp_g(float cx, float cy, float cz, float t) {
+    return fmaf(-t, t, fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
+}
+__device__ __forceinline__ float exp_b(float b) { return __fmul_ru(b, 1.f + 71.f * kU32); }
+// Largest distance from the centroid of a cell whose expanded test passes, for the
+// cell's B (at most bmax's) and the entry's T; sw = RU(0.0016 r).
+__device__ __forceinline__ float exp_pass_reach(float bb, float t, float sw) {
+    return __fmaf_ru(__fadd_ru(bb, t), 1.f + 21.f * kU32, sw);
 }
 
 // A cell's bound in the mixed path, from its smallest FP32 squared distance so far, d2:
@@ -121,7 +152,8 @@ __device__ __forceinline__ float plane_reach(float b, float nerr, float ebr4) {
 // (wr an upper bound, rounded up), and a cell's test passes only when the cell is
 // within lim (1 + 4u) of the centroid (the test's own rounding), lim = reach(b, term) at
 // most lim_max = reach(bmax, term) for the warp's largest bound bmax (reach grows with
-// b). So the centre is within (lim_max + wr)(1 + 4u) of the centroid, and the squared
+// b); in the expanded form only within lim_max = exp_pass_reach(exp_b(bmax), T, sw).
+// So the centre is within (lim_max + wr)(1 + 4u) of the centroid, and the squared
 // distance computed from the centre (relative rounding within 7u) stays below the
 // square of RU(RU(lim_max + wr)(1 + 16u)) rounded to nearest.
 __device__ __forceinline__ float warp_reach(float lim_max, float wr) {
@@ -180,10 +212,13 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
           Out o, Stats* __restrict__ st) {
     constexpr bool MIX = PREC != kPrecFP64;     // the FP32 pass (mixed or exact)
     constexpr bool EXACT = PREC == kPrecExact;  // ... refined to the FP64 minimum everywhere
+    constexpr bool EXPAND = PREC == kPrecMixed && !STAGE;  // expanded sphere tests (exp_*)
     constexpr int kCap = Cap<PREC, STAGE>::value;
+    static_assert(kCap >= kBatch * kSubThreads, "a round must hold one filter step");
     // exact path: per cell, its near-ties (triangle, FP32 squared distance), slot-major
     __shared__ int2 s_near[EXACT ? kNear : 1][kSubThreads];
     __shared__ float4 s_c[kCap];  // centroid relative to the sub-brick centre, radius
+    __shared__ float s_g[EXPAND ? kCap : 1];  // EXPAND: exp_g of the entry
     // FP64 path: unit normal and plane offset n . centroid, and a bound on the error of
     // the plane distances computed from them
     __shared__ float4 s_nrm[PREC == kPrecFP64 ? kCap : 1];
@@ -233,6 +268,9 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
         const float px = static_cast<float>((x + 0.5) * g.h - ckx);
         const float py = static_cast<float>((y + 0.5) * g.h - cky);
         const float pz = static_cast<float>((z + 0.5) * g.h - ckz);
+        // EXPAND: |p|^2, the entries' radius margin (exp_sr) and the warp test's (exp_pass_reach)
+        const float p2 = EXPAND ? fmaf(px, px, fmaf(py, py, pz * pz)) : 0.f;
+        const float sr = EXPAND ? exp_sr(r4) : 0.f, sw = EXPAND ? __fmul_ru(0.0016f, r4) : 0.f;
         const int64_t c0 = cand_off[gb], c1 = cand_off[gb + 1];
         if (MIX && !STAGE) {
             // the warp's sphere for the chunk pre-test: centre at the middle of the box of
@@ -421,7 +459,15 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     base = __shfl_sync(0xffffffffu, base, 0);
                     if (take) {
                         const int pos = base + __popc(m & ((1u << lane) - 1u));
-                        if (MIX && !STAGE) e.w = reach_term(e.w, r4);
+                        if (EXPAND) {
+                            e.w = exp_term(reach_term(e.w, r4), sr);
+                            s_g[pos] = exp_g(e.x, e.y, e.z, e.w);
+                            e.x *= -2.f;
+                            e.y *= -2.f;
+                            e.z *= -2.f;
+                        } else if (MIX && !STAGE) {
+                            e.w = reach_term(e.w, r4);
+                        }
                         s_c[pos] = e;
                         if (PREC == kPrecFP64) {
                             s_nrm[pos] = nv;
@@ -445,7 +491,9 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
             if (MIX && !STAGE) {
                 // In chunks of kChunk entries: each lane marks the entries its cell may
                 // need under its bound at the start of the chunk (s_c[].w holds the
-                // radius term of the reach, see reach_term); the warp stages the records
+                // radius term of the reach, see reach_term; EXPAND: the widened term T of
+                // the expanded test, with -2 x the centroid in s_c[].xyz and exp_g in
+                // s_g, see exp_term); the warp stages the records
                 // of the union into its shared slots (lane k loads entry k's record:
                 // every load of the chunk in flight at once) and evaluates every marked
                 // entry. The bound only shrinks and the test admits at least what the
@@ -465,13 +513,41 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                     if (lane < cnt) {
                         const float4 ws = s_wsph[warp];
                         const float4 e = s_c[j0 + lane];
-                        const float dx = ws.x - e.x, dy = ws.y - e.y, dz = ws.z - e.z;
-                        const float lw = warp_reach(reach(bmax, e.w), ws.w);
+                        float dx, dy, dz, lw;
+                        if (EXPAND) {
+                            dx = fmaf(0.5f, e.x, ws.x);
+                            dy = fmaf(0.5f, e.y, ws.y);
+                            dz = fmaf(0.5f, e.z, ws.z);
+                            lw = warp_reach(exp_pass_reach(exp_b(bmax), e.w, sw), ws.w);
+                        } else {
+                            dx = ws.x - e.x;
+                            dy = ws.y - e.y;
+                            dz = ws.z - e.z;
+                            lw = warp_reach(reach(bmax, e.w), ws.w);
+                        }
                         pass = dx * dx + dy * dy + dz * dz <= lw * lw;
                     }
                     const unsigned cand = __ballot_sync(0xffffffffu, pass);
                     unsigned mine = 0;
-                    if (valid) {
+                    if (valid && EXPAND) {
+                        const float bb = exp_b(bestd);
+                        const float kk = fmaf(bb, bb, -p2), mb = -2.f * bb;
+                        if (cnt == kChunk && __popc(cand) >= kDenseChunk) {
+#pragma unroll
+                            for (int k = 0; k < kChunk; ++k) {
+                                const float4 e = s_c[j0 + k];
+                                const float a = fmaf(px, e.x, fmaf(py, e.y, fmaf(pz, e.z, fmaf(mb, e.w, s_g[j0 + k]))));
+                                if (a <= kk) mine |= 1u << k;
+                            }
+                        } else {
+                            for (unsigned m = cand; m; m &= m - 1u) {
+                                const int k = __ffs(m) - 1;
+                                const float4 e = s_c[j0 + k];
+                                const float a = fmaf(px, e.x, fmaf(py, e.y, fmaf(pz, e.z, fmaf(mb, e.w, s_g[j0 + k]))));
+                                if (a <= kk) mine |= 1u << k;
+                            }
+                        }
+                    } else if (valid) {
                         const float bl = bestd;
                         if (cnt == kChunk && __popc(cand) >= kDenseChunk) {
                             // most entries passed: every entry, unrolled (the entries that
@@ -511,7 +587,9 @@ k_sdf_sub(const MeshSeg* __restrict__ segs, int nseg, const uint32_t* __restrict
                         const int k = __ffs(m) - 1;
                         m &= m - 1u;
                         const float4 e = s_c[j0 + k];
-                        const float dx = px - e.x, dy = py - e.y, dz = pz - e.z;
+                        const float dx = EXPAND ? fmaf(0.5f, e.x, px) : px - e.x;
+                        const float dy = EXPAND ? fmaf(0.5f, e.y, py) : py - e.y;
+                        const float dz = EXPAND ? fmaf(0.5f, e.z, pz) : pz - e.z;
                         // the plane: a triangle is no nearer than the plane of its frame
                         // (every triangle, degenerate or not, lies in one), so a marked
                         // triangle whose plane lies beyond every lane's bound is skipped
