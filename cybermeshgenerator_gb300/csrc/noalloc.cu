@@ -11,9 +11,10 @@
 // holds that array until the process exits.
 //
 // Set-up: the first call on a device resolves the array's device address with
-// cudaGetSymbolAddress, with that device current; make that first call before any
-// stream capture. Every call reads two sizes back from the device and waits for
-// `stream` to finish before it returns (it synchronises the stream). Calls share the
+// cudaGetSymbolAddress, with that device current. Every call reads two sizes back from
+// the device and waits for `stream` to finish before it returns (it synchronises the
+// stream), so no call can be captured into a CUDA graph: on a stream being captured the
+// call is rejected before any device work. Calls share the
 // array and it keeps the last call's contents, so each call clears what must start at
 // zero; calls that overlap on the GPU (two streams, or two host threads) race on it
 // and must be serialised by the caller.
@@ -120,6 +121,13 @@ extern "C" cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t n
     }
     try {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CMG_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+            set_err(errbuf, errbuf_len,
+                    "cmg_gpu_occupancy_static: the call synchronises its stream, which is being captured");
+            return CMG_ERR_UNSUPPORTED_OPTION;
+        }
         int dev = 0;
         CMG_CUDA(cudaGetDevice(&dev));
         if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("device ordinal out of range");

@@ -359,12 +359,13 @@ void cmg_host_free(void* p);
  * bytes, idx = (k*ny + j)*nx + i) and all working memory taken from a fixed 32 MiB
  * array in device memory that the library holds on every GPU it is loaded on.
  * Allocates nothing. Inputs that need more working memory than the array holds
- * are rejected with CMG_ERR_INVALID_INPUT and a message. The first call on a device
- * resolves the array's address (make it before any stream capture); calls share
- * the array, so calls that overlap on the GPU race and must be serialised.
+ * are rejected with CMG_ERR_INVALID_INPUT and a message. Calls share the array, so
+ * calls that overlap on the GPU race and must be serialised.
  * `stream` is a cudaStream_t (NULL for the default stream); the call reads two
  * sizes back from the device and synchronises `stream`, so it returns after the
- * work on it has finished. predicates: CMG_PRED_COMPAT or
+ * work on it has finished, and it cannot be part of a CUDA graph: on a stream that
+ * is being captured it returns CMG_ERR_UNSUPPORTED_OPTION before any device work.
+ * predicates: CMG_PRED_COMPAT or
  * CMG_PRED_EXACT. The result equals cmg_plc_voxelize_ex's occupancy. */
 cmg_status cmg_gpu_occupancy_static(const double* d_points, int64_t npoints,
                                     const int* d_triangles, int64_t ntriangles,

@@ -53,3 +53,40 @@ def test_static_scratch_rejects_oversized_input(cm, golden):
     st, msg, _ = _call(cm, torch, g["points"], g["triangles"], g["corner"], float(g["spacing"]),
                        (4096, 4096, 1))
     assert st == 1 and "static scratch" in msg
+
+
+def test_static_scratch_rejects_a_stream_being_captured(cm, golden):
+    """The call synchronises its stream, so on a stream being captured into a CUDA graph
+    it returns CMG_ERR_UNSUPPORTED_OPTION before any device work: the capture goes on
+    (its graph replays), and the next call on an ordinary stream is correct."""
+    torch = pytest.importorskip("torch")
+    from cybermeshgenerator_gb300 import _lib as L
+    lib = L.load()
+    g = golden("cube4_r16p1")
+    d_pts = torch.tensor(np.ascontiguousarray(g["points"], np.float64), device="cuda")
+    d_tri = torch.tensor(np.ascontiguousarray(g["triangles"], np.int32), device="cuda")
+    dims = np.ascontiguousarray(g["dims"], np.int32)
+    corner = np.ascontiguousarray(g["corner"], np.float64)
+    d_occ = torch.zeros(int(np.prod(dims)), dtype=torch.uint8, device="cuda")
+    x = torch.zeros(16, device="cuda")
+    err = ctypes.create_string_buffer(256)
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        graph.capture_begin()
+        st = lib.cmg_gpu_occupancy_static(
+            ctypes.c_void_p(d_pts.data_ptr()), len(g["points"]), ctypes.c_void_p(d_tri.data_ptr()),
+            len(g["triangles"]), corner.ctypes.data_as(L.c_double_p), float(g["spacing"]),
+            dims.ctypes.data_as(L.c_int_p), 0, ctypes.c_void_p(d_occ.data_ptr()),
+            ctypes.c_void_p(side.cuda_stream), err, 256)
+        x.add_(1.0)
+        graph.capture_end()
+    assert st == 3 and "being captured" in err.value.decode()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(x[0].item()) == 1.0
+    st, msg, got = _call(cm, torch, g["points"], g["triangles"], corner, float(g["spacing"]),
+                         tuple(int(v) for v in dims))
+    assert st == 0, msg
+    assert np.array_equal(got, unpack_occ(g))
